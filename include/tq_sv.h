@@ -1,0 +1,236 @@
+/*
+ * tq_sv.h -- C ABI of the tyxonq_gb300 statevector library (libtyxonq_gb300.so).
+ *
+ * One GB300, one process.  Every entry point takes raw device pointers,
+ * plain integers and a CUDA stream (passed as void*, NULL = legacy default
+ * stream), enqueues its kernels on that stream and returns without
+ * synchronising.  The caller owns every buffer: the library never allocates
+ * or frees device memory on these paths.  Buffers that a call needs beyond its
+ * inputs and outputs ("workspace") are passed in by the caller; the matching
+ * *_workspace_bytes() query gives the size.
+ *
+ * Return convention: TQ_OK (0) on success, a negative TQ_ERR_* code on
+ * failure; tq_last_error() copies a message for the last failure on the
+ * calling thread.  Calls are thread-compatible: different threads may use
+ * different streams concurrently.
+ *
+ * Basis ordering is the reference engine's big-endian convention: qubit 0 is
+ * the most significant bit of the basis index
+ * (tyxonq/libs/quantum_library/kernels/statevector.py:32,49;
+ *  tyxonq/devices/simulators/statevector/engine.py:454,1050-1057).
+ * Amplitudes are interleaved (re, im): TQ_C64 = float2, TQ_C128 = double2.
+ * Matrices are passed as host arrays of doubles, row-major, (re, im)
+ * interleaved; multi-qubit matrix indices take the FIRST listed qubit as the
+ * most significant bit (statevector.py:53-56, gates.py:265-284).
+ */
+#ifndef TQ_SV_H
+#define TQ_SV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define TQ_API __attribute__((visibility("default")))
+#else
+#define TQ_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TQ_C64 0
+#define TQ_C128 1
+
+#define TQ_MAX_QUBITS 34
+#define TQ_MAX_KQ 5
+
+#define TQ_OK 0
+#define TQ_ERR_ARG (-1)
+#define TQ_ERR_CUDA (-2)
+#define TQ_ERR_RANGE (-3)
+#define TQ_ERR_TIMEOUT (-4)
+#define TQ_ERR_WORKSPACE (-5)
+#define TQ_ERR_UNSUPPORTED (-6)
+
+/* ------------------------------------------------------------ library */
+
+/* Library ABI version (major*100 + minor). */
+TQ_API int tq_version(void);
+
+/* Copies the last error message of the calling thread into buf (always
+ * NUL-terminated when len > 0).  Returns the last error code. */
+TQ_API int tq_last_error(char* buf, size_t len);
+
+/* ------------------------------------------------------------ state preparation */
+
+/* |basis_index> over n qubits.  Replaces init_statevector
+ * (tyxonq/libs/quantum_library/kernels/statevector.py:19-25), which builds
+ * |0...0>; basis_index generalises it to the Hartree-Fock bitstrings built by
+ * get_init_circuit (chem_libs/quantum_chem_library/statevector_ops.py:172-199). */
+TQ_API int tq_sv_init_basis(void* psi, int n, int dtype, int64_t basis_index, void* stream);
+
+/* ------------------------------------------------------------ single gates (plain engine) */
+
+/* Dense 2x2 on `qubit`.  Replaces apply_1q_statevector (statevector.py:28-42).
+ * u: 8 doubles = [[u00,u01],[u10,u11]] as (re,im) pairs. */
+TQ_API int tq_sv_apply_1q(void* psi, int n, int dtype, int qubit, const double* u, void* stream);
+
+/* Diagonal 1q gate diag(d0, d1); d: 4 doubles.  Fast path of
+ * apply_1q_statevector for rz/s/sdg/t/tdg/z/phase (gates.py:19-35,68-79,180-200).
+ * When d0 == 1 only the |1> half of the state is read and written. */
+TQ_API int tq_sv_apply_diag1(void* psi, int n, int dtype, int qubit, const double* d, void* stream);
+
+/* Dense 4x4 on (q0, q1), q0 = high bit of the matrix index.  Replaces
+ * apply_2q_statevector (statevector.py:45-59); q0 == q1 is a no-op as there
+ * (statevector.py:46-47).  u: 32 doubles. */
+TQ_API int tq_sv_apply_2q(void* psi, int n, int dtype, int q0, int q1, const double* u, void* stream);
+
+/* CX / CZ / SWAP fast paths of apply_2q_statevector with gate_cx_4x4,
+ * gate_cz_4x4, gate_swap_4x4 (gates.py:82-161). q0 == q1 is a no-op. */
+TQ_API int tq_sv_apply_cx(void* psi, int n, int dtype, int control, int target, void* stream);
+TQ_API int tq_sv_apply_cz(void* psi, int n, int dtype, int q0, int q1, void* stream);
+TQ_API int tq_sv_apply_swap(void* psi, int n, int dtype, int q0, int q1, void* stream);
+
+/* Dense 2^k x 2^k unitary on k <= TQ_MAX_KQ distinct qubits, qubits[0] = most
+ * significant bit of the matrix index.  Replaces apply_kqubit_unitary
+ * (statevector.py:71-129).  u: 2*4^k doubles (host). */
+TQ_API int tq_sv_apply_kq(void* psi, int n, int dtype, const int* qubits, int k, const double* u, void* stream);
+
+/* exp(-i theta/2 P) for a Pauli string P given as bit masks over basis-index
+ * bits (x_mask = bits carrying X or Y, z_mask = bits carrying Y or Z).  One pass
+ * over the state; equals the gate sequence of evolve_pauli_ops
+ * (tyxonq/libs/circuits_library/utils.py:29-59) up to rounding. */
+TQ_API int tq_sv_apply_pauli_rotation(void* psi, int n, int dtype, uint64_t x_mask, uint64_t z_mask,
+                               double theta, void* stream);
+
+/* psi <- (re + i im) * psi.  Used for the renormalisation after a Z projection
+ * (engine.py:1075-1086, _project_z). */
+TQ_API int tq_sv_scale(void* psi, int n, int dtype, double re, double im, void* stream);
+
+/* ------------------------------------------------------------ measurement */
+
+/* <Z_q> for every qubit q in [0, n): out_dev[q] (device, n doubles).
+ * Replaces expect_z_statevector (statevector.py:62-68) and the per-qubit loop
+ * of engine.py:467-473 with one pass.  FP64 accumulation. */
+TQ_API size_t tq_sv_expect_z_workspace_bytes(int n);
+TQ_API int tq_sv_expect_z_all(const void* psi, int n, int dtype, double* out_dev, void* ws,
+                       size_t ws_bytes, void* stream);
+
+/* probs[i] = |psi_i|^2 (float for TQ_C64, double for TQ_C128).  Replaces
+ * engine.py:377-379 / probability() engine.py:1041-1047. */
+TQ_API int tq_sv_probabilities(const void* psi, int n, int dtype, void* probs, void* stream);
+
+/* Squared norm sum_i |psi_i|^2 into *out_dev (FP64). */
+TQ_API size_t tq_sv_norm_workspace_bytes(int n);
+TQ_API int tq_sv_norm2(const void* psi, int n, int dtype, double* out_dev, void* ws, size_t ws_bytes,
+                void* stream);
+
+/* Z-basis shot sampling from exact probabilities: out_indices[0..shots) gets
+ * basis indices drawn i.i.d. from |psi_i|^2 / sum|psi|^2, returned in
+ * ascending order (counts are their run lengths).  Replaces
+ * nb.choice + bincount of engine.py:381-418.  Counter-based RNG (Philox4x32-10,
+ * Salmon et al. SC'11) keyed by `seed`: the same seed gives the same shots. */
+TQ_API size_t tq_sv_sample_workspace_bytes(int n, int64_t shots);
+TQ_API int tq_sv_sample(const void* psi, int n, int dtype, int64_t shots, uint64_t seed,
+                 int64_t* out_indices, void* ws, size_t ws_bytes, void* stream);
+
+/* ------------------------------------------------------------ Pauli sums */
+
+/* A Pauli-sum Hamiltonian H = sum_k c_k P_k in flip-mask groups.
+ * Term k: P_k |i> = i^{ny_k} (-1)^{popc(i & zy_k)} |i ^ flip>, with
+ * flip = bits carrying X or Y, zy = bits carrying Y or Z, ny = #Y.
+ * weight = c_k * i^{ny_k} (complex: one of re/im is zero).
+ * Groups are contiguous term ranges sharing one flip mask.  Tables live in
+ * device memory.  Semantics equal pauli_string_to_matrix / pauli_string_sum_dense
+ * (tyxonq/libs/quantum_library/kernels/pauli.py:65-87) without forming 4^n. */
+typedef struct {
+  uint64_t flip;
+  int32_t first_term;
+  int32_t n_terms;
+} tq_pauli_group;
+
+typedef struct {
+  uint64_t zy;
+  double w_re;
+  double w_im;
+} tq_pauli_term;
+
+/* E = <psi|H|psi> (real part) into *out_dev, FP64 accumulation, deterministic.
+ * Replaces dynamics.expectation(psi, pauli_string_sum_dense(...))
+ * (tyxonq/libs/quantum_library/dynamics.py:117-126). */
+TQ_API size_t tq_sv_pauli_expectation_workspace_bytes(int n, int n_groups);
+TQ_API int tq_sv_pauli_expectation(const void* psi, int n, int dtype, const tq_pauli_group* groups,
+                            int n_groups, const tq_pauli_term* terms, int n_terms,
+                            double* out_dev, void* ws, size_t ws_bytes, void* stream);
+
+/* out = H psi (out must not alias psi).  Replaces apply_op
+ * (chem_libs/hamiltonians_chem_library/hamiltonian_builders.py:283-318) without
+ * densifying H. */
+TQ_API int tq_sv_apply_pauli_sum(const void* psi, void* out, int n, int dtype, const tq_pauli_group* groups,
+                          int n_groups, const tq_pauli_term* terms, int n_terms, void* stream);
+
+/* ------------------------------------------------------------ fused tile passes */
+
+/* A gate program executed as shared-memory tile passes.  Pass p names t local
+ * bit positions pos[0..t) (ascending; pos[j] == j for j < nlow so global reads
+ * come in runs of 2^nlow contiguous amplitudes).  The state is cut into
+ * 2^(n-t) tiles of 2^t amplitudes (one tile = one value of the non-local
+ * bits); each tile is read once, ops[op_begin..op_end) are applied to it in
+ * shared memory, and it is written back once.  Op bit positions and masks are
+ * LOCAL (0..t-1).  This replaces the reference's per-op interpreter loop
+ * (engine.py:52-374 / :914-1039), which touches the whole state for every gate.
+ *
+ * Gradient fields (adjoint only): slot >= 0 marks a parametrised op whose
+ * derivative dU/dtheta = -i/2 G U contributes Im <lam|G|psi> to slot_out[slot],
+ * with G|i> = [i & gcm == gcm] i^gny (-1)^{popc(i & gzm)} |i ^ gxm>. */
+#define TQ_TILE_MAX_BITS 16
+
+typedef struct {
+  int32_t kind; /* 1 dense2x2, 2 diag2x2, 3 dense4x4, 4 CX, 5 CZ, 6 SWAP, 7 Pauli rotation */
+  int32_t a;    /* local bit of the first qubit (matrix high bit / control) */
+  int32_t b;    /* local bit of the second qubit (matrix low bit / target) */
+  int32_t slot; /* gradient slot, -1 = none */
+  uint32_t xm, zm;          /* Pauli-rotation masks (kind 7): m[0] = cos, m[1] = -i sin * i^ny */
+  uint32_t gxm, gzm, gcm;   /* generator masks (slot >= 0) */
+  int32_t gny;              /* number of Y factors in the generator */
+  float mf[32];             /* matrix, complex64 kernels: row-major (re, im) */
+  double md[32];            /* matrix, complex128 kernels */
+} tq_tile_op;
+
+typedef struct {
+  int32_t t;
+  int32_t nlow;
+  int32_t op_begin;
+  int32_t op_end;
+  int32_t pos[TQ_TILE_MAX_BITS];
+} tq_tile_pass;
+
+/* Largest t supported for a dtype (shared-memory capacity). */
+TQ_API int tq_sv_tile_max_bits(int dtype);
+
+/* Forward: apply passes[0..n_passes) in order.  passes: host array; ops: device. */
+TQ_API int tq_sv_run_tiles(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
+                           const tq_tile_op* ops, void* stream);
+
+/* Adjoint reverse sweep over passes (already in reverse order, ops in each pass
+ * in reverse application order): for each op, first the gradient term (slot >= 0)
+ * on (psi, lam), then psi <- U^dag psi, lam <- U^dag lam.  slot_out: device,
+ * n_slots doubles (FP64, overwritten).  Follows the reverse loop of the
+ * reference's CI-space adjoint energy_and_grad_civector
+ * (chem_libs/quantum_chem_library/civector_ops.py:141-200). */
+TQ_API size_t tq_sv_adjoint_tiles_workspace_bytes(int n, int n_slots);
+TQ_API int tq_sv_adjoint_tiles(void* psi, void* lam, int n, int dtype, const tq_tile_pass* passes, int n_passes,
+                               const tq_tile_op* ops, int n_slots, double* slot_out, void* ws, size_t ws_bytes,
+                               void* stream);
+
+/* Re <a|b> into *out_dev (FP64), used by energy = <psi|H psi>. */
+TQ_API size_t tq_sv_inner_workspace_bytes(int n);
+TQ_API int tq_sv_inner_re(const void* a, const void* b, int n, int dtype, double* out_dev, void* ws,
+                   size_t ws_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TQ_SV_H */

@@ -1,0 +1,125 @@
+"""The CPU oracle reproduces the reference's own outputs (golden vectors) and
+the known answers of the reference's tests.  CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import sv
+from tests import golden_data
+
+
+@pytest.mark.parametrize("case", golden_data.circuit_cases(), ids=lambda c: c[0])
+def test_state_and_run_z(case):
+    name, n, ops, ucache, ref_state, ref_z = case
+    psi, _ = sv.run_ops(n, ops, mode="state", unitary_cache=ucache)
+    np.testing.assert_allclose(psi, ref_state, atol=1e-12, rtol=0)
+    psi_run, _ = sv.run_ops(n, ops, mode="run", unitary_cache=ucache)
+    z = [sv.expect_z(psi_run, q, n) for q in range(n)]
+    np.testing.assert_allclose(z, ref_z, atol=1e-12, rtol=0)
+
+
+def test_kqubit_unitary():
+    arrays, meta = golden_data.load()
+    for c in meta["kq"]:
+        k = c["k"]
+        out = sv.apply_kq(arrays[f"kq{k}_in"], arrays[f"kq{k}_u"], c["qubits"], c["n"])
+        np.testing.assert_allclose(out, arrays[f"kq{k}_out"], atol=1e-13, rtol=0)
+
+
+def test_pauli_energy_and_hpsi():
+    arrays, meta = golden_data.load()
+    for c in meta["pauli"]:
+        nm = c["name"]
+        codes, w, psi = arrays[f"{nm}_codes"], arrays[f"{nm}_w"], arrays[f"{nm}_psi"]
+        assert abs(sv.pauli_expectation(psi, codes, w) - c["energy"]) < 1e-12
+        np.testing.assert_allclose(sv.apply_pauli_sum(psi, codes, w), arrays[f"{nm}_hpsi"], atol=1e-12)
+
+
+def hea12_ops(theta):
+    n, L = 12, 4
+    ops = []
+    for l in range(L):
+        for q in range(n):
+            ops.append(("ry", q, float(theta[l * n + q])))
+        for q in range(n - 1):
+            ops.append(("cx", q, q + 1))
+    return ops
+
+
+def test_hea12_energy_and_autograd_gradient():
+    arrays, meta = golden_data.load()
+    theta = arrays["hea12_theta"].reshape(-1)
+    codes, w = arrays["hea12_codes"], arrays["hea12_w"]
+    psi, _ = sv.run_ops(12, hea12_ops(theta))
+    np.testing.assert_allclose(psi, arrays["hea12_state"], atol=1e-12, rtol=0)
+    e = sv.pauli_expectation(psi, codes, w)
+    assert abs(e - 0.1195334104542979) < 1e-12
+    assert abs(e - meta["hea12"]["energy_pytorch"]) < 1e-12
+    gates = []
+    for l in range(4):
+        for q in range(12):
+            gates.append(("ry", [q], l * 12 + q, 1.0))
+        for q in range(11):
+            gates.append(("cx", [q, q + 1], None, 1.0))
+    e2, g = sv.grad_adjoint(12, gates, theta, codes, w)
+    assert abs(e2 - e) < 1e-12
+    np.testing.assert_allclose(g, arrays["hea12_grad_autograd"].reshape(-1), atol=1e-10)
+
+
+def test_reference_known_answers():
+    # Bell: <Z>=0, norm 1 (test_devices_simulators_gates.py:17-30)
+    psi, _ = sv.run_ops(2, [("h", 0), ("cx", 0, 1)])
+    assert abs(np.vdot(psi, psi) - 1) < 1e-12
+    assert abs(sv.expect_z(psi, 0, 2)) < 1e-12
+    # big-endian: h(0) on 2 qubits -> p[0] + p[2] = 1 (test_statevector_engine_probs.py:15-17)
+    p = sv.probabilities(sv.run_ops(2, [("h", 0)])[0])
+    assert abs(p[0] + p[2] - 1) < 1e-12
+    # <X> on |+> = 1; ZZ, XX on Bell = 1; TFIM |+++> = -3 (test_circuit_expectation.py)
+    plus, _ = sv.run_ops(1, [("h", 0)])
+    assert abs(sv.pauli_expectation(plus, np.array([[1]]), np.array([1.0])) - 1) < 1e-10
+    assert abs(sv.pauli_expectation(psi, np.array([[3, 3]]), np.array([1.0])) - 1) < 1e-10
+    assert abs(sv.pauli_expectation(psi, np.array([[1, 1]]), np.array([1.0])) - 1) < 1e-10
+    ppp, _ = sv.run_ops(3, [("h", 0), ("h", 1), ("h", 2)])
+    codes, w = sv.terms_to_codes(3, [(-1.0, [("X", i)]) for i in range(3)] + [(1.0, [("Z", 0), ("Z", 1)]), (1.0, [("Z", 1), ("Z", 2)])])
+    assert abs(sv.pauli_expectation(ppp, codes, w) + 3) < 1e-10
+    # <Z> after RX(0.5) = cos 0.5 (test_circuit_state_autograd.py:84-102)
+    r, _ = sv.run_ops(1, [("rx", 0, 0.5)])
+    assert abs(sv.expect_z(r, 0, 1) - math.cos(0.5)) < 1e-12
+    # projection / reset (test_mid_measure_postselect.py:9-16)
+    s, m = sv.run_ops(2, [("h", 0), ("project_z", 0, 0), ("reset", 1), ("measure_z", 0), ("measure_z", 1)], mode="run")
+    assert abs(sv.expect_z(s, 0, 2) - 1) < 1e-12 and abs(sv.expect_z(s, 1, 2) - 1) < 1e-12
+
+
+def test_gradient_oracles_agree():
+    rng = np.random.default_rng(5)
+    n = 5
+    theta = rng.uniform(0, 2 * np.pi, 2 * n)
+    from tyxonq_gb300.hamiltonian import random_pauli_sum
+
+    H = random_pauli_sum(n, 20, rng)
+
+    def ops_fn(t):
+        ops = [("ry", q, float(t[q])) for q in range(n)]
+        ops += [("cx", q, q + 1) for q in range(n - 1)]
+        ops += [("rz", q, float(t[n + q])) for q in range(n)]
+        return ops
+
+    gates = [("ry", [q], q, 1.0) for q in range(n)] + [("cx", [q, q + 1], None, 1.0) for q in range(n - 1)] + [
+        ("rz", [q], n + q, 1.0) for q in range(n)]
+    e, g = sv.grad_adjoint(n, gates, theta, H.codes, H.coeffs)
+    gfd = sv.grad_central_fd(n, ops_fn, theta, H.codes, H.coeffs)
+    gps = sv.grad_param_shift(n, ops_fn, theta, H.codes, H.coeffs)
+    np.testing.assert_allclose(g, gps, atol=1e-12)
+    np.testing.assert_allclose(g, gfd, atol=1e-7)
+
+
+def test_chi2_sampler_check_is_sensitive():
+    rng = np.random.default_rng(3)
+    psi, _ = sv.run_ops(4, [("h", 0), ("ry", 1, 0.3), ("cx", 0, 2), ("rx", 3, 1.1)])
+    p = sv.probabilities(psi)
+    good = sv.sample_counts(psi, 20000, rng)
+    assert sv.chi2_pvalue(good, p) > 1e-4
+    # a planted mistake in the oracle side: sample from the wrong distribution
+    bad = sv.sample_counts(sv.run_ops(4, [("h", 0), ("ry", 1, 0.5), ("cx", 0, 2), ("rx", 3, 1.1)])[0], 20000, rng)
+    assert sv.chi2_pvalue(bad, p) < 1e-6

@@ -1,0 +1,241 @@
+"""Adjoint (reverse-sweep) energy gradients on the GPU.
+
+For psi = U_G ... U_1 |psi0> and E = <psi|H|psi>:
+  forward:  psi (fused tile passes), lam = H psi, E = Re <psi|lam>;
+  reverse:  for g = G..1: dE/dtheta_g += coef_g * Im <lam|G_g|psi>, then
+            psi <- U_g^dag psi, lam <- U_g^dag lam,
+which is the reference's CI-space reverse loop (energy_and_grad_civector,
+chem_libs/quantum_chem_library/civector_ops.py:141-200) generalised to gates
+and Pauli rotations.  The reverse sweep runs as adjoint tile passes
+(``tq_sv_adjoint_tiles``) carrying psi and lam together, gradient reductions
+fused in.  ``AdjointEnergy`` wraps it as a torch.autograd.Function, the
+replacement for the reference's autograd through per-gate einsums
+(numerics/backends/pytorch_backend.py:446-564).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Any, Sequence
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from . import kernels as K
+from .hamiltonian import PauliSum, as_pauli_sum
+from .ir import Gate, lower_ops
+from .program import DEFAULT_NLOW, _canon, compile_forward, encode_passes, plan_passes, tileable
+
+
+@dataclass
+class ParamGate:
+    """Gate whose angle = scale * theta[param] + shift (param None = fixed)."""
+
+    gate: Gate
+    param: int | None = None
+    scale: float = 1.0
+
+
+@dataclass
+class AdjointProgram:
+    n: int
+    dtype: torch.dtype
+    forward: Any
+    reverse: list  # ('tiles', EncodedTiles) | ('gate', Gate)
+    n_slots: int
+    slot_param: np.ndarray  # slot -> param index
+    slot_coef: np.ndarray  # slot -> coef * scale
+    n_params: int
+
+
+def _build(pgates: Sequence[ParamGate], n: int, n_params: int, dtype, t_fwd=None, t_adj=None) -> AdjointProgram:
+    from .autotune import tile_bits_for
+
+    gates = [_canon(p.gate) for p in pgates]
+    for g in gates:
+        if not tileable(g):
+            raise NotImplementedError(f"adjoint gradient through a '{g.kind}' gate is not supported")
+    fwd = compile_forward(gates, n, dtype, t=t_fwd)
+    t_adj = t_adj or tile_bits_for(n, dtype, adjoint=True)
+    segs = plan_passes(list(reversed(gates)), n, t_adj, DEFAULT_NLOW)
+    # plan_passes on the reversed list gives the reverse sweep order directly;
+    # indices refer to the reversed list.
+    rgates = list(reversed(gates))
+    slots = {}
+    slot_param = []
+    slot_scale = []
+    G = len(gates)
+    for ri, g in enumerate(rgates):
+        pg = pgates[G - 1 - ri]
+        if pg.param is not None:
+            slots[ri] = len(slot_param)
+            slot_param.append(pg.param)
+            slot_scale.append(pg.scale)
+    rev = []
+    coef = np.zeros(len(slot_param))
+    for s in segs:
+        if s.kind == "gate":  # pragma: no cover - tileable check above
+            raise NotImplementedError
+        enc, coefs = encode_passes(n, s.passes, rgates, fuse=False, reverse=False, slots=slots)
+        for sl, c in coefs:
+            coef[sl] = c
+        rev.append(("tiles", enc))
+    return AdjointProgram(n, dtype, fwd, rev, len(slot_param), np.asarray(slot_param, dtype=np.int64),
+                          coef * np.asarray(slot_scale, dtype=np.float64), n_params)
+
+
+def _with_angles(pgates: Sequence[ParamGate], theta: np.ndarray) -> list[ParamGate]:
+    """Rebuild parametrised gate matrices for new angles."""
+    from .ir import _rot_gate, pauli_rotation
+
+    out = []
+    for p in pgates:
+        if p.param is None:
+            out.append(p)
+            continue
+        a = p.scale * float(theta[p.param])
+        g = p.gate
+        if g.kind == "prot":
+            ng = pauli_rotation(g.pauli, a)
+        elif g.rot is not None and g.rot[0] == "phase":
+            ng = Gate("d1", g.qubits, np.diag([1.0, np.exp(1j * a)]), rot=("phase", a, a))
+        else:
+            ng = _rot_gate(g.rot[0], g.qubits, a)
+        out.append(ParamGate(ng, p.param, p.scale))
+    return out
+
+
+def reverse_sweep(prog: AdjointProgram, psi: torch.Tensor, lam: torch.Tensor) -> torch.Tensor:
+    """Run the adjoint passes in place on (psi, lam); returns slot values (device, FP64)."""
+    dt = K.dtype_tag(psi)
+    out = torch.zeros(max(prog.n_slots, 1), dtype=torch.float64, device=psi.device)
+    lib = nat.load()
+    for kind, enc in prog.reverse:
+        ops = enc.device_ops(psi.device)
+        # slots of this segment only are written; other segments' slots must be kept
+        seg_out = torch.empty_like(out)
+        p, cap = K._ws(lib.tq_sv_adjoint_tiles_workspace_bytes(prog.n, prog.n_slots), psi.device)
+        nat.call("tq_sv_adjoint_tiles", ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), prog.n, dt,
+                 enc.passes, enc.n_passes, ctypes.c_void_p(ops.data_ptr()), prog.n_slots,
+                 ctypes.c_void_p(seg_out.data_ptr()), p, cap, K.stream_ptr(psi.device))
+        out += seg_out
+    return out[: prog.n_slots]
+
+
+def slots_to_grad(prog: AdjointProgram, slot_vals: np.ndarray) -> np.ndarray:
+    g = np.zeros(prog.n_params, dtype=np.float64)
+    np.add.at(g, prog.slot_param, prog.slot_coef * slot_vals)
+    return g
+
+
+class AdjointEstimator:
+    """Energy and adjoint gradient of one parametrised circuit and Pauli sum.
+
+    `pgates` fixes the structure; angles come from theta at each call.  The
+    structure (pass plans) is compiled once and reused across calls.
+    """
+
+    def __init__(self, n: int, pgates: Sequence[ParamGate], n_params: int, hamiltonian, dtype=torch.complex64,
+                 device="cuda", init_basis: int = 0):
+        self.n = int(n)
+        self.pgates = list(pgates)
+        self.n_params = int(n_params)
+        self.H = as_pauli_sum(hamiltonian, self.n)
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self.init_basis = int(init_basis)
+        self._lam = None
+
+    def _program(self, theta):
+        pg = _with_angles(self.pgates, np.asarray(theta, dtype=np.float64))
+        return _build(pg, self.n, self.n_params, self.dtype)
+
+    def state(self, theta) -> torch.Tensor:
+        prog = self._program(theta)
+        psi = K.init_statevector(self.n, self.dtype, self.device, self.init_basis)
+        return prog.forward.run(psi)
+
+    def energy(self, theta) -> float:
+        psi = self.state(theta)
+        return float(K.pauli_expectation(psi, self.H).item())
+
+    def energy_and_grad(self, theta) -> tuple[float, np.ndarray]:
+        prog = self._program(theta)
+        psi = K.init_statevector(self.n, self.dtype, self.device, self.init_basis)
+        prog.forward.run(psi)
+        lam = K.apply_pauli_sum(psi, self.H)
+        e = K.inner_re(psi, lam)
+        sv = reverse_sweep(prog, psi, lam)
+        e_h = float(e.item())
+        return e_h, slots_to_grad(prog, sv.cpu().numpy())
+
+
+class AdjointEnergy(torch.autograd.Function):
+    """E(theta) with an adjoint-kernel backward: use as AdjointEnergy.apply(theta, estimator)."""
+
+    @staticmethod
+    def forward(ctx, theta: torch.Tensor, est: AdjointEstimator):
+        e, g = est.energy_and_grad(theta.detach().cpu().numpy())
+        ctx.save_for_backward(torch.as_tensor(g, dtype=theta.dtype, device=theta.device))
+        return torch.tensor(e, dtype=theta.dtype, device=theta.device)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (g,) = ctx.saved_tensors
+        return gout * g, None
+
+
+# ---------------------------------------------------------------- circuit-level autograd
+def _angle_leaves(circuit) -> tuple[list, list]:
+    """(angle tensors requiring grad, (op index, arg position) for each)."""
+    leaves, where = [], []
+    for oi, op in enumerate(getattr(circuit, "ops", [])):
+        if isinstance(op, (list, tuple)):
+            for ai, a in enumerate(op[1:], start=1):
+                if isinstance(a, torch.Tensor) and a.requires_grad:
+                    leaves.append(a)
+                    where.append((oi, ai))
+    return leaves, where
+
+
+class _StateFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, engine, circuit, pgates, n, *angles):
+        prog = _build(pgates, n, len(angles), engine.dtype)
+        psi = K.init_statevector(n, engine.dtype, engine.device)
+        prog.forward.run(psi)
+        ctx.prog = prog
+        ctx.save_for_backward(psi.clone())
+        ctx.n_angles = len(angles)
+        return psi
+
+    @staticmethod
+    def backward(ctx, gout):
+        (psi,) = ctx.saved_tensors
+        prog = ctx.prog
+        lam = gout.detach().to(dtype=psi.dtype).contiguous().clone()
+        ps = psi.clone()
+        sv = reverse_sweep(prog, ps, lam).cpu().numpy()
+        g = 0.5 * slots_to_grad(prog, sv)  # dL/dtheta = 1/2 Im<grad|G|psi>
+        grads = [torch.tensor(float(x), dtype=torch.float64, device=gout.device) for x in g]
+        return (None, None, None, None, *grads)
+
+
+def state_with_grad(engine, circuit) -> torch.Tensor:
+    """Final state as a differentiable function of the circuit's tensor angles."""
+    n = int(circuit.num_qubits)
+    if getattr(circuit, "_initial_state", None) is not None:
+        raise NotImplementedError("autograd with a custom initial state")
+    gates, _ = lower_ops(circuit, mode="state", extended=engine.extended_gates)
+    leaves, where = _angle_leaves(circuit)
+    leaf_id = {id(t): k for k, t in enumerate(leaves)}
+    pgates = []
+    for g in gates:
+        src = g.rot[2] if g.rot is not None else None
+        if isinstance(src, torch.Tensor) and id(src) in leaf_id:
+            pgates.append(ParamGate(g, leaf_id[id(src)], 1.0))
+        else:
+            pgates.append(ParamGate(g, None))
+    out = _StateFn.apply(engine, circuit, pgates, n, *leaves)
+    return out

@@ -1,0 +1,314 @@
+// Fused gate programs as shared-memory tile passes (forward and adjoint).
+//
+// Per pass, every tile (2^t amplitudes sharing the non-local bits) is read
+// from HBM once with 128-bit loads in runs of 2^nlow contiguous amplitudes,
+// all the pass's gates are applied in shared memory, and the tile is written
+// back once: algorithmic bytes 2*N*S per pass (4*N*S for the adjoint pass,
+// which carries psi and lambda), however many gates the pass holds.
+#include "tile.cuh"
+
+namespace tq {
+
+static const int kTileGridCap = 152 * 8;
+
+struct PassArgs {
+  int t, nlow;
+  int op_begin, op_end;
+  int pos[TQ_TILE_MAX_BITS];
+};
+
+static PassArgs to_args(const tq_tile_pass& p) {
+  PassArgs a;
+  a.t = p.t;
+  a.nlow = p.nlow;
+  a.op_begin = p.op_begin;
+  a.op_end = p.op_end;
+  for (int i = 0; i < TQ_TILE_MAX_BITS; ++i) a.pos[i] = p.pos[i];
+  return a;
+}
+
+// hoff[h] = global offset of local index (h << nlow).
+__device__ __forceinline__ void build_hoff(int64_t* hoff, const PassArgs& P) {
+  const int nh = 1 << (P.t - P.nlow);
+  for (int h = threadIdx.x; h < nh; h += blockDim.x) {
+    int64_t off = 0;
+    for (int k = 0; k < P.t - P.nlow; ++k)
+      if ((h >> k) & 1) off |= int64_t(1) << P.pos[P.nlow + k];
+    hoff[h] = off;
+  }
+}
+
+__device__ __forceinline__ int64_t tile_base(int64_t g, const PassArgs& P) {
+  int64_t x = g << P.nlow;
+  for (int k = P.nlow; k < P.t; ++k) x = insert_zero(x, P.pos[k]);
+  return x;
+}
+
+// Tile <-> global copies.  complex64 moves two amplitudes per 16-byte access.
+template <typename R>
+__device__ __forceinline__ void tile_load(cplx<R>* s, const typename C2<R>::T* psi, int64_t base, const int64_t* hoff,
+                                          const PassArgs& P);
+template <>
+__device__ __forceinline__ void tile_load<float>(cplx<float>* s, const float2* psi, int64_t base, const int64_t* hoff,
+                                                 const PassArgs& P) {
+  const int nv = 1 << (P.t - 1);
+  const int lm = (1 << P.nlow) - 1;
+  const float4* g4 = reinterpret_cast<const float4*>(psi);
+  float4* s4 = reinterpret_cast<float4*>(s);
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    const int j = 2 * v;
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    s4[v] = g4[gi >> 1];
+  }
+}
+template <>
+__device__ __forceinline__ void tile_load<double>(cplx<double>* s, const double2* psi, int64_t base,
+                                                  const int64_t* hoff, const PassArgs& P) {
+  const int N = 1 << P.t;
+  const int lm = (1 << P.nlow) - 1;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    const double2 v = psi[base + hoff[j >> P.nlow] + (j & lm)];
+    s[j] = cplx<double>(v.x, v.y);
+  }
+}
+template <typename R>
+__device__ __forceinline__ void tile_store(const cplx<R>* s, typename C2<R>::T* psi, int64_t base, const int64_t* hoff,
+                                           const PassArgs& P);
+template <>
+__device__ __forceinline__ void tile_store<float>(const cplx<float>* s, float2* psi, int64_t base, const int64_t* hoff,
+                                                  const PassArgs& P) {
+  const int nv = 1 << (P.t - 1);
+  const int lm = (1 << P.nlow) - 1;
+  float4* g4 = reinterpret_cast<float4*>(psi);
+  const float4* s4 = reinterpret_cast<const float4*>(s);
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    const int j = 2 * v;
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    g4[gi >> 1] = s4[v];
+  }
+}
+template <>
+__device__ __forceinline__ void tile_store<double>(const cplx<double>* s, double2* psi, int64_t base,
+                                                   const int64_t* hoff, const PassArgs& P) {
+  const int N = 1 << P.t;
+  const int lm = (1 << P.nlow) - 1;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    psi[base + hoff[j >> P.nlow] + (j & lm)] = make_double2(s[j].x, s[j].y);
+  }
+}
+
+template <typename R>
+__global__ void k_tile_forward(typename C2<R>::T* psi, int n, const PassArgs P, const tq_tile_op* __restrict__ ops) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  cplx<R>* s = reinterpret_cast<cplx<R>*>(smem);
+  int64_t* hoff = reinterpret_cast<int64_t*>(smem + (sizeof(cplx<R>) << P.t));
+  build_hoff(hoff, P);
+  __syncthreads();
+  const int64_t ntiles = int64_t(1) << (n - P.t);
+  for (int64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
+    const int64_t base = tile_base(g, P);
+    tile_load<R>(s, psi, base, hoff, P);
+    __syncthreads();
+    for (int k = P.op_begin; k < P.op_end; ++k) {
+      tile_apply<R>(s, P.t, ops[k], threadIdx.x, blockDim.x, false);
+      __syncthreads();
+    }
+    tile_store<R>(s, psi, base, hoff, P);
+    __syncthreads();
+  }
+}
+
+// Adjoint pass: psi and lam tiles; per op: gradient term then un-apply.
+// Per-block slot sums go to partials[block * n_slots + slot].
+template <typename R>
+__global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, int n, const PassArgs P,
+                               const tq_tile_op* __restrict__ ops, int n_slots, double* partials) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const size_t tb = sizeof(cplx<R>) << P.t;
+  cplx<R>* sp = reinterpret_cast<cplx<R>*>(smem);
+  cplx<R>* sl = reinterpret_cast<cplx<R>*>(smem + tb);
+  int64_t* hoff = reinterpret_cast<int64_t*>(smem + 2 * tb);
+  double* acc = reinterpret_cast<double*>(smem + 2 * tb + (sizeof(int64_t) << (P.t - P.nlow)));
+  __shared__ double red[32];
+  build_hoff(hoff, P);
+  const int nops = P.op_end - P.op_begin;
+  for (int k = threadIdx.x; k < nops; k += blockDim.x) acc[k] = 0.0;
+  __syncthreads();
+  const int64_t ntiles = int64_t(1) << (n - P.t);
+  for (int64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
+    const int64_t base = tile_base(g, P);
+    tile_load<R>(sp, psi, base, hoff, P);
+    tile_load<R>(sl, lam, base, hoff, P);
+    __syncthreads();
+    for (int k = 0; k < nops; ++k) {
+      const tq_tile_op& o = ops[P.op_begin + k];
+      if (o.slot >= 0) {
+        const R phr[4] = {R(1), R(0), R(-1), R(0)}, phi[4] = {R(0), R(1), R(0), R(-1)};
+        const cplx<R> ph(phr[o.gny & 3], phi[o.gny & 3]);
+        const R part = tile_grad_partial<R>(sp, sl, P.t, o.gxm, o.gzm, o.gcm, ph, threadIdx.x, blockDim.x);
+        double v = (double)part;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double sum = 0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += red[w];
+          acc[k] += sum;
+        }
+        __syncthreads();
+      }
+      tile_apply<R>(sp, P.t, o, threadIdx.x, blockDim.x, true);
+      tile_apply<R>(sl, P.t, o, threadIdx.x, blockDim.x, true);
+      __syncthreads();
+    }
+    tile_store<R>(sp, psi, base, hoff, P);
+    tile_store<R>(sl, lam, base, hoff, P);
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < nops; k += blockDim.x) {
+    const int slot = ops[P.op_begin + k].slot;
+    if (slot >= 0) partials[(int64_t)blockIdx.x * n_slots + slot] = acc[k];
+  }
+}
+
+__global__ void k_finalize_slots(const double* partials, int nblk, int nslots, double* out) {
+  __shared__ double sh[32];
+  const int o = blockIdx.x;
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += partials[(int64_t)b * nslots + o];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
+    out[o] = s;
+  }
+}
+
+static int tile_threads(int t) {
+  int nt = 1 << (t - 1);
+  if (nt > 512) nt = 512;
+  if (nt < 32) nt = 32;
+  return nt;
+}
+
+static int check_passes(int n, int dtype, const tq_tile_pass* passes, int n_passes, int max_t, const char* name) {
+  for (int p = 0; p < n_passes; ++p) {
+    const tq_tile_pass& P = passes[p];
+    if (P.t < 1 || P.t > n || P.t > max_t)
+      return fail(TQ_ERR_ARG, "%s: pass %d has t=%d (n=%d, max %d)", name, p, P.t, n, max_t);
+    if (P.nlow < 1 || P.nlow > P.t) return fail(TQ_ERR_ARG, "%s: pass %d has nlow=%d", name, p, P.nlow);
+    for (int j = 0; j < P.t; ++j) {
+      if (P.pos[j] < 0 || P.pos[j] >= n) return fail(TQ_ERR_RANGE, "%s: pass %d pos out of range", name, p);
+      if (j < P.nlow && P.pos[j] != j) return fail(TQ_ERR_ARG, "%s: pass %d low positions not 0..nlow-1", name, p);
+      if (j > 0 && P.pos[j] <= P.pos[j - 1]) return fail(TQ_ERR_ARG, "%s: pass %d pos not ascending", name, p);
+    }
+    if (P.op_begin < 0 || P.op_end < P.op_begin) return fail(TQ_ERR_ARG, "%s: pass %d op range", name, p);
+  }
+  (void)dtype;
+  return TQ_OK;
+}
+
+static int max_bits(int dtype, bool adjoint) {
+  // complex64: 2^14 * 8 B = 128 KiB; complex128: 2^13 * 16 B = 128 KiB per tile
+  const int f = (dtype == TQ_C64) ? 14 : 13;
+  return adjoint ? f - 1 : f;
+}
+
+template <typename R>
+static int run_fwd(void* psi, int n, const tq_tile_pass* passes, int n_passes, const tq_tile_op* ops, cudaStream_t s) {
+  for (int p = 0; p < n_passes; ++p) {
+    const PassArgs P = to_args(passes[p]);
+    if (P.op_end == P.op_begin) continue;
+    const size_t smem = (sizeof(cplx<R>) << P.t) + (sizeof(int64_t) << (P.t - P.nlow));
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_tile_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return cuda_status(e, "tq_sv_run_tiles: smem attribute");
+    }
+    const int64_t ntiles = int64_t(1) << (n - P.t);
+    const unsigned grid = (unsigned)(ntiles < kTileGridCap ? ntiles : kTileGridCap);
+    k_tile_forward<R><<<grid, tile_threads(P.t), smem, s>>>((typename C2<R>::T*)psi, n, P, ops);
+    TQ_CHECK_LAUNCH("tq_sv_run_tiles");
+  }
+  return TQ_OK;
+}
+
+static unsigned adjoint_grid(int n, const tq_tile_pass* passes, int n_passes) {
+  int64_t g = 1;
+  for (int p = 0; p < n_passes; ++p) {
+    const int64_t nt = int64_t(1) << (n - passes[p].t);
+    if (nt > g) g = nt;
+  }
+  return (unsigned)(g < kTileGridCap ? g : kTileGridCap);
+}
+
+template <typename R>
+static int run_adj(void* psi, void* lam, int n, const tq_tile_pass* passes, int n_passes, const tq_tile_op* ops,
+                   int n_slots, double* slot_out, double* partials, cudaStream_t s) {
+  const unsigned grid = adjoint_grid(n, passes, n_passes);
+  if (n_slots > 0) cudaMemsetAsync(partials, 0, sizeof(double) * (size_t)grid * n_slots, s);
+  for (int p = 0; p < n_passes; ++p) {
+    const PassArgs P = to_args(passes[p]);
+    const int nops = P.op_end - P.op_begin;
+    if (nops == 0) continue;
+    const size_t smem = 2 * (sizeof(cplx<R>) << P.t) + (sizeof(int64_t) << (P.t - P.nlow)) + sizeof(double) * nops;
+    if (smem > 227 * 1024) return fail(TQ_ERR_ARG, "tq_sv_adjoint_tiles: pass %d needs %zu B shared memory", p, smem);
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_tile_adjoint<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return cuda_status(e, "tq_sv_adjoint_tiles: smem attribute");
+    }
+    k_tile_adjoint<R><<<grid, tile_threads(P.t), smem, s>>>((typename C2<R>::T*)psi, (typename C2<R>::T*)lam, n, P,
+                                                            ops, n_slots, partials);
+    TQ_CHECK_LAUNCH("tq_sv_adjoint_tiles");
+  }
+  if (n_slots > 0) {
+    k_finalize_slots<<<n_slots, 256, 0, s>>>(partials, (int)grid, n_slots, slot_out);
+    TQ_CHECK_LAUNCH("tq_sv_adjoint_tiles: finalize");
+  }
+  return TQ_OK;
+}
+
+}  // namespace tq
+
+using namespace tq;
+
+extern "C" int tq_sv_tile_max_bits(int dtype) { return (dtype == TQ_C64 || dtype == TQ_C128) ? max_bits(dtype, false) : 0; }
+
+extern "C" int tq_sv_run_tiles(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
+                               const tq_tile_op* ops, void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (n_passes < 0) return fail(TQ_ERR_ARG, "tq_sv_run_tiles: negative pass count");
+  if (n_passes == 0) return TQ_OK;
+  if (!psi || !passes || !ops) return fail(TQ_ERR_ARG, "tq_sv_run_tiles: NULL pointer");
+  if ((rc = check_passes(n, dtype, passes, n_passes, max_bits(dtype, false), "tq_sv_run_tiles"))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == TQ_C64 ? run_fwd<float>(psi, n, passes, n_passes, ops, s)
+                         : run_fwd<double>(psi, n, passes, n_passes, ops, s);
+}
+
+extern "C" size_t tq_sv_adjoint_tiles_workspace_bytes(int n, int n_slots) {
+  if (n < 1 || n > TQ_MAX_QUBITS || n_slots < 0) return 0;
+  return sizeof(double) * (size_t)kTileGridCap * (size_t)(n_slots > 0 ? n_slots : 1);
+}
+
+extern "C" int tq_sv_adjoint_tiles(void* psi, void* lam, int n, int dtype, const tq_tile_pass* passes, int n_passes,
+                                   const tq_tile_op* ops, int n_slots, double* slot_out, void* ws, size_t ws_bytes,
+                                   void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (n_passes < 0 || n_slots < 0) return fail(TQ_ERR_ARG, "tq_sv_adjoint_tiles: negative count");
+  if (!psi || !lam || (n_passes > 0 && (!passes || !ops)) || (n_slots > 0 && !slot_out))
+    return fail(TQ_ERR_ARG, "tq_sv_adjoint_tiles: NULL pointer");
+  if (psi == lam) return fail(TQ_ERR_ARG, "tq_sv_adjoint_tiles: psi aliases lam");
+  if ((rc = check_passes(n, dtype, passes, n_passes, max_bits(dtype, true), "tq_sv_adjoint_tiles"))) return rc;
+  const size_t need = tq_sv_adjoint_tiles_workspace_bytes(n, n_slots);
+  if (n_slots > 0 && (!ws || ws_bytes < need))
+    return fail(TQ_ERR_WORKSPACE, "tq_sv_adjoint_tiles: workspace of %zu bytes < %zu", ws_bytes, need);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == TQ_C64 ? run_adj<float>(psi, lam, n, passes, n_passes, ops, n_slots, slot_out, (double*)ws, s)
+                         : run_adj<double>(psi, lam, n, passes, n_passes, ops, n_slots, slot_out, (double*)ws, s);
+}

@@ -1,0 +1,180 @@
+"""Pauli-sum Hamiltonians packed for the GPU kernels.
+
+Input formats accepted (all from the reference):
+  * list of ``(coeff, [(pauli_char, qubit), ...])`` — the HEA runtime format
+    (tyxonq/applications/chem/runtimes/hea_numeric_runtime.py:36-53);
+  * Pauli code lists + weights, codes 0..3 = I, X, Y, Z, qubit 0 first
+    (tyxonq/libs/quantum_library/kernels/pauli.py:65-87);
+  * a dict ``{((q, 'X'), ...): coeff}`` as in openfermion's ``QubitOperator.terms``.
+
+Packing: term P = prod_q sigma_q acts as P|i> = i^{ny} (-1)^{popc(i & zy)} |i ^ flip>
+with flip = X/Y bits, zy = Y/Z bits (qubit q <-> bit n-1-q).  Terms are
+sorted by flip mask into groups so the kernels sweep the state once per
+distinct mask.  Repeated qubits inside one term keep the last Pauli, as the
+reference's ``term[qubit_idx] = code`` does (hea_numeric_runtime.py:45-47).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Iterable, Sequence
+
+import numpy as np
+
+GROUP_DTYPE = np.dtype([("flip", "<u8"), ("first_term", "<i4"), ("n_terms", "<i4")])
+TERM_DTYPE = np.dtype([("zy", "<u8"), ("w_re", "<f8"), ("w_im", "<f8")])
+_CODE = {"I": 0, "X": 1, "Y": 2, "Z": 3}
+_I_POW = [(1.0, 0.0), (0.0, 1.0), (-1.0, 0.0), (0.0, -1.0)]
+
+
+@dataclass
+class PauliSum:
+    """H = sum_k coeff_k * P_k on n qubits; codes[k, q] in {0,1,2,3}."""
+
+    n: int
+    codes: np.ndarray  # (K, n) int8
+    coeffs: np.ndarray  # (K,) float64
+    _packed: tuple | None = field(default=None, repr=False)
+    _device_cache: dict = field(default_factory=dict, repr=False)
+
+    # ------------------------------------------------------------ constructors
+    @classmethod
+    def from_terms(cls, n: int, terms: Iterable) -> "PauliSum":
+        terms = list(terms)
+        codes = np.zeros((len(terms), n), dtype=np.int8)
+        coeffs = np.zeros(len(terms), dtype=np.float64)
+        for k, (c, ops) in enumerate(terms):
+            coeffs[k] = float(c)
+            for p, q in ops:
+                q = int(q)
+                if q < 0 or q >= n:
+                    raise ValueError(f"qubit {q} out of range for {n} qubits")
+                codes[k, q] = _CODE[str(p).upper()]
+        return cls(n, codes, coeffs)
+
+    @classmethod
+    def from_codes(cls, ls: Sequence[Sequence[int]], weights: Sequence[float] | None = None) -> "PauliSum":
+        arr = np.asarray(ls, dtype=np.int8)
+        if arr.ndim != 2:
+            raise ValueError("Pauli code list must be 2-D (terms x qubits)")
+        if np.any((arr < 0) | (arr > 3)):
+            raise ValueError("Pauli codes must be in 0..3")
+        w = np.ones(arr.shape[0]) if weights is None else np.asarray(weights, dtype=np.float64)
+        return cls(arr.shape[1], arr.copy(), w.astype(np.float64))
+
+    @classmethod
+    def from_qubit_operator_terms(cls, n: int, terms: dict) -> "PauliSum":
+        items = []
+        for key, c in terms.items():
+            if abs(complex(c).imag) > 1e-12:
+                raise ValueError("non-Hermitian term coefficient")
+            items.append((complex(c).real, [(p, q) for (q, p) in key]))
+        return cls.from_terms(n, items)
+
+    # ------------------------------------------------------------ views
+    @property
+    def n_terms(self) -> int:
+        return int(self.codes.shape[0])
+
+    def terms(self) -> list:
+        inv = "IXYZ"
+        out = []
+        for k in range(self.n_terms):
+            out.append((float(self.coeffs[k]), [(inv[c], q) for q, c in enumerate(self.codes[k]) if c]))
+        return out
+
+    def masks(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(flip, zy, ny) per term as uint64/uint64/int."""
+        n = self.n
+        bits = (np.uint64(1) << (np.uint64(n - 1) - np.arange(n, dtype=np.uint64))) if n else np.zeros(0, np.uint64)
+        c = self.codes
+        xy = (c == 1) | (c == 2)
+        yz = (c == 2) | (c == 3)
+        flip = np.bitwise_or.reduce(np.where(xy, bits, np.uint64(0)), axis=1) if n else np.zeros(len(c), np.uint64)
+        zy = np.bitwise_or.reduce(np.where(yz, bits, np.uint64(0)), axis=1) if n else np.zeros(len(c), np.uint64)
+        ny = (c == 2).sum(axis=1)
+        return flip.astype(np.uint64), zy.astype(np.uint64), ny.astype(np.int64)
+
+    def pack(self) -> tuple[np.ndarray, np.ndarray]:
+        """(groups, terms) structured arrays matching tq_pauli_group / tq_pauli_term."""
+        if self._packed is not None:
+            return self._packed
+        flip, zy, ny = self.masks()
+        order = np.lexsort((zy, flip))
+        terms = np.zeros(self.n_terms, dtype=TERM_DTYPE)
+        groups = []
+        for pos, k in enumerate(order):
+            re, im = _I_POW[int(ny[k]) & 3]
+            terms[pos] = (zy[k], self.coeffs[k] * re, self.coeffs[k] * im)
+            if not groups or groups[-1][0] != flip[k]:
+                groups.append([flip[k], pos, 0])
+            groups[-1][2] += 1
+        g = np.zeros(len(groups), dtype=GROUP_DTYPE)
+        for i, (f, first, cnt) in enumerate(groups):
+            g[i] = (f, first, cnt)
+        self._packed = (g, terms)
+        return self._packed
+
+    @property
+    def n_groups(self) -> int:
+        return int(self.pack()[0].shape[0])
+
+    def to_device(self, device):
+        """Device copies of the packed tables (uint8 tensors), cached per device."""
+        import torch
+
+        key = str(device)
+        hit = self._device_cache.get(key)
+        if hit is not None:
+            return hit
+        g, t = self.pack()
+        gd = torch.from_numpy(np.frombuffer(g.tobytes() or b"\0" * 16, dtype=np.uint8).copy()).to(device)
+        td = torch.from_numpy(np.frombuffer(t.tobytes() or b"\0" * 24, dtype=np.uint8).copy()).to(device)
+        out = (gd, td, int(g.shape[0]), int(t.shape[0]))
+        self._device_cache[key] = out
+        return out
+
+    def one_norm(self) -> float:
+        return float(np.abs(self.coeffs).sum())
+
+
+def as_pauli_sum(H, n: int | None = None) -> PauliSum:
+    """Coerce any accepted Hamiltonian format to PauliSum."""
+    if isinstance(H, PauliSum):
+        return H
+    if isinstance(H, dict):
+        if n is None:
+            raise ValueError("n is required for dict Hamiltonians")
+        return PauliSum.from_qubit_operator_terms(n, H)
+    if hasattr(H, "terms") and isinstance(getattr(H, "terms"), dict):
+        if n is None:
+            raise ValueError("n is required for QubitOperator Hamiltonians")
+        return PauliSum.from_qubit_operator_terms(n, H.terms)
+    if isinstance(H, tuple) and len(H) == 2 and not isinstance(H[0], (int, float)):
+        return PauliSum.from_codes(H[0], H[1])
+    if n is None:
+        raise ValueError("n is required for term-list Hamiltonians")
+    return PauliSum.from_terms(n, H)
+
+
+# ---------------------------------------------------------------- generators
+def tfim_terms(n: int, hx: float = 1.0, hzz: float = 1.0, pbc: bool = False) -> list:
+    """H = -hzz sum Z_i Z_{i+1} - hx sum X_i (open chain unless pbc); the
+    term set of tyxonq/libs/circuits_library/hamiltonians.py:17-27."""
+    terms = []
+    for i in range(n - 1 + (1 if pbc and n > 2 else 0)):
+        terms.append((-hzz, [("Z", i), ("Z", (i + 1) % n)]))
+    for i in range(n):
+        terms.append((-hx, [("X", i)]))
+    return terms
+
+
+def random_pauli_sum(n: int, n_terms: int, rng: np.random.Generator, max_weight: int = 4) -> PauliSum:
+    """Random H: n_terms terms, weight uniform in 1..max_weight on distinct
+    random qubits, Paulis uniform in {X,Y,Z}, coefficients N(0,1)."""
+    codes = np.zeros((n_terms, n), dtype=np.int8)
+    for k in range(n_terms):
+        w = int(rng.integers(1, min(max_weight, n) + 1))
+        qs = rng.choice(n, size=w, replace=False)
+        codes[k, qs] = rng.integers(1, 4, size=w)
+    coeffs = rng.standard_normal(n_terms)
+    return PauliSum(n, codes, coeffs)

@@ -1,0 +1,51 @@
+"""Registration of the GPU engine into an installed TyxonQ.
+
+TyxonQ picks simulator engines in ``devices/simulators/driver.py:_select_engine``
+(:20-30), called as ``Engine()`` (driver.py:97,164), and ``Circuit.state()``
+imports ``StatevectorEngine`` from ``devices/simulators/statevector/engine``
+at call time (core/ir/circuit.py:491-494).  ``install`` wraps the former so
+``device="statevector_gpu"`` (and, with ``replace_statevector``, plain
+``"statevector"``) returns GpuStatevectorEngine, and rebinds the latter so
+``Circuit.state()`` runs on the GPU.  The chain API
+``c.compile().device(provider="simulator", device="statevector").run()`` then
+reaches the GPU engine unchanged.  ``uninstall`` restores both.
+"""
+from __future__ import annotations
+
+_saved: dict = {}
+
+
+def install(replace_statevector: bool = True, alias: str = "statevector_gpu"):
+    import tyxonq.devices.simulators.driver as drv  # type: ignore
+    import tyxonq.devices.simulators.statevector.engine as sv_mod  # type: ignore
+
+    from .engine import GpuStatevectorEngine
+
+    if "select" not in _saved:
+        _saved["select"] = drv._select_engine
+        _saved["sv_cls"] = sv_mod.StatevectorEngine
+    orig = _saved["select"]
+    names = {alias, f"simulator:{alias}"}
+    if replace_statevector:
+        names |= {"statevector", "simulator:statevector"}
+
+    def _select_engine(device: str):
+        name = device.split("::")[-1] if "::" in device else device
+        if name in names:
+            return GpuStatevectorEngine
+        return orig(device)
+
+    drv._select_engine = _select_engine
+    if replace_statevector:
+        sv_mod.StatevectorEngine = GpuStatevectorEngine
+    return GpuStatevectorEngine
+
+
+def uninstall():
+    if "select" not in _saved:
+        return
+    import tyxonq.devices.simulators.driver as drv  # type: ignore
+    import tyxonq.devices.simulators.statevector.engine as sv_mod  # type: ignore
+
+    drv._select_engine = _saved["select"]
+    sv_mod.StatevectorEngine = _saved["sv_cls"]

@@ -1,0 +1,401 @@
+"""Tile-pass planning and execution of gate programs on the GPU.
+
+A *program* is the gate list of one circuit cut into shared-memory tile
+passes (``csrc/program.cu``).  ``plan_passes`` schedules gates greedily over
+the gate DAG: each pass keeps the lowest ``nlow`` index bits local (for
+coalesced HBM access) and adds up to ``t - nlow`` further qubits, taking every
+ready gate whose qubits fit.  Within a forward pass single-qubit gates are
+folded into neighbouring two-qubit gates (``fuse_pass``), so a pass costs one
+HBM round trip plus a few shared-memory sweeps.  Gates that cannot run inside
+a tile (k >= 3 dense unitaries, Z projections) split the program into
+segments executed by the single-gate kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+from collections import deque
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from . import kernels as K
+from .ir import Gate
+
+TILE_OP_DTYPE = np.dtype({
+    "names": ["kind", "a", "b", "slot", "xm", "zm", "gxm", "gzm", "gcm", "gny", "mf", "md"],
+    "formats": ["<i4", "<i4", "<i4", "<i4", "<u4", "<u4", "<u4", "<u4", "<u4", "<i4", ("<f4", 32), ("<f8", 32)],
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 168],
+    "itemsize": 424,
+})
+TOP = {"u1": 1, "d1": 2, "u2": 3, "cx": 4, "cz": 5, "swap": 6, "prot": 7}
+TILE_KINDS = {"u1", "d1", "u2", "cx", "cz", "swap", "prot"}
+MAX_BITS = 16
+DEFAULT_NLOW = 5
+
+
+class TilePass(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_int32), ("nlow", ctypes.c_int32), ("op_begin", ctypes.c_int32),
+                ("op_end", ctypes.c_int32), ("pos", ctypes.c_int32 * MAX_BITS)]
+
+
+def tileable(g: Gate) -> bool:
+    if g.kind in TILE_KINDS:
+        return True
+    return g.kind == "uk" and len(g.qubits) <= 2
+
+
+def _canon(g: Gate) -> Gate:
+    if g.kind == "uk" and len(g.qubits) == 1:
+        return Gate("u1", g.qubits, g.mat, rot=g.rot)
+    if g.kind == "uk" and len(g.qubits) == 2:
+        return Gate("u2", g.qubits, g.mat, rot=g.rot)
+    return g
+
+
+# ---------------------------------------------------------------- planning
+@dataclass
+class PassPlan:
+    qubits: list  # local qubits (sorted by bit position ascending)
+    gates: list  # gate indices in execution order
+    nlow: int = DEFAULT_NLOW  # the lowest nlow index bits are local
+
+
+@dataclass
+class Segment:
+    kind: str  # 'tiles' or 'gate'
+    passes: list = field(default_factory=list)  # list[PassPlan]
+    gate: int = -1
+
+
+def plan_passes(gates: Sequence[Gate], n: int, t: int, nlow: int = DEFAULT_NLOW) -> list[Segment]:
+    """Greedy DAG scheduling of `gates` into tile passes of t local qubits."""
+    t = min(t, n)
+
+    def fits(g: Gate) -> bool:
+        return tileable(g) and (len(set(g.qubits)) <= t - 1 or t == n)
+
+    # keep room for the widest tile gate next to the always-local low bits
+    maxw = max([len(set(g.qubits)) for g in gates if fits(g)] or [1])
+    nlow = n if t == n else max(1, min(nlow, t - maxw))
+    low = set(range(n - nlow, n))  # qubits whose bits are 0..nlow-1
+    queues: list[deque] = [deque() for _ in range(n)]
+    for i, g in enumerate(gates):
+        for q in set(g.qubits):
+            queues[q].append(i)
+    done = [False] * len(gates)
+
+    def is_ready(i: int) -> bool:
+        return all(queues[q] and queues[q][0] == i for q in set(gates[i].qubits))
+
+    ready = set(i for i in range(len(gates)) if is_ready(i))
+    segments: list[Segment] = []
+    remaining = len(gates)
+
+    def execute(i: int):
+        nonlocal remaining
+        done[i] = True
+        remaining -= 1
+        ready.discard(i)
+        for q in set(gates[i].qubits):
+            queues[q].popleft()
+            if queues[q]:
+                h = queues[q][0]
+                if not done[h] and is_ready(h):
+                    ready.add(h)
+
+    while remaining:
+        # plain-kernel gates that are ready run first
+        plain = sorted(i for i in ready if not fits(gates[i]))
+        if plain:
+            for i in plain:
+                segments.append(Segment("gate", gate=i))
+                execute(i)
+            continue
+        L = set(low)
+        order: list[int] = []
+        while True:
+            best, best_cost = None, None
+            for i in ready:
+                g = gates[i]
+                if not fits(g):
+                    continue
+                new = set(g.qubits) - L
+                if len(L) + len(new) > t:
+                    continue
+                c = len(new)
+                if best is None or c < best_cost or (c == best_cost and i < best):
+                    best, best_cost = i, c
+                    if c == 0:
+                        break
+            if best is None:
+                break
+            L |= set(gates[best].qubits)
+            order.append(best)
+            execute(best)
+        if not order:  # pragma: no cover - a ready tileable gate always fits an empty pass
+            raise RuntimeError("tile planner made no progress")
+        # pad the local set up to t with the lowest free bits (bigger, fewer tiles)
+        for q in range(n - 1, -1, -1):
+            if len(L) >= t:
+                break
+            L.add(q)
+        qs = sorted(L, key=lambda q: n - 1 - q)
+        if segments and segments[-1].kind == "tiles":
+            segments[-1].passes.append(PassPlan(qs, order, min(nlow, len(qs))))
+        else:
+            segments.append(Segment("tiles", passes=[PassPlan(qs, order, min(nlow, len(qs)))]))
+    return segments
+
+
+# ---------------------------------------------------------------- fusion
+def _kron_local(P: np.ndarray, which: int) -> np.ndarray:
+    I = np.eye(2, dtype=np.complex128)
+    return np.kron(P, I) if which == 0 else np.kron(I, P)
+
+
+def _mat4(g: Gate) -> np.ndarray:
+    from . import gates as G
+
+    if g.kind == "u2":
+        return g.mat
+    return {"cx": G.gate_cx_4x4, "cz": G.gate_cz_4x4, "swap": G.gate_swap_4x4}[g.kind]()
+
+
+def fuse_pass(gates: Sequence[Gate]) -> list[Gate]:
+    """Fold single-qubit gates into neighbouring two-qubit gates (forward only)."""
+    out: list[Gate] = []
+    pending: dict[int, np.ndarray] = {}
+    last: dict[int, int] = {}
+    for g0 in gates:
+        g = _canon(g0)
+        if g.kind in ("u1", "d1"):
+            q = g.qubits[0]
+            M = g.mat if g.kind == "u1" else np.diag(np.diag(g.mat))
+            pending[q] = M @ pending[q] if q in pending else M.copy()
+        elif g.kind in ("u2", "cx", "cz", "swap"):
+            a, b = g.qubits
+            pa, pb = pending.pop(a, None), pending.pop(b, None)
+            if pa is None and pb is None:
+                out.append(g)
+            else:
+                M = _mat4(g)
+                if pa is not None:
+                    M = M @ _kron_local(pa, 0)
+                if pb is not None:
+                    M = M @ _kron_local(pb, 1)
+                out.append(Gate("u2", (a, b), M))
+            last[a] = last[b] = len(out) - 1
+        else:  # prot: flush its qubits first
+            for q in g.qubits:
+                if q in pending:
+                    out.append(_one_q(q, pending.pop(q)))
+                    last[q] = len(out) - 1
+            out.append(g)
+            for q in g.qubits:
+                last[q] = len(out) - 1
+    for q, P in pending.items():
+        j = last.get(q)
+        if j is not None and out[j].kind in ("u2", "cx", "cz", "swap"):
+            tg = out[j]
+            M = _mat4(tg)
+            which = 0 if tg.qubits[0] == q else 1
+            out[j] = Gate("u2", tg.qubits, _kron_local(P, which) @ M)
+        else:
+            out.append(_one_q(q, P))
+    return out
+
+
+def _one_q(q: int, M: np.ndarray) -> Gate:
+    if abs(M[0, 1]) == 0 and abs(M[1, 0]) == 0:
+        return Gate("d1", (q,), M)
+    return Gate("u1", (q,), M)
+
+
+# ---------------------------------------------------------------- encoding
+_PH = [1.0, 1j, -1.0, -1j]
+
+
+def _generator(g: Gate, loc: dict) -> tuple[int, int, int, int, float] | None:
+    """(gxm, gzm, gcm, gny, coef) with dE/dangle = coef * Im<lam|G|psi>."""
+    if g.rot is None:
+        return None
+    name = g.rot[0]
+    if name in ("rx", "ry", "rz", "rxx", "ryy", "rzz"):
+        from .ir import ROTATION_GENERATORS
+
+        ps = ROTATION_GENERATORS[name]
+        xm = zm = ny = 0
+        for q, p in zip(g.qubits, ps):
+            b = 1 << loc[q]
+            if p in "XY":
+                xm |= b
+            if p in "YZ":
+                zm |= b
+            ny += p == "Y"
+        return xm, zm, 0, ny, 1.0
+    if name == "cry":
+        c, tq_ = g.qubits
+        return 1 << loc[tq_], 1 << loc[tq_], 1 << loc[c], 1, 1.0
+    if name == "phase":
+        return 0, 0, 1 << loc[g.qubits[0]], 0, -2.0
+    if name == "prot":
+        xm = zm = ny = 0
+        for q, p in g.pauli:
+            b = 1 << loc[q]
+            if p in "XY":
+                xm |= b
+            if p in "YZ":
+                zm |= b
+            ny += p == "Y"
+        return xm, zm, 0, ny, 1.0
+    return None
+
+
+def encode_op(rec, g: Gate, loc: dict, slot: int = -1, gen=None) -> None:
+    g = _canon(g)
+    rec["kind"] = TOP[g.kind]
+    rec["a"] = loc[g.qubits[0]]
+    rec["b"] = loc[g.qubits[1]] if len(g.qubits) > 1 else 0
+    rec["slot"] = slot
+    if g.kind == "u1":
+        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
+    elif g.kind == "d1":
+        m = np.array([g.mat[0, 0], g.mat[1, 1]], dtype=np.complex128)
+    elif g.kind == "u2":
+        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
+    elif g.kind == "prot":
+        xm = zm = ny = 0
+        for q, p in g.pauli:
+            b = 1 << loc[q]
+            if p in "XY":
+                xm |= b
+            if p in "YZ":
+                zm |= b
+            ny += p == "Y"
+        a = g.rot[1]
+        c, s = np.cos(0.5 * a), np.sin(0.5 * a)
+        m = np.array([c, -1j * s * _PH[ny & 3]], dtype=np.complex128)
+        rec["xm"], rec["zm"] = xm, zm
+    else:
+        m = np.zeros(0, dtype=np.complex128)
+    if m.size:
+        flat = np.stack([m.real, m.imag], axis=-1).reshape(-1)
+        rec["md"][: flat.size] = flat
+        rec["mf"][: flat.size] = flat.astype(np.float32)
+    if gen is not None:
+        rec["gxm"], rec["gzm"], rec["gcm"], rec["gny"] = gen[0], gen[1], gen[2], gen[3]
+
+
+@dataclass
+class EncodedTiles:
+    passes: ctypes.Array
+    n_passes: int
+    ops_host: np.ndarray
+    ops_dev: torch.Tensor | None = None
+
+    def device_ops(self, device) -> torch.Tensor:
+        if self.ops_dev is None or self.ops_dev.device != torch.device(device):
+            raw = self.ops_host.tobytes() or bytes(TILE_OP_DTYPE.itemsize)
+            self.ops_dev = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(device)
+        return self.ops_dev
+
+
+def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, fuse: bool, reverse: bool = False,
+                  slots: dict | None = None, nlow: int = DEFAULT_NLOW) -> tuple[EncodedTiles, list]:
+    """Encode pass plans.  reverse=True lists passes and ops in reverse (for the
+    adjoint sweep); `slots` maps gate index -> gradient slot.  Returns the
+    encoded tiles and per-slot coefficients [(slot, coef)]."""
+    recs = []
+    passes = []
+    coefs = []
+    seq = list(reversed(plans)) if reverse else list(plans)
+    for pp in seq:
+        qs = pp.qubits
+        loc = {q: j for j, q in enumerate(qs)}
+        t = len(qs)
+        gl = [gates[i] for i in (reversed(pp.gates) if reverse else pp.gates)]
+        idx = list(reversed(pp.gates)) if reverse else list(pp.gates)
+        begin = len(recs)
+        if fuse and not reverse:
+            for g in fuse_pass(gl):
+                r = np.zeros(1, dtype=TILE_OP_DTYPE)[0]
+                encode_op(r, g, loc)
+                recs.append(r)
+        else:
+            for gi, g in zip(idx, gl):
+                r = np.zeros(1, dtype=TILE_OP_DTYPE)[0]
+                slot = -1
+                gen = None
+                if slots is not None and gi in slots:
+                    slot = slots[gi]
+                    gen = _generator(g, loc)
+                    coefs.append((slot, gen[4]))
+                encode_op(r, g, loc, slot, gen)
+                recs.append(r)
+        p = TilePass()
+        p.t = t
+        p.nlow = min(pp.nlow, t)
+        p.op_begin = begin
+        p.op_end = len(recs)
+        for j, q in enumerate(qs):
+            p.pos[j] = n - 1 - q
+        passes.append(p)
+    arr = (TilePass * max(len(passes), 1))(*passes)
+    ops = np.array(recs, dtype=TILE_OP_DTYPE) if recs else np.zeros(0, dtype=TILE_OP_DTYPE)
+    return EncodedTiles(arr, len(passes), ops), coefs
+
+
+# ---------------------------------------------------------------- execution
+def default_tile_bits(n: int, dtype: torch.dtype, adjoint: bool = False) -> int:
+    from .autotune import tile_bits_for
+
+    return tile_bits_for(n, dtype, adjoint)
+
+
+@dataclass
+class ForwardProgram:
+    n: int
+    segments: list  # list of ('tiles', EncodedTiles) | ('gate', Gate)
+    n_gates: int
+    n_passes: int
+
+    def run(self, psi: torch.Tensor) -> torch.Tensor:
+        from .engine import execute_plain
+
+        dt = K.dtype_tag(psi)
+        for kind, obj in self.segments:
+            if kind == "gate":
+                execute_plain(psi, [obj])
+            else:
+                ops = obj.device_ops(psi.device)
+                nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), self.n, dt, obj.passes, obj.n_passes,
+                         ctypes.c_void_p(ops.data_ptr()), K.stream_ptr(psi.device))
+        return psi
+
+
+def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int | None = None,
+                    nlow: int = DEFAULT_NLOW, fuse: bool = True) -> ForwardProgram:
+    gates = [_canon(g) for g in gates]
+    if t is None:
+        t = default_tile_bits(n, dtype)
+    segs = plan_passes(gates, n, t, nlow)
+    out = []
+    npass = 0
+    for s in segs:
+        if s.kind == "gate":
+            out.append(("gate", gates[s.gate]))
+        else:
+            enc, _ = encode_passes(n, s.passes, gates, fuse=fuse, nlow=nlow)
+            out.append(("tiles", enc))
+            npass += enc.n_passes
+    return ForwardProgram(n, out, len(gates), npass)
+
+
+def execute_fused(psi: torch.Tensor, gates: Sequence[Gate]) -> torch.Tensor:
+    n = K._check_state(psi)
+    if n == 0:
+        return psi
+    return compile_forward(gates, n, psi.dtype).run(psi)
