@@ -204,7 +204,7 @@ def main():
                 b = torch.cuda.Event(enable_timing=True)
                 a.record(st)
                 nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), n2, 0,
-                         ctypes.byref(obj.passes[p]), 1, ctypes.c_void_p(ops_d.data_ptr()), K.stream_ptr())
+                         ctypes.byref(obj.passes[p]), 1, ctypes.c_void_p(ops_d.data_ptr()), None, K.stream_ptr())
                 b.record(st)
                 evs.append((a, b))
         return evs

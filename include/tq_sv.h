@@ -191,9 +191,14 @@ typedef struct {
   int32_t a;    /* local bit of the first qubit (matrix high bit / control) */
   int32_t b;    /* local bit of the second qubit (matrix low bit / target) */
   int32_t slot; /* gradient slot, -1 = none */
-  uint32_t xm, zm;          /* Pauli-rotation masks (kind 7): m[0] = cos, m[1] = -i sin * i^ny */
+  uint32_t xm, zm, cm;      /* kind 7: exp(-i a/2 P) on indices with (i & cm) == cm;
+                               m[0] = cos(a/2), m[1] = -i sin(a/2) i^ny */
   uint32_t gxm, gzm, gcm;   /* generator masks (slot >= 0) */
   int32_t gny;              /* number of Y factors in the generator */
+  int32_t pidx;             /* >= 0: angle a = pscale * theta[pidx], matrix built on the device
+                               (kind 7: Pauli rotation; kind 2: phase diag(1, e^{ia})) */
+  double pscale;
+  double gcoef;             /* dE/d(angle) = gcoef * Im <lam|G|psi> (batched kernel) */
   float mf[32];             /* matrix, complex64 kernels: row-major (re, im) */
   double md[32];            /* matrix, complex128 kernels */
 } tq_tile_op;
@@ -209,9 +214,10 @@ typedef struct {
 /* Largest t supported for a dtype (shared-memory capacity). */
 TQ_API int tq_sv_tile_max_bits(int dtype);
 
-/* Forward: apply passes[0..n_passes) in order.  passes: host array; ops: device. */
+/* Forward: apply passes[0..n_passes) in order.  passes: host array; ops and
+ * theta (angles of ops with pidx >= 0; may be NULL if there are none): device. */
 TQ_API int tq_sv_run_tiles(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
-                           const tq_tile_op* ops, void* stream);
+                           const tq_tile_op* ops, const double* theta, void* stream);
 
 /* Adjoint reverse sweep over passes (already in reverse order, ops in each pass
  * in reverse application order): for each op, first the gradient term (slot >= 0)
@@ -221,8 +227,50 @@ TQ_API int tq_sv_run_tiles(void* psi, int n, int dtype, const tq_tile_pass* pass
  * (chem_libs/quantum_chem_library/civector_ops.py:141-200). */
 TQ_API size_t tq_sv_adjoint_tiles_workspace_bytes(int n, int n_slots);
 TQ_API int tq_sv_adjoint_tiles(void* psi, void* lam, int n, int dtype, const tq_tile_pass* passes, int n_passes,
-                               const tq_tile_op* ops, int n_slots, double* slot_out, void* ws, size_t ws_bytes,
-                               void* stream);
+                               const tq_tile_op* ops, const double* theta, int n_slots, double* slot_out, void* ws,
+                               size_t ws_bytes, void* stream);
+
+/* Im <lam|G|psi> into *out_dev (FP64) for one generator G|i> = [i & cm == cm]
+ * i^ny (-1)^{popc(i & zm)} |i ^ xm> (masks over basis-index bits, ny = popc(xm & zm)):
+ * the per-gate gradient term of the unfused (plain engine) reverse sweep. */
+TQ_API int tq_sv_generator_im(const void* psi, const void* lam, int n, int dtype, uint64_t xm, uint64_t zm,
+                              uint64_t cm, double* out_dev, void* ws, size_t ws_bytes, void* stream);
+
+/* ------------------------------------------------------------ batched VQE */
+
+/* One VQE instance of a batch: energy E = <psi|H|psi> and dE/dtheta by the
+ * adjoint sweep, psi = U(theta)|basis>.  Resident instances (streamed == 0)
+ * keep psi and lam = H psi in shared memory: fwd/adj index op ranges whose bit
+ * positions are global.  Streamed instances keep psi, lam in the caller's
+ * pool at pool + scratch_offset (psi) and + scratch_offset + 2^n (lam),
+ * amplitudes; fwd/adj index pass-table ranges.  Adjoint ops carry
+ * slot = parameter index within the instance and gcoef. */
+typedef struct {
+  int32_t n;
+  int32_t streamed;
+  int32_t fwd_begin, fwd_count;
+  int32_t adj_begin, adj_count;
+  int32_t group_begin, group_count; /* Pauli groups of this instance's H (terms indexed globally) */
+  int32_t theta_offset;
+  int32_t grad_offset;
+  int64_t scratch_offset;
+  int64_t basis;
+} tq_batch_inst;
+
+/* Persistent launch over work[0..n_work) (instance indices, cost-sorted).
+ * CTAs pull instances from *counter (device int, zeroed by the caller before
+ * the launch) with atomicAdd; each CTA runs groups_per_cta independent thread
+ * groups (threads_per_cta / groups_per_cta threads each, named barriers) for
+ * resident instances, or one group for streamed ones.  grads must be zeroed
+ * by the caller; energies[i] and grads[grad_offset..] are written per instance.
+ * This is new: the reference evaluates VQE instances one at a time in Python
+ * loops (devices/base.py:378-381, examples/vqe_batched_architecture_search.py:181-201). */
+TQ_API size_t tq_batch_smem_bytes(int dtype, int max_resident_n, int groups_per_cta, int streamed_t);
+TQ_API int tq_batch_run(int dtype, const tq_batch_inst* insts, const int32_t* work, int n_work, int streamed,
+                        int groups_per_cta, int threads_per_cta, int grid, size_t smem_bytes,
+                        const tq_tile_pass* passes, const tq_tile_op* ops, const tq_pauli_group* groups,
+                        const tq_pauli_term* terms, const double* theta, void* pool, double* energies,
+                        double* grads, int32_t* counter, void* stream);
 
 /* Re <a|b> into *out_dev (FP64), used by energy = <psi|H psi>. */
 TQ_API size_t tq_sv_inner_workspace_bytes(int n);

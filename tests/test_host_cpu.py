@@ -53,8 +53,9 @@ def test_host_validation_without_gpu():
 
 class _CTileOp(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32), ("slot", ctypes.c_int32),
-                ("xm", ctypes.c_uint32), ("zm", ctypes.c_uint32), ("gxm", ctypes.c_uint32), ("gzm", ctypes.c_uint32),
-                ("gcm", ctypes.c_uint32), ("gny", ctypes.c_int32), ("mf", ctypes.c_float * 32),
+                ("xm", ctypes.c_uint32), ("zm", ctypes.c_uint32), ("cm", ctypes.c_uint32), ("gxm", ctypes.c_uint32),
+                ("gzm", ctypes.c_uint32), ("gcm", ctypes.c_uint32), ("gny", ctypes.c_int32), ("pidx", ctypes.c_int32),
+                ("pscale", ctypes.c_double), ("gcoef", ctypes.c_double), ("mf", ctypes.c_float * 32),
                 ("md", ctypes.c_double * 32)]
 
 
@@ -161,6 +162,13 @@ def _emulate_tiles(psi, n, enc):
                         s[i0], s[i1] = s[i1].copy(), s[i0].copy()
                     else:
                         s[base4 | (1 << a) | (1 << b)] *= -1
+                elif o["kind"] == 7:
+                    xm, zm, cm = int(o["xm"]), int(o["zm"]), int(o["cm"])
+                    c, w = m[0], m[1]
+                    sgn = np.array([-1 if bin(int(x) & zm).count("1") % 2 else 1 for x in j])
+                    on = (j & cm) == cm
+                    new = c * s + w * sgn[j ^ xm] * s[j ^ xm]
+                    s = np.where(on, new, s)
                 else:
                     raise AssertionError("unexpected op kind")
             psi[idx] = s

@@ -71,9 +71,10 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_pauli_expectation": (c_int, [_P, c_int, c_int, _P, c_int, _P, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_apply_pauli_sum": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, c_int, _P]),
     "tq_sv_tile_max_bits": (c_int, [c_int]),
-    "tq_sv_run_tiles": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P]),
+    "tq_sv_run_tiles": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P, _P]),
     "tq_sv_adjoint_tiles_workspace_bytes": (c_size_t, [c_int, c_int]),
-    "tq_sv_adjoint_tiles": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, c_int, _P, _P, c_size_t, _P]),
+    "tq_sv_adjoint_tiles": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, _P, c_int, _P, _P, c_size_t, _P]),
+    "tq_sv_generator_im": (c_int, [_P, _P, c_int, c_int, c_uint64, c_uint64, c_uint64, _P, _P, c_size_t, _P]),
     "tq_sv_inner_workspace_bytes": (c_size_t, [c_int]),
     "tq_sv_inner_re": (c_int, [_P, _P, c_int, c_int, _P, _P, c_size_t, _P]),
 }

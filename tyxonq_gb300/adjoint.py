@@ -117,7 +117,7 @@ def reverse_sweep(prog: AdjointProgram, psi: torch.Tensor, lam: torch.Tensor) ->
         seg_out = torch.empty_like(out)
         p, cap = K._ws(lib.tq_sv_adjoint_tiles_workspace_bytes(prog.n, prog.n_slots), psi.device)
         nat.call("tq_sv_adjoint_tiles", ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), prog.n, dt,
-                 enc.passes, enc.n_passes, ctypes.c_void_p(ops.data_ptr()), prog.n_slots,
+                 enc.passes, enc.n_passes, ctypes.c_void_p(ops.data_ptr()), None, prog.n_slots,
                  ctypes.c_void_p(seg_out.data_ptr()), p, cap, K.stream_ptr(psi.device))
         out += seg_out
     return out[: prog.n_slots]

@@ -98,7 +98,8 @@ __device__ __forceinline__ void tile_store<double>(const cplx<double>* s, double
 }
 
 template <typename R>
-__global__ void k_tile_forward(typename C2<R>::T* psi, int n, const PassArgs P, const tq_tile_op* __restrict__ ops) {
+__global__ void k_tile_forward(typename C2<R>::T* psi, int n, const PassArgs P, const tq_tile_op* __restrict__ ops,
+                               const double* __restrict__ theta) {
   extern __shared__ __align__(16) unsigned char smem[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem);
   int64_t* hoff = reinterpret_cast<int64_t*>(smem + (sizeof(cplx<R>) << P.t));
@@ -110,7 +111,7 @@ __global__ void k_tile_forward(typename C2<R>::T* psi, int n, const PassArgs P, 
     tile_load<R>(s, psi, base, hoff, P);
     __syncthreads();
     for (int k = P.op_begin; k < P.op_end; ++k) {
-      tile_apply<R>(s, P.t, ops[k], threadIdx.x, blockDim.x, false);
+      tile_apply<R>(s, P.t, ops[k], threadIdx.x, blockDim.x, false, theta);
       __syncthreads();
     }
     tile_store<R>(s, psi, base, hoff, P);
@@ -122,7 +123,8 @@ __global__ void k_tile_forward(typename C2<R>::T* psi, int n, const PassArgs P, 
 // Per-block slot sums go to partials[block * n_slots + slot].
 template <typename R>
 __global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, int n, const PassArgs P,
-                               const tq_tile_op* __restrict__ ops, int n_slots, double* partials) {
+                               const tq_tile_op* __restrict__ ops, const double* __restrict__ theta, int n_slots,
+                               double* partials) {
   extern __shared__ __align__(16) unsigned char smem[];
   const size_t tb = sizeof(cplx<R>) << P.t;
   cplx<R>* sp = reinterpret_cast<cplx<R>*>(smem);
@@ -158,8 +160,8 @@ __global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, i
         }
         __syncthreads();
       }
-      tile_apply<R>(sp, P.t, o, threadIdx.x, blockDim.x, true);
-      tile_apply<R>(sl, P.t, o, threadIdx.x, blockDim.x, true);
+      tile_apply<R>(sp, P.t, o, threadIdx.x, blockDim.x, true, theta);
+      tile_apply<R>(sl, P.t, o, threadIdx.x, blockDim.x, true, theta);
       __syncthreads();
     }
     tile_store<R>(sp, psi, base, hoff, P);
@@ -219,7 +221,8 @@ static int max_bits(int dtype, bool adjoint) {
 }
 
 template <typename R>
-static int run_fwd(void* psi, int n, const tq_tile_pass* passes, int n_passes, const tq_tile_op* ops, cudaStream_t s) {
+static int run_fwd(void* psi, int n, const tq_tile_pass* passes, int n_passes, const tq_tile_op* ops,
+                   const double* theta, cudaStream_t s) {
   for (int p = 0; p < n_passes; ++p) {
     const PassArgs P = to_args(passes[p]);
     if (P.op_end == P.op_begin) continue;
@@ -230,7 +233,7 @@ static int run_fwd(void* psi, int n, const tq_tile_pass* passes, int n_passes, c
     }
     const int64_t ntiles = int64_t(1) << (n - P.t);
     const unsigned grid = (unsigned)(ntiles < kTileGridCap ? ntiles : kTileGridCap);
-    k_tile_forward<R><<<grid, tile_threads(P.t), smem, s>>>((typename C2<R>::T*)psi, n, P, ops);
+    k_tile_forward<R><<<grid, tile_threads(P.t), smem, s>>>((typename C2<R>::T*)psi, n, P, ops, theta);
     TQ_CHECK_LAUNCH("tq_sv_run_tiles");
   }
   return TQ_OK;
@@ -247,6 +250,7 @@ static unsigned adjoint_grid(int n, const tq_tile_pass* passes, int n_passes) {
 
 template <typename R>
 static int run_adj(void* psi, void* lam, int n, const tq_tile_pass* passes, int n_passes, const tq_tile_op* ops,
+                   const double* theta,
                    int n_slots, double* slot_out, double* partials, cudaStream_t s) {
   const unsigned grid = adjoint_grid(n, passes, n_passes);
   if (n_slots > 0) cudaMemsetAsync(partials, 0, sizeof(double) * (size_t)grid * n_slots, s);
@@ -261,7 +265,7 @@ static int run_adj(void* psi, void* lam, int n, const tq_tile_pass* passes, int 
       if (e != cudaSuccess) return cuda_status(e, "tq_sv_adjoint_tiles: smem attribute");
     }
     k_tile_adjoint<R><<<grid, tile_threads(P.t), smem, s>>>((typename C2<R>::T*)psi, (typename C2<R>::T*)lam, n, P,
-                                                            ops, n_slots, partials);
+                                                            ops, theta, n_slots, partials);
     TQ_CHECK_LAUNCH("tq_sv_adjoint_tiles");
   }
   if (n_slots > 0) {
@@ -278,7 +282,7 @@ using namespace tq;
 extern "C" int tq_sv_tile_max_bits(int dtype) { return (dtype == TQ_C64 || dtype == TQ_C128) ? max_bits(dtype, false) : 0; }
 
 extern "C" int tq_sv_run_tiles(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
-                               const tq_tile_op* ops, void* stream) {
+                               const tq_tile_op* ops, const double* theta, void* stream) {
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_passes < 0) return fail(TQ_ERR_ARG, "tq_sv_run_tiles: negative pass count");
@@ -286,8 +290,8 @@ extern "C" int tq_sv_run_tiles(void* psi, int n, int dtype, const tq_tile_pass* 
   if (!psi || !passes || !ops) return fail(TQ_ERR_ARG, "tq_sv_run_tiles: NULL pointer");
   if ((rc = check_passes(n, dtype, passes, n_passes, max_bits(dtype, false), "tq_sv_run_tiles"))) return rc;
   cudaStream_t s = (cudaStream_t)stream;
-  return dtype == TQ_C64 ? run_fwd<float>(psi, n, passes, n_passes, ops, s)
-                         : run_fwd<double>(psi, n, passes, n_passes, ops, s);
+  return dtype == TQ_C64 ? run_fwd<float>(psi, n, passes, n_passes, ops, theta, s)
+                         : run_fwd<double>(psi, n, passes, n_passes, ops, theta, s);
 }
 
 extern "C" size_t tq_sv_adjoint_tiles_workspace_bytes(int n, int n_slots) {
@@ -296,8 +300,8 @@ extern "C" size_t tq_sv_adjoint_tiles_workspace_bytes(int n, int n_slots) {
 }
 
 extern "C" int tq_sv_adjoint_tiles(void* psi, void* lam, int n, int dtype, const tq_tile_pass* passes, int n_passes,
-                                   const tq_tile_op* ops, int n_slots, double* slot_out, void* ws, size_t ws_bytes,
-                                   void* stream) {
+                                   const tq_tile_op* ops, const double* theta, int n_slots, double* slot_out,
+                                   void* ws, size_t ws_bytes, void* stream) {
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_passes < 0 || n_slots < 0) return fail(TQ_ERR_ARG, "tq_sv_adjoint_tiles: negative count");
@@ -309,6 +313,66 @@ extern "C" int tq_sv_adjoint_tiles(void* psi, void* lam, int n, int dtype, const
   if (n_slots > 0 && (!ws || ws_bytes < need))
     return fail(TQ_ERR_WORKSPACE, "tq_sv_adjoint_tiles: workspace of %zu bytes < %zu", ws_bytes, need);
   cudaStream_t s = (cudaStream_t)stream;
-  return dtype == TQ_C64 ? run_adj<float>(psi, lam, n, passes, n_passes, ops, n_slots, slot_out, (double*)ws, s)
-                         : run_adj<double>(psi, lam, n, passes, n_passes, ops, n_slots, slot_out, (double*)ws, s);
+  return dtype == TQ_C64
+             ? run_adj<float>(psi, lam, n, passes, n_passes, ops, theta, n_slots, slot_out, (double*)ws, s)
+             : run_adj<double>(psi, lam, n, passes, n_passes, ops, theta, n_slots, slot_out, (double*)ws, s);
+}
+
+// ----------------------------------------------------------------- generator term (plain reverse sweep)
+namespace tq {
+template <typename R>
+__global__ void k_generator_im(const typename C2<R>::T* psi, const typename C2<R>::T* lam, int64_t N, uint64_t xm,
+                               uint64_t zm, uint64_t cm, cplx<R> ph, double* partials) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  while (i < N) {
+    R loc = 0;
+    for (int u = 0; u < 8 && i < N; ++u, i += stride) {
+      if (((uint64_t)i & cm) != cm) continue;
+      const typename C2<R>::T pv = psi[i];
+      const typename C2<R>::T lv = lam[i ^ (int64_t)xm];
+      const cplx<R> v = cmul(ph, cplx<R>(pv.x, pv.y));
+      const R sg = (__popcll((uint64_t)i & zm) & 1) ? R(-1) : R(1);
+      loc += sg * (lv.x * v.y - lv.y * v.x);
+    }
+    acc += (double)loc;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    partials[blockIdx.x] = s;
+  }
+}
+}  // namespace tq
+
+extern "C" int tq_sv_generator_im(const void* psi, const void* lam, int n, int dtype, uint64_t xm, uint64_t zm,
+                                  uint64_t cm, double* out_dev, void* ws, size_t ws_bytes, void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (!psi || !lam || !out_dev) return fail(TQ_ERR_ARG, "tq_sv_generator_im: NULL pointer");
+  const uint64_t full = (n >= 64) ? ~0ull : ((1ull << n) - 1);
+  if ((xm | zm | cm) & ~full) return fail(TQ_ERR_RANGE, "tq_sv_generator_im: mask has bits above n=%d", n);
+  const int64_t N = int64_t(1) << n;
+  int64_t nb = (N + 4095) / 4096;
+  if (nb > 1216) nb = 1216;
+  if (!ws || ws_bytes < sizeof(double) * nb)
+    return fail(TQ_ERR_WORKSPACE, "tq_sv_generator_im: workspace of %zu bytes < %zu", ws_bytes, sizeof(double) * nb);
+  const int ny = __builtin_popcountll(xm & zm) & 3;
+  const double phr[4] = {1, 0, -1, 0}, phi[4] = {0, 1, 0, -1};
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == TQ_C64)
+    k_generator_im<float><<<(unsigned)nb, 256, 0, s>>>((const float2*)psi, (const float2*)lam, N, xm, zm, cm,
+                                                        cplx<float>((float)phr[ny], (float)phi[ny]), (double*)ws);
+  else
+    k_generator_im<double><<<(unsigned)nb, 256, 0, s>>>((const double2*)psi, (const double2*)lam, N, xm, zm, cm,
+                                                         cplx<double>(phr[ny], phi[ny]), (double*)ws);
+  k_finalize_slots<<<1, 256, 0, s>>>((const double*)ws, (int)nb, 1, out_dev);
+  TQ_CHECK_LAUNCH("tq_sv_generator_im");
+  return TQ_OK;
 }

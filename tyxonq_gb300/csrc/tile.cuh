@@ -35,10 +35,33 @@ __device__ __forceinline__ cplx<double> op_m<double>(const tq_tile_op& o, int e)
   return cplx<double>(o.md[2 * e], o.md[2 * e + 1]);
 }
 
+__device__ __forceinline__ void rot_cs(double a, float& c, float& s) { sincosf((float)(0.5 * a), &s, &c); }
+__device__ __forceinline__ void rot_cs(double a, double& c, double& s) { sincos(0.5 * a, &s, &c); }
+
+// (m0, m1) of a kind-7 op: fixed, or built from theta for parametrised ops.
+template <typename R>
+__device__ __forceinline__ void prot_coeffs(const tq_tile_op& o, const double* theta, cplx<R>& m0, cplx<R>& m1) {
+  if (o.pidx < 0 || theta == nullptr) {
+    m0 = op_m<R>(o, 0);
+    m1 = op_m<R>(o, 1);
+    return;
+  }
+  R c, s;
+  rot_cs(o.pscale * theta[o.pidx], c, s);
+  const int ny = __popc(o.xm & o.zm) & 3;
+  // -i s i^ny
+  const R re[4] = {R(0), s, R(0), -s};
+  const R im[4] = {-s, R(0), s, R(0)};
+  m0 = cplx<R>(c, R(0));
+  m1 = cplx<R>(re[ny], im[ny]);
+}
+
 // Apply one op to tile s[0..2^t) with `nt` cooperating threads (index tid).
 // `adj` = apply the inverse (U^dagger).  No barrier inside: the caller syncs.
+// theta: device angles for ops with pidx >= 0 (may be NULL otherwise).
 template <typename R>
-__device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& o, int tid, int nt, bool adj) {
+__device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& o, int tid, int nt, bool adj,
+                                           const double* theta = nullptr) {
   const int kind = o.kind;
   const int a = o.a, b = o.b;
   if (kind == TOP_U1) {
@@ -59,6 +82,12 @@ __device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& 
     }
   } else if (kind == TOP_D1) {
     cplx<R> d0 = op_m<R>(o, 0), d1 = op_m<R>(o, 1);
+    if (o.pidx >= 0 && theta != nullptr) {  // phase(a) = diag(1, e^{ia})
+      R c, sn;
+      rot_cs(2.0 * o.pscale * theta[o.pidx], c, sn);
+      d0 = cplx<R>(R(1), R(0));
+      d1 = cplx<R>(c, sn);
+    }
     if (adj) {
       d0.y = -d0.y;
       d1.y = -d1.y;
@@ -112,14 +141,15 @@ __device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& 
       }
     }
   } else if (kind == TOP_PROT) {
-    // psi_i <- c psi_i + w * (-1)^{popc(j & zm)} psi_j  with j = i ^ xm
-    const cplx<R> c = op_m<R>(o, 0);
-    cplx<R> w = op_m<R>(o, 1);
+    // psi_i <- c psi_i + w * (-1)^{popc(j & zm)} psi_j  with j = i ^ xm, on (i & cm) == cm
+    cplx<R> c, w;
+    prot_coeffs<R>(o, theta, c, w);
     if (adj) w = cplx<R>(-w.x, -w.y);  // exp(+i t/2 P): the sin term flips sign
-    const uint32_t xm = o.xm, zm = o.zm;
+    const uint32_t xm = o.xm, zm = o.zm, cm = o.cm;
     if (xm == 0) {
       const int N = 1 << t;
       for (int i = tid; i < N; i += nt) {
+        if ((i & cm) != cm) continue;
         const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
         s[i] = cmul(cplx<R>(c.x + sg * w.x, sg * w.y), s[i]);
       }
@@ -128,6 +158,7 @@ __device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& 
       const int np = 1 << (t - 1);
       for (int p = tid; p < np; p += nt) {
         const int i = insz(p, h), j = i ^ (int)xm;
+        if ((i & cm) != cm) continue;
         const cplx<R> x = s[i], y = s[j];
         const R si = (__popc(i & zm) & 1) ? R(-1) : R(1);
         const R sj = (__popc(j & zm) & 1) ? R(-1) : R(1);
@@ -137,6 +168,27 @@ __device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& 
     }
   }
 }
+
+// f(i) = sum_t w_t (-1)^{popc(i & zy_t)} over a Pauli group's terms.
+template <typename R>
+__device__ __forceinline__ cplx<R> group_f(const tq_pauli_term* __restrict__ terms, int first, int cnt, uint64_t i) {
+  R fr = 0, fi = 0;
+  for (int t = 0; t < cnt; ++t) {
+    const uint64_t zy = __ldg(&terms[first + t].zy);
+    const R wr = (R)__ldg(&terms[first + t].w_re), wi = (R)__ldg(&terms[first + t].w_im);
+    const bool neg = __popcll(i & zy) & 1;
+    fr += neg ? -wr : wr;
+    fi += neg ? -wi : wi;
+  }
+  return cplx<R>(fr, fi);
+}
+
+// 16-byte global -> shared asynchronous copy (cp.async, L2-only caching).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Thread-partial of Im <lam| G |psi> over the tile, G|i> = [i & cm == cm]
 // i^{ny} (-1)^{popc(i & zy)} |i ^ xm> (a Pauli string with optional control

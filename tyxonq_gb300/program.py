@@ -25,10 +25,12 @@ from . import kernels as K
 from .ir import Gate
 
 TILE_OP_DTYPE = np.dtype({
-    "names": ["kind", "a", "b", "slot", "xm", "zm", "gxm", "gzm", "gcm", "gny", "mf", "md"],
-    "formats": ["<i4", "<i4", "<i4", "<i4", "<u4", "<u4", "<u4", "<u4", "<u4", "<i4", ("<f4", 32), ("<f8", 32)],
-    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 168],
-    "itemsize": 424,
+    "names": ["kind", "a", "b", "slot", "xm", "zm", "cm", "gxm", "gzm", "gcm", "gny", "pidx", "pscale", "gcoef",
+              "mf", "md"],
+    "formats": ["<i4", "<i4", "<i4", "<i4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<i4", "<i4", "<f8", "<f8",
+                ("<f4", 32), ("<f8", 32)],
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44, 48, 56, 64, 192],
+    "itemsize": 448,
 })
 TOP = {"u1": 1, "d1": 2, "u2": 3, "cx": 4, "cz": 5, "swap": 6, "prot": 7}
 TILE_KINDS = {"u1", "d1", "u2", "cx", "cz", "swap", "prot"}
@@ -254,33 +256,71 @@ def _generator(g: Gate, loc: dict) -> tuple[int, int, int, int, float] | None:
     return None
 
 
-def encode_op(rec, g: Gate, loc: dict, slot: int = -1, gen=None) -> None:
+def _rotation_masks(g: Gate, loc: dict) -> tuple[int, int, int, int] | None:
+    """(xm, zm, cm, ny) of a Pauli-rotation gate (rx/ry/rz/rxx/ryy/rzz/cry/prot)."""
+    from .ir import ROTATION_GENERATORS
+
+    if g.rot is None:
+        return None
+    name = g.rot[0]
+    if name in ROTATION_GENERATORS:
+        pairs = list(zip(g.qubits, ROTATION_GENERATORS[name]))
+        cm = 0
+    elif name == "prot":
+        pairs = list(g.pauli)
+        cm = 0
+    elif name == "cry":
+        pairs = [(g.qubits[1], "Y")]
+        cm = 1 << loc[g.qubits[0]]
+    else:
+        return None
+    xm = zm = ny = 0
+    for q, p in pairs:
+        b = 1 << loc[q]
+        if p in "XY":
+            xm |= b
+        if p in "YZ":
+            zm |= b
+        ny += p == "Y"
+    return xm, zm, cm, ny
+
+
+def encode_op(rec, g: Gate, loc: dict, slot: int = -1, gen=None, pidx: int = -1, pscale: float = 1.0,
+              gcoef: float = 0.0, as_rotation: bool = False) -> None:
+    """Fill one tq_tile_op record.  as_rotation=True encodes Pauli rotations
+    (and cry) as kind 7 (cheaper than a dense 4x4 sweep); pidx >= 0 makes the
+    device build the rotation from theta[pidx] * pscale."""
     g = _canon(g)
-    rec["kind"] = TOP[g.kind]
+    rm = _rotation_masks(g, loc) if (as_rotation or pidx >= 0 or g.kind == "prot") else None
+    rec["slot"] = slot
+    rec["pidx"] = pidx
+    rec["pscale"] = pscale
+    rec["gcoef"] = gcoef
     rec["a"] = loc[g.qubits[0]]
     rec["b"] = loc[g.qubits[1]] if len(g.qubits) > 1 else 0
-    rec["slot"] = slot
-    if g.kind == "u1":
-        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
-    elif g.kind == "d1":
-        m = np.array([g.mat[0, 0], g.mat[1, 1]], dtype=np.complex128)
-    elif g.kind == "u2":
-        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
-    elif g.kind == "prot":
-        xm = zm = ny = 0
-        for q, p in g.pauli:
-            b = 1 << loc[q]
-            if p in "XY":
-                xm |= b
-            if p in "YZ":
-                zm |= b
-            ny += p == "Y"
+    if rm is not None:
+        xm, zm, cm, ny = rm
+        rec["kind"] = TOP["prot"]
+        rec["xm"], rec["zm"], rec["cm"] = xm, zm, cm
         a = g.rot[1]
         c, s = np.cos(0.5 * a), np.sin(0.5 * a)
         m = np.array([c, -1j * s * _PH[ny & 3]], dtype=np.complex128)
-        rec["xm"], rec["zm"] = xm, zm
+    elif g.kind == "u1":
+        rec["kind"] = TOP["u1"]
+        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
+    elif g.kind == "d1":
+        rec["kind"] = TOP["d1"]
+        m = np.array([g.mat[0, 0], g.mat[1, 1]], dtype=np.complex128)
+        if pidx < 0:
+            rec["pidx"] = -1
+    elif g.kind == "u2":
+        rec["kind"] = TOP["u2"]
+        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
     else:
+        rec["kind"] = TOP[g.kind]
         m = np.zeros(0, dtype=np.complex128)
+    if pidx >= 0 and rm is None and not (g.rot is not None and g.rot[0] == "phase"):
+        raise ValueError(f"gate '{g.kind}' cannot take a device-side angle")
     if m.size:
         flat = np.stack([m.real, m.imag], axis=-1).reshape(-1)
         rec["md"][: flat.size] = flat
@@ -303,11 +343,28 @@ class EncodedTiles:
         return self.ops_dev
 
 
+def _fuse_around_params(gl: list, idx: list, params: dict | None) -> list:
+    """Fuse maximal runs of fixed gates; parametrised gates stay single ops.
+    Returns [(gate, gate index or None)]."""
+    out, run = [], []
+    for gi, g in zip(idx, gl):
+        if params is not None and gi in params:
+            out += [(x, None) for x in fuse_pass(run)]
+            run = []
+            out.append((g, gi))
+        else:
+            run.append(g)
+    out += [(x, None) for x in fuse_pass(run)]
+    return out
+
+
 def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, fuse: bool, reverse: bool = False,
-                  slots: dict | None = None, nlow: int = DEFAULT_NLOW) -> tuple[EncodedTiles, list]:
-    """Encode pass plans.  reverse=True lists passes and ops in reverse (for the
-    adjoint sweep); `slots` maps gate index -> gradient slot.  Returns the
-    encoded tiles and per-slot coefficients [(slot, coef)]."""
+                  slots: dict | None = None, params: dict | None = None,
+                  nlow: int = DEFAULT_NLOW) -> tuple[EncodedTiles, list]:
+    """Encode pass plans.  reverse=True lists passes and ops in reverse.
+    `slots` maps gate index -> gradient slot; `params` maps gate index ->
+    (pidx, pscale) for angles read from device theta.  Returns the encoded
+    tiles and [(slot, coef)] with dE/d(angle) = coef * Im<lam|G|psi>."""
     recs = []
     passes = []
     coefs = []
@@ -316,24 +373,31 @@ def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, f
         qs = pp.qubits
         loc = {q: j for j, q in enumerate(qs)}
         t = len(qs)
-        gl = [gates[i] for i in (reversed(pp.gates) if reverse else pp.gates)]
         idx = list(reversed(pp.gates)) if reverse else list(pp.gates)
+        gl = [gates[i] for i in idx]
         begin = len(recs)
         if fuse and not reverse:
-            for g in fuse_pass(gl):
+            for g, gi in _fuse_around_params(gl, idx, params):
                 r = np.zeros(1, dtype=TILE_OP_DTYPE)[0]
-                encode_op(r, g, loc)
+                if gi is None:
+                    encode_op(r, g, loc)
+                else:
+                    pidx, psc = params[gi]
+                    encode_op(r, g, loc, pidx=pidx, pscale=psc, as_rotation=True)
                 recs.append(r)
         else:
             for gi, g in zip(idx, gl):
                 r = np.zeros(1, dtype=TILE_OP_DTYPE)[0]
                 slot = -1
                 gen = None
+                pidx, psc = params[gi] if (params is not None and gi in params) else (-1, 1.0)
+                gcoef = 0.0
                 if slots is not None and gi in slots:
                     slot = slots[gi]
                     gen = _generator(g, loc)
                     coefs.append((slot, gen[4]))
-                encode_op(r, g, loc, slot, gen)
+                    gcoef = gen[4] * psc
+                encode_op(r, g, loc, slot, gen, pidx=pidx, pscale=psc, gcoef=gcoef, as_rotation=True)
                 recs.append(r)
         p = TilePass()
         p.t = t
@@ -362,22 +426,27 @@ class ForwardProgram:
     n_gates: int
     n_passes: int
 
-    def run(self, psi: torch.Tensor) -> torch.Tensor:
+    def run(self, psi: torch.Tensor, theta: torch.Tensor | None = None) -> torch.Tensor:
+        """Apply the program in place; theta (float64 device tensor) feeds the
+        ops compiled with device-side angles."""
         from .engine import execute_plain
 
         dt = K.dtype_tag(psi)
+        th = ctypes.c_void_p(theta.data_ptr()) if theta is not None else None
         for kind, obj in self.segments:
             if kind == "gate":
                 execute_plain(psi, [obj])
             else:
                 ops = obj.device_ops(psi.device)
                 nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), self.n, dt, obj.passes, obj.n_passes,
-                         ctypes.c_void_p(ops.data_ptr()), K.stream_ptr(psi.device))
+                         ctypes.c_void_p(ops.data_ptr()), th, K.stream_ptr(psi.device))
         return psi
 
 
 def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int | None = None,
-                    nlow: int = DEFAULT_NLOW, fuse: bool = True) -> ForwardProgram:
+                    nlow: int = DEFAULT_NLOW, fuse: bool = True, params: dict | None = None) -> ForwardProgram:
+    """Plan and encode a forward program.  params: gate index -> (pidx, pscale)
+    for gates whose angle is read from device theta at run time."""
     gates = [_canon(g) for g in gates]
     if t is None:
         t = default_tile_bits(n, dtype)
@@ -388,7 +457,7 @@ def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int
         if s.kind == "gate":
             out.append(("gate", gates[s.gate]))
         else:
-            enc, _ = encode_passes(n, s.passes, gates, fuse=fuse, nlow=nlow)
+            enc, _ = encode_passes(n, s.passes, gates, fuse=fuse, params=params, nlow=nlow)
             out.append(("tiles", enc))
             npass += enc.n_passes
     return ForwardProgram(n, out, len(gates), npass)
