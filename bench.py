@@ -144,12 +144,82 @@ def _ref_one(arg):
 
 
 # ------------------------------------------------------------------ our arm
+def _events():
+    import torch
+
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def bench_gate_kernels(args, dev):
+    """28 qubits, depth 40 random circuit, complex64: fused tile passes (per-launch
+    events) and the one-launch-per-gate engine."""
+    import ctypes
+
+    import torch
+
+    from tyxonq_gb300 import _native as nat
+    from tyxonq_gb300 import kernels as K
+    from tyxonq_gb300.engine import execute_plain
+    from tyxonq_gb300.ir import lower_ops
+    from tyxonq_gb300.program import compile_forward
+    from tyxonq_gb300.workloads import random_circuit
+
+    class _C:
+        def __init__(self, n, ops):
+            self.num_qubits, self.ops = n, ops
+
+    n2 = 28
+    gates, _ = lower_ops(_C(n2, random_circuit(n2, 40, seed=1)), mode="run")
+    prog = compile_forward(gates, n2, torch.complex64)
+    psi = K.init_statevector(n2, dtype=torch.complex64)
+    st = torch.cuda.current_stream()
+    for _ in range(2):
+        prog.run(psi)
+    torch.cuda.synchronize()
+    launch_ms, step_ms = [], []
+    for _ in range(2):
+        a, b = _events()
+        a.record(st)
+        evs = []
+        for kind, obj in prog.segments:
+            ops_d = obj.device_ops(psi.device)
+            for p in range(obj.n_passes):
+                x, y = _events()
+                x.record(st)
+                nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), n2, 0, ctypes.byref(obj.passes[p]), 1,
+                         ctypes.c_void_p(ops_d.data_ptr()), None, K.stream_ptr())
+                y.record(st)
+                evs.append((x, y))
+        b.record(st)
+        torch.cuda.synchronize()
+        step_ms.append(a.elapsed_time(b))
+        launch_ms += [x.elapsed_time(y) for x, y in evs]
+    psi2 = K.init_statevector(n2, dtype=torch.complex64)
+    execute_plain(psi2, gates[:40])
+    torch.cuda.synchronize()
+    a, b = _events()
+    a.record()
+    execute_plain(psi2, gates)
+    b.record()
+    torch.cuda.synchronize()
+    plain_ms = a.elapsed_time(b)
+    del psi, psi2
+    torch.cuda.empty_cache()
+    N, S = 1 << n2, 8
+    avg_launch = sum(launch_ms) / len(launch_ms)
+    return {"fused_ms": sum(step_ms) / len(step_ms), "plain_ms": plain_ms, "passes": prog.n_passes,
+            "gates": len(gates), "avg_pass_ms": avg_launch, "pass_alg_bytes": 2 * N * S,
+            "pass_gbs": 2 * N * S / (avg_launch * 1e-3) / 1e9,
+            "plain_gbs_equiv": len(gates) * 2 * N * S / (plain_ms * 1e-3) / 1e9}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--count", type=int, default=4096)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -161,10 +231,8 @@ def main():
     import __graft_entry__ as ge
 
     ge.build()
-    from tyxonq_gb300 import kernels as K
-    from tyxonq_gb300.ir import lower_ops
-    from tyxonq_gb300.program import compile_forward
-    from tyxonq_gb300.workloads import random_circuit
+    from tyxonq_gb300.batch import BatchedVQE, plain_energy_and_grad
+    from tyxonq_gb300.workloads import batched_vqe
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -175,112 +243,111 @@ def main():
 
         dist.init_process_group("nccl")
 
-    class _C:
-        def __init__(self, n, ops):
-            self.num_qubits, self.ops = n, ops
-
-    # ---------------- config 2: 28 qubits, depth 40, complex64, fused tile passes
-    n2 = 28
-    ops = random_circuit(n2, 40, seed=1)
-    gates, _ = lower_ops(_C(n2, ops), mode="run")
-    prog = compile_forward(gates, n2, torch.complex64)
-    psi = K.init_statevector(n2, dtype=torch.complex64)
-    S = 8
-    N = 1 << n2
-    launch_ms = []
-
-    def timed_fused():
-        # per-launch events on the launching stream
-        st = torch.cuda.current_stream()
-        evs = []
-        from tyxonq_gb300 import _native as nat
-        import ctypes
-
-        for kind, obj in prog.segments:
-            assert kind == "tiles"
-            ops_d = obj.device_ops(psi.device)
-            for p in range(obj.n_passes):
-                a = torch.cuda.Event(enable_timing=True)
-                b = torch.cuda.Event(enable_timing=True)
-                a.record(st)
-                nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), n2, 0,
-                         ctypes.byref(obj.passes[p]), 1, ctypes.c_void_p(ops_d.data_ptr()), None, K.stream_ptr())
-                b.record(st)
-                evs.append((a, b))
-        return evs
-
+    # ---------------- batched workload: every rank evaluates its own 4096 instances (weak scaling)
+    insts = batched_vqe(args.count, seed=3 + 1000 * rank)
+    t0 = time.perf_counter()
+    bv = BatchedVQE(insts, dtype=torch.complex64)
+    build_s = time.perf_counter() - t0
+    theta_host = torch.from_numpy(np.concatenate([i.theta for i in insts])).pin_memory()
+    bv.set_theta(theta_host)
+    bv.capture()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
     for _ in range(args.warmup):
-        prog.run(psi)
+        bv.run()
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = []
     with ClockSampler(dev) as clk:
-        t_total = 0.0
         for _ in range(args.steps):
-            torch.cuda.synchronize()
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            a, b = _events()
             a.record()
-            evs = timed_fused()
+            bv.run()
             b.record()
             torch.cuda.synchronize()
-            t_total += a.elapsed_time(b)
-            launch_ms += [x.elapsed_time(y) for x, y in evs]
-    fused_ms = t_total / args.steps
-    n_pass = prog.n_passes
-    avg_launch_ms = sum(launch_ms) / len(launch_ms)
-    alg_bytes = 2 * N * S
-    achieved = alg_bytes / (avg_launch_ms * 1e-3) / 1e9
-    peak, peak_kind = _peaks()
+            step_ms.append(a.elapsed_time(b))
+    if world > 1:
+        dist.barrier()
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * len(insts) / (ms * 1e-3)
 
-    # unfused plain engine on the same circuit (one step)
-    from tyxonq_gb300.engine import execute_plain
-
-    psi2 = K.init_statevector(n2, dtype=torch.complex64)
-    execute_plain(psi2, gates[:40])
+    # ---------------- e2e: host theta -> device, evaluate, energies + gradients -> host
+    e_host = torch.empty(bv.count, dtype=torch.float64).pin_memory()
+    g_host = torch.empty(bv.grads.numel(), dtype=torch.float64).pin_memory()
     torch.cuda.synchronize()
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    a.record()
-    execute_plain(psi2, gates)
-    b.record()
-    torch.cuda.synchronize()
-    plain_ms = a.elapsed_time(b)
-    del psi, psi2
-    torch.cuda.empty_cache()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = _events()
+        a.record()
+        bv.run(theta_host)
+        e_host.copy_(bv.energies, non_blocking=True)
+        g_host.copy_(bv.grads, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        e2e_ms.append(a.elapsed_time(b))
+    e2e = world * len(insts) / (sum(e2e_ms) / len(e2e_ms) * 1e-3)
+    h2d = theta_host.numel() * 8
+    d2h = (e_host.numel() + g_host.numel()) * 8
+    energies = e_host.numpy().copy()
 
-    # ---------------- interim batched value: per-instance fused adjoint on a sample
-    from tyxonq_gb300.adjoint import AdjointEstimator, ParamGate
-    from tyxonq_gb300.ir import Gate, _rot_gate
-    from tyxonq_gb300.workloads import batched_vqe
-
-    insts = batched_vqe(4096, seed=3)[:64]
-    ests = []
-    for inst in insts:
-        pg = [ParamGate(_rot_gate(nm, qs, 0.0), p) if p is not None else ParamGate(Gate(nm, qs))
-              for nm, qs, p in inst.structure()]
-        ests.append((AdjointEstimator(inst.n, pg, inst.n_params, inst.H), inst.theta))
-    for e, th in ests[:4]:
-        e.energy_and_grad(th)
+    # ---------------- plain single-circuit engine on an every-8th-instance sample
+    sample = list(range(0, len(insts), 8))
+    plain_energy_and_grad(insts[sample[0]])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for e, th in ests:
-        e.energy_and_grad(th)
+    worst = 0.0
+    for i in sample:
+        e_p, _ = plain_energy_and_grad(insts[i])
+        worst = max(worst, abs(e_p - energies[i]) / max(1.0, insts[i].H.one_norm()))
     torch.cuda.synchronize()
-    seq_s = time.perf_counter() - t0
-    evals_s = len(ests) / seq_s
+    plain_evals = len(sample) / (time.perf_counter() - t0)
 
+    # ---------------- 28q gate kernels (memory-bound case) + roofline
+    gk = bench_gate_kernels(args, dev)
+    peak, peak_kind = _peaks()
+
+    # ---------------- CPU baseline: oracle port, bounded sample, one core
+    cpu = None
+    if rank == 0:
+        from oracle import sv
+
+        rng = np.random.default_rng(11)
+        pick = [i for i in rng.permutation(len(insts)) if insts[i].n <= 14][:6]
+        t0 = time.perf_counter()
+        for i in pick:
+            inst = insts[i]
+            sv.grad_adjoint(inst.n, [(nm, list(qs), p, 1.0) for nm, qs, p in inst.structure()], inst.theta,
+                            inst.H.codes, inst.H.coeffs)
+        dt_cpu = time.perf_counter() - t0
+        cpu = {"value": len(pick) / dt_cpu, "unit": "evals/s", "cores": 1, "kind": "port",
+               "sample": f"{len(pick)} random instances with n<=14 of the 4096 (energy + adjoint gradient, c128)"}
+
+    launches_per_step = len(bv.launch_order)
     line = {
-        "metric": METRIC, "value": evals_s, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": seq_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": {"workload": "interim: first 64 instances of batched_vqe_4096, sequential fused adjoint",
-                   "l2": "28q state 2 GiB > L2"},
-        "gate_kernels": {"fused_28q_depth40_ms": fused_ms, "plain_28q_depth40_ms": plain_ms, "passes": n_pass,
-                         "gates": len(gates)},
-        "roofline": {"kernel": "k_tile_forward (28q c64 tile pass)", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "peak_kind": peak_kind},
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+        "config": {"workload": f"batched_vqe_{len(insts)}: n~U{{8..20}}, HEA depth~U{{2..8}} [RY;RZ;CX ladder], "
+                               "50-500 random Pauli terms (weight 1-4, N(0,1)), energy + adjoint gradient",
+                   "l2": "512 MiB buffer written between timed steps", "graph": "CUDA graph replay",
+                   "classes": {c.name: len(c.work) for c in bv.launch_order}, "structures": bv.n_structures,
+                   "build_s": build_s},
+        "plain_gpu": {"value": plain_evals, "unit": "evals/s", "sample": f"{len(sample)} of {len(insts)} (every 8th)",
+                      "speedup_batched": value / world / plain_evals, "max_energy_diff_rel": worst},
+        "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gate_kernels_28q": gk,
+        "roofline": {"kernel": "k_tile_forward (28-qubit complex64 tile pass, 2*N*8 B per launch)", "bound": "hbm",
+                     "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,
+                     "traffic": None, "peak_kind": peak_kind},
+        "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": len(launch_ms),
+        "gpu_launches": launches_per_step * args.steps,
     }
     if rank == 0:
         print(json.dumps(line))

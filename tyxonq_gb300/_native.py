@@ -77,6 +77,9 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_generator_im": (c_int, [_P, _P, c_int, c_int, c_uint64, c_uint64, c_uint64, _P, _P, c_size_t, _P]),
     "tq_sv_inner_workspace_bytes": (c_size_t, [c_int]),
     "tq_sv_inner_re": (c_int, [_P, _P, c_int, c_int, _P, _P, c_size_t, _P]),
+    "tq_batch_smem_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
+    "tq_batch_run": (c_int, [c_int, _P, _P, c_int, c_int, c_int, c_int, c_int, c_size_t, _P, _P, _P, _P, _P, _P,
+                             _P, _P, _P, _P]),
 }
 
 _lock = threading.Lock()

@@ -100,17 +100,17 @@ class PauliSum:
             return self._packed
         flip, zy, ny = self.masks()
         order = np.lexsort((zy, flip))
+        pw = np.array(_I_POW)[ny[order] & 3]
         terms = np.zeros(self.n_terms, dtype=TERM_DTYPE)
-        groups = []
-        for pos, k in enumerate(order):
-            re, im = _I_POW[int(ny[k]) & 3]
-            terms[pos] = (zy[k], self.coeffs[k] * re, self.coeffs[k] * im)
-            if not groups or groups[-1][0] != flip[k]:
-                groups.append([flip[k], pos, 0])
-            groups[-1][2] += 1
-        g = np.zeros(len(groups), dtype=GROUP_DTYPE)
-        for i, (f, first, cnt) in enumerate(groups):
-            g[i] = (f, first, cnt)
+        terms["zy"] = zy[order]
+        terms["w_re"] = self.coeffs[order] * pw[:, 0] if self.n_terms else 0
+        terms["w_im"] = self.coeffs[order] * pw[:, 1] if self.n_terms else 0
+        fs = flip[order]
+        starts = np.flatnonzero(np.r_[True, fs[1:] != fs[:-1]]) if self.n_terms else np.zeros(0, np.int64)
+        g = np.zeros(len(starts), dtype=GROUP_DTYPE)
+        g["flip"] = fs[starts]
+        g["first_term"] = starts
+        g["n_terms"] = np.diff(np.r_[starts, self.n_terms])
         self._packed = (g, terms)
         return self._packed
 
@@ -171,10 +171,12 @@ def tfim_terms(n: int, hx: float = 1.0, hzz: float = 1.0, pbc: bool = False) -> 
 def random_pauli_sum(n: int, n_terms: int, rng: np.random.Generator, max_weight: int = 4) -> PauliSum:
     """Random H: n_terms terms, weight uniform in 1..max_weight on distinct
     random qubits, Paulis uniform in {X,Y,Z}, coefficients N(0,1)."""
-    codes = np.zeros((n_terms, n), dtype=np.int8)
-    for k in range(n_terms):
-        w = int(rng.integers(1, min(max_weight, n) + 1))
-        qs = rng.choice(n, size=w, replace=False)
-        codes[k, qs] = rng.integers(1, 4, size=w)
+    w = rng.integers(1, min(max_weight, n) + 1, size=n_terms)
+    # the first w[k] entries of a random permutation of the qubits are the support
+    perm = np.argsort(rng.random((n_terms, n)), axis=1)
+    rank = np.empty_like(perm)
+    np.put_along_axis(rank, perm, np.arange(n)[None, :].repeat(n_terms, 0), axis=1)
+    on = rank < w[:, None]
+    codes = np.where(on, rng.integers(1, 4, size=(n_terms, n)), 0).astype(np.int8)
     coeffs = rng.standard_normal(n_terms)
     return PauliSum(n, codes, coeffs)

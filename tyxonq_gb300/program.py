@@ -72,8 +72,10 @@ class Segment:
     gate: int = -1
 
 
-def plan_passes(gates: Sequence[Gate], n: int, t: int, nlow: int = DEFAULT_NLOW) -> list[Segment]:
-    """Greedy DAG scheduling of `gates` into tile passes of t local qubits."""
+def plan_passes(gates: Sequence[Gate], n: int, t: int, nlow: int = DEFAULT_NLOW,
+                max_ops: int | None = None) -> list[Segment]:
+    """Greedy DAG scheduling of `gates` into tile passes of t local qubits
+    (at most max_ops gates per pass when given)."""
     t = min(t, n)
 
     def fits(g: Gate) -> bool:
@@ -118,7 +120,7 @@ def plan_passes(gates: Sequence[Gate], n: int, t: int, nlow: int = DEFAULT_NLOW)
             continue
         L = set(low)
         order: list[int] = []
-        while True:
+        while max_ops is None or len(order) < max_ops:
             best, best_cost = None, None
             for i in ready:
                 g = gates[i]
@@ -285,48 +287,62 @@ def _rotation_masks(g: Gate, loc: dict) -> tuple[int, int, int, int] | None:
     return xm, zm, cm, ny
 
 
-def encode_op(rec, g: Gate, loc: dict, slot: int = -1, gen=None, pidx: int = -1, pscale: float = 1.0,
-              gcoef: float = 0.0, as_rotation: bool = False) -> None:
-    """Fill one tq_tile_op record.  as_rotation=True encodes Pauli rotations
-    (and cry) as kind 7 (cheaper than a dense 4x4 sweep); pidx >= 0 makes the
-    device build the rotation from theta[pidx] * pscale."""
+def op_fields(g: Gate, loc: dict, slot: int = -1, gen=None, pidx: int = -1, pscale: float = 1.0,
+              gcoef: float = 0.0, as_rotation: bool = False) -> tuple:
+    """Field values of one tq_tile_op: (kind, a, b, slot, xm, zm, cm, gxm, gzm,
+    gcm, gny, pidx, pscale, gcoef, matrix entries or None).  as_rotation=True
+    encodes Pauli rotations (and cry) as kind 7, which is cheaper than a dense
+    4x4 sweep; pidx >= 0 makes the device build the rotation from
+    theta[pidx] * pscale."""
     g = _canon(g)
     rm = _rotation_masks(g, loc) if (as_rotation or pidx >= 0 or g.kind == "prot") else None
-    rec["slot"] = slot
-    rec["pidx"] = pidx
-    rec["pscale"] = pscale
-    rec["gcoef"] = gcoef
-    rec["a"] = loc[g.qubits[0]]
-    rec["b"] = loc[g.qubits[1]] if len(g.qubits) > 1 else 0
+    a = loc[g.qubits[0]]
+    b = loc[g.qubits[1]] if len(g.qubits) > 1 else 0
+    xm = zm = cm = 0
     if rm is not None:
         xm, zm, cm, ny = rm
-        rec["kind"] = TOP["prot"]
-        rec["xm"], rec["zm"], rec["cm"] = xm, zm, cm
-        a = g.rot[1]
-        c, s = np.cos(0.5 * a), np.sin(0.5 * a)
+        kind = TOP["prot"]
+        ang = g.rot[1]
+        c, s = np.cos(0.5 * ang), np.sin(0.5 * ang)
         m = np.array([c, -1j * s * _PH[ny & 3]], dtype=np.complex128)
-    elif g.kind == "u1":
-        rec["kind"] = TOP["u1"]
+    elif g.kind in ("u1", "u2"):
+        kind = TOP[g.kind]
         m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
     elif g.kind == "d1":
-        rec["kind"] = TOP["d1"]
+        kind = TOP["d1"]
         m = np.array([g.mat[0, 0], g.mat[1, 1]], dtype=np.complex128)
-        if pidx < 0:
-            rec["pidx"] = -1
-    elif g.kind == "u2":
-        rec["kind"] = TOP["u2"]
-        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
     else:
-        rec["kind"] = TOP[g.kind]
-        m = np.zeros(0, dtype=np.complex128)
+        kind = TOP[g.kind]
+        m = None
     if pidx >= 0 and rm is None and not (g.rot is not None and g.rot[0] == "phase"):
         raise ValueError(f"gate '{g.kind}' cannot take a device-side angle")
-    if m.size:
-        flat = np.stack([m.real, m.imag], axis=-1).reshape(-1)
-        rec["md"][: flat.size] = flat
-        rec["mf"][: flat.size] = flat.astype(np.float32)
-    if gen is not None:
-        rec["gxm"], rec["gzm"], rec["gcm"], rec["gny"] = gen[0], gen[1], gen[2], gen[3]
+    gx, gz, gc, gn = gen[:4] if gen is not None else (0, 0, 0, 0)
+    return (kind, a, b, slot, xm, zm, cm, gx, gz, gc, gn, pidx, pscale, gcoef, m)
+
+
+_SCALAR_FIELDS = ["kind", "a", "b", "slot", "xm", "zm", "cm", "gxm", "gzm", "gcm", "gny", "pidx", "pscale", "gcoef"]
+
+
+def pack_ops(fields: list) -> np.ndarray:
+    """Column-wise fill of a tq_tile_op array from op_fields tuples."""
+    arr = np.zeros(len(fields), dtype=TILE_OP_DTYPE)
+    if not fields:
+        return arr
+    for k, name in enumerate(_SCALAR_FIELDS):
+        arr[name] = [f[k] for f in fields]
+    for size in (2, 4, 16):
+        idx = [i for i, f in enumerate(fields) if f[14] is not None and f[14].size == size]
+        if idx:
+            M = np.stack([fields[i][14] for i in idx])
+            flat = np.stack([M.real, M.imag], axis=-1).reshape(len(idx), -1)
+            arr["md"][idx, : 2 * size] = flat
+            arr["mf"][idx, : 2 * size] = flat.astype(np.float32)
+    return arr
+
+
+def encode_op(rec, g: Gate, loc: dict, **kw) -> None:
+    """Fill one tq_tile_op record (see op_fields)."""
+    rec[...] = pack_ops([op_fields(g, loc, **kw)])[0]
 
 
 @dataclass
@@ -365,7 +381,7 @@ def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, f
     `slots` maps gate index -> gradient slot; `params` maps gate index ->
     (pidx, pscale) for angles read from device theta.  Returns the encoded
     tiles and [(slot, coef)] with dE/d(angle) = coef * Im<lam|G|psi>."""
-    recs = []
+    fields = []
     passes = []
     coefs = []
     seq = list(reversed(plans)) if reverse else list(plans)
@@ -375,19 +391,16 @@ def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, f
         t = len(qs)
         idx = list(reversed(pp.gates)) if reverse else list(pp.gates)
         gl = [gates[i] for i in idx]
-        begin = len(recs)
+        begin = len(fields)
         if fuse and not reverse:
             for g, gi in _fuse_around_params(gl, idx, params):
-                r = np.zeros(1, dtype=TILE_OP_DTYPE)[0]
                 if gi is None:
-                    encode_op(r, g, loc)
+                    fields.append(op_fields(g, loc))
                 else:
                     pidx, psc = params[gi]
-                    encode_op(r, g, loc, pidx=pidx, pscale=psc, as_rotation=True)
-                recs.append(r)
+                    fields.append(op_fields(g, loc, pidx=pidx, pscale=psc, as_rotation=True))
         else:
             for gi, g in zip(idx, gl):
-                r = np.zeros(1, dtype=TILE_OP_DTYPE)[0]
                 slot = -1
                 gen = None
                 pidx, psc = params[gi] if (params is not None and gi in params) else (-1, 1.0)
@@ -397,19 +410,17 @@ def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, f
                     gen = _generator(g, loc)
                     coefs.append((slot, gen[4]))
                     gcoef = gen[4] * psc
-                encode_op(r, g, loc, slot, gen, pidx=pidx, pscale=psc, gcoef=gcoef, as_rotation=True)
-                recs.append(r)
+                fields.append(op_fields(g, loc, slot, gen, pidx=pidx, pscale=psc, gcoef=gcoef, as_rotation=True))
         p = TilePass()
         p.t = t
         p.nlow = min(pp.nlow, t)
         p.op_begin = begin
-        p.op_end = len(recs)
+        p.op_end = len(fields)
         for j, q in enumerate(qs):
             p.pos[j] = n - 1 - q
         passes.append(p)
     arr = (TilePass * max(len(passes), 1))(*passes)
-    ops = np.array(recs, dtype=TILE_OP_DTYPE) if recs else np.zeros(0, dtype=TILE_OP_DTYPE)
-    return EncodedTiles(arr, len(passes), ops), coefs
+    return EncodedTiles(arr, len(passes), pack_ops(fields)), coefs
 
 
 # ---------------------------------------------------------------- execution
