@@ -135,6 +135,23 @@ TQ_API size_t tq_sv_sample_workspace_bytes(int n, int64_t shots);
 TQ_API int tq_sv_sample(const void* psi, int n, int dtype, int64_t shots, uint64_t seed,
                  int64_t* out_indices, void* ws, size_t ws_bytes, void* stream);
 
+/* tq_sv_sample for callers that cannot allocate device memory.  No
+ * counterpart in the reference.  Some callers cannot call cudaMalloc or hand
+ * over a workspace: a host runtime that owns the device memory budget, or a
+ * latency-critical loop in which an allocation (and the device
+ * synchronisation it can imply) is not allowed.  This entry point takes only
+ * the state and the output; its scratch is a fixed 8 MiB array in the
+ * library's device memory (held on every GPU that loads the library, until
+ * the process exits).  Requests whose tq_sv_sample_workspace_bytes(n, shots)
+ * exceeds 8 MiB fail with TQ_ERR_RANGE (at 28 qubits that is about 980,000
+ * shots).  The first call on a device looks the scratch address up
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the one scratch array: calls that overlap on the GPU
+ * (different streams, or different host threads) race and must be ordered by
+ * the caller.  Results equal tq_sv_sample's for the same arguments. */
+TQ_API int tq_sv_sample_noalloc(const void* psi, int n, int dtype, int64_t shots, uint64_t seed,
+                                int64_t* out_indices, void* stream);
+
 /* ------------------------------------------------------------ Pauli sums */
 
 /* A Pauli-sum Hamiltonian H = sum_k c_k P_k in flip-mask groups.

@@ -67,6 +67,7 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_norm2": (c_int, [_P, c_int, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_sample_workspace_bytes": (c_size_t, [c_int, c_int64]),
     "tq_sv_sample": (c_int, [_P, c_int, c_int, c_int64, c_uint64, _P, _P, c_size_t, _P]),
+    "tq_sv_sample_noalloc": (c_int, [_P, c_int, c_int, c_int64, c_uint64, _P, _P]),
     "tq_sv_pauli_expectation_workspace_bytes": (c_size_t, [c_int, c_int]),
     "tq_sv_pauli_expectation": (c_int, [_P, c_int, c_int, _P, c_int, _P, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_apply_pauli_sum": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, c_int, _P]),

@@ -619,3 +619,49 @@ extern "C" int tq_sv_sample(const void* psi, int n, int dtype, int64_t shots, ui
   TQ_CHECK_LAUNCH("tq_sv_sample");
   return TQ_OK;
 }
+
+// ----------------------------------------------------------------- sampling without allocation
+// Scratch for tq_sv_sample_noalloc: a fixed device array that lives as long as
+// the library is loaded, one copy per GPU that uses it.  Host code cannot
+// use the symbol itself as a device address, so the address is looked up
+// once per device with cudaGetSymbolAddress and cached.
+#define TQ_NOALLOC_SCRATCH_BYTES (size_t(8) << 20)
+static __device__ __align__(256) unsigned char g_sample_scratch[TQ_NOALLOC_SCRATCH_BYTES];
+
+#include <mutex>
+
+namespace tq {
+static std::mutex g_scratch_mu;
+static void* g_scratch_ptr[64] = {nullptr};
+}  // namespace tq
+
+extern "C" int tq_sv_sample_noalloc(const void* psi, int n, int dtype, int64_t shots, uint64_t seed,
+                                    int64_t* out_indices, void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (shots < 0) return fail(TQ_ERR_ARG, "tq_sv_sample_noalloc: negative shots");
+  const size_t need = tq_sv_sample_workspace_bytes(n, shots);
+  if (need > TQ_NOALLOC_SCRATCH_BYTES)
+    return fail(TQ_ERR_RANGE,
+                "tq_sv_sample_noalloc: n=%d with %lld shots needs %zu bytes of scratch, above the fixed %zu bytes; "
+                "use tq_sv_sample with a caller-provided workspace",
+                n, (long long)shots, need, (size_t)TQ_NOALLOC_SCRATCH_BYTES);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "tq_sv_sample_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(TQ_ERR_RANGE, "tq_sv_sample_noalloc: device ordinal %d", dev);
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_sample_scratch);
+      if (e != cudaSuccess) return cuda_status(e, "tq_sv_sample_noalloc: cudaGetSymbolAddress");
+      g_scratch_ptr[dev] = p;
+    }
+    scratch = g_scratch_ptr[dev];
+  }
+  // Every scratch word the sampler reads is written earlier in the same call
+  // (chunk sums, scans, spacings), so the previous call's contents need no clearing.
+  return tq_sv_sample(psi, n, dtype, shots, seed, out_indices, scratch, TQ_NOALLOC_SCRATCH_BYTES, stream);
+}
