@@ -228,6 +228,22 @@ typedef struct {
   int32_t pos[TQ_TILE_MAX_BITS];
 } tq_tile_pass;
 
+/* Register stage of a staged tile pass: 4 local bit positions (ascending) whose
+ * 16 amplitudes each thread holds in registers while ops[op_begin..op_end)
+ * (bit indices / masks in register space 0..3) are applied. */
+typedef struct {
+  int32_t bits[4];
+  int32_t op_begin;
+  int32_t op_end;
+} tq_tile_stage;
+
+/* Forward staged passes: like tq_sv_run_tiles, but each pass's
+ * [op_begin, op_end) indexes `stages` (device), and each stage applies its ops
+ * in registers (one shared-memory sweep per stage instead of per op).  Needs
+ * 9 <= t <= 14 (complex64) / 13 (complex128); CTAs of 2^(t-4) threads. */
+TQ_API int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
+                            const tq_tile_stage* stages, const tq_tile_op* ops, const double* theta, void* stream);
+
 /* Largest t supported for a dtype (shared-memory capacity). */
 TQ_API int tq_sv_tile_max_bits(int dtype);
 

@@ -135,6 +135,43 @@ def _emulate_tiles(psi, n, enc):
             idx = np.array([base + sum(((j >> k) & 1) << pos[k] for k in range(t)) for j in range(1 << t)])
             s = psi[idx]
             for o in ops[pa.op_begin:pa.op_end]:
+                s = _apply_local(s, o, t)
+            psi[idx] = s
+    return psi
+
+
+def _emulate_staged(psi, n, enc):
+    """NumPy emulation of k_staged_forward: per stage, every thread's 16
+    register amplitudes get the stage's ops in register-bit space."""
+    psi = psi.copy()
+    for p in range(enc.n_passes):
+        pa = enc.passes[p]
+        t = pa.t
+        pos = [pa.pos[j] for j in range(t)]
+        nonloc = [b for b in range(n) if b not in pos]
+        for g in range(1 << (n - t)):
+            base = sum(((g >> k) & 1) << b for k, b in enumerate(nonloc))
+            idx = np.array([base + sum(((j >> k) & 1) << pos[k] for k in range(t)) for j in range(1 << t)])
+            s = psi[idx]
+            for st in enc.stages_host[pa.op_begin:pa.op_end]:
+                bits = [int(b) for b in st["bits"]]
+                rest = [b for b in range(t) if b not in bits]
+                for tid in range(1 << (t - 4)):
+                    b0 = sum(((tid >> k) & 1) << b for k, b in enumerate(rest))
+                    ridx = np.array([b0 + sum(((i >> k) & 1) << bits[k] for k in range(4)) for i in range(16)])
+                    v = s[ridx]
+                    for o in enc.ops_host[st["op_begin"]:st["op_end"]]:
+                        v = _apply_local(v, o, 4)
+                    s[ridx] = v
+            psi[idx] = s
+    return psi
+
+
+def _apply_local(s, o, t):
+    s = s.copy()
+    if True:
+        if True:
+            if True:
                 m = o["md"][0::2] + 1j * o["md"][1::2]
                 a, b = int(o["a"]), int(o["b"])
                 j = np.arange(1 << t)
@@ -171,8 +208,24 @@ def _emulate_tiles(psi, n, enc):
                     s = np.where(on, new, s)
                 else:
                     raise AssertionError("unexpected op kind")
-            psi[idx] = s
-    return psi
+    return s
+
+
+def test_staged_encoding_emulated_matches_oracle():
+    n = 11
+    ops = random_circuit(n, 8, seed=12)
+    ops += [("rxx", 0, 9, 0.4), ("cry", 3, 10, 1.3), ("iswap", 2, 8)]
+    gates, _ = lower_ops(_C(n, ops), mode="run")
+    ref = sv.init_state(n)
+    for g in gates:
+        ref = _oracle_apply(ref, g, n) if g.kind != "u2" or g.rot is None else sv.apply_kq(ref, g.mat, list(g.qubits), n)
+    segs = P.plan_passes(gates, n, 9, nlow=3)
+    psi = sv.init_state(n)
+    for s in segs:
+        enc = P.encode_staged(n, s.passes, [P._canon(g) for g in gates])
+        assert len(enc.stages_host) < sum(len(pp.gates) for pp in s.passes)
+        psi = _emulate_staged(psi, n, enc)
+    np.testing.assert_allclose(psi, ref, atol=1e-12)
 
 
 @pytest.mark.parametrize("fuse", [False, True])

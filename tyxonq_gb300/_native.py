@@ -72,6 +72,7 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_pauli_expectation": (c_int, [_P, c_int, c_int, _P, c_int, _P, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_apply_pauli_sum": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, c_int, _P]),
     "tq_sv_tile_max_bits": (c_int, [c_int]),
+    "tq_sv_run_staged": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P, _P, _P]),
     "tq_sv_run_tiles": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P, _P]),
     "tq_sv_adjoint_tiles_workspace_bytes": (c_size_t, [c_int, c_int]),
     "tq_sv_adjoint_tiles": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, _P, c_int, _P, _P, c_size_t, _P]),

@@ -5,7 +5,7 @@
 // all the pass's gates are applied in shared memory, and the tile is written
 // back once: algorithmic bytes 2*N*S per pass (4*N*S for the adjoint pass,
 // which carries psi and lambda), however many gates the pass holds.
-#include "tile.cuh"
+#include "stage.cuh"
 
 namespace tq {
 
@@ -375,4 +375,119 @@ extern "C" int tq_sv_generator_im(const void* psi, const void* lam, int n, int d
   k_finalize_slots<<<1, 256, 0, s>>>((const double*)ws, (int)nb, 1, out_dev);
   TQ_CHECK_LAUNCH("tq_sv_generator_im");
   return TQ_OK;
+}
+
+// ----------------------------------------------------------------- register-staged forward passes
+namespace tq {
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Issue (without waiting) the async copy of one tile into a padded buffer.
+template <typename R>
+__device__ __forceinline__ void staged_issue_load(cplx<R>* s, const typename C2<R>::T* g, int64_t base,
+                                                  const int64_t* hoff, const PassArgs& P) {
+  constexpr int A = 16 / sizeof(cplx<R>);
+  const int nc = (1 << P.t) / A;
+  const int lm = (1 << P.nlow) - 1;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    const int j = c * A;
+    cp_async16(&s[pphys(j)], &g[base + hoff[j >> P.nlow] + (j & lm)]);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void staged_store(const cplx<R>* s, typename C2<R>::T* g, int64_t base,
+                                             const int64_t* hoff, const PassArgs& P) {
+  constexpr int A = 16 / sizeof(cplx<R>);
+  const int nc = (1 << P.t) / A;
+  const int lm = (1 << P.nlow) - 1;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    const int j = c * A;
+    *reinterpret_cast<float4*>(&g[base + hoff[j >> P.nlow] + (j & lm)]) =
+        *reinterpret_cast<const float4*>(&s[pphys(j)]);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(512, 1)
+    k_staged_forward(typename C2<R>::T* psi, int n, const PassArgs P, const tq_tile_stage* __restrict__ stages,
+                     const tq_tile_op* __restrict__ ops, const double* __restrict__ theta, int dbuf) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int PT = padded_len(P.t);
+  cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem);
+  cplx<R>* buf1 = buf0 + (dbuf ? PT : 0);
+  int64_t* hoff = reinterpret_cast<int64_t*>(smem + (size_t)(dbuf ? 2 : 1) * PT * sizeof(cplx<R>));
+  build_hoff(hoff, P);
+  __syncthreads();
+  const int64_t ntiles = int64_t(1) << (n - P.t);
+  int64_t g = blockIdx.x;
+  if (g < ntiles) staged_issue_load<R>(buf0, psi, tile_base(g, P), hoff, P);
+  cp_async_commit();
+  int cur = 0;
+  for (; g < ntiles; g += gridDim.x) {
+    const int64_t gn = g + gridDim.x;
+    cplx<R>* s = cur ? buf1 : buf0;
+    if (dbuf) {
+      if (gn < ntiles) staged_issue_load<R>(cur ? buf0 : buf1, psi, tile_base(gn, P), hoff, P);
+      cp_async_commit();
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
+    }
+    __syncthreads();
+    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta, false);
+    staged_store<R>(s, psi, tile_base(g, P), hoff, P);
+    __syncthreads();
+    if (!dbuf && gn < ntiles) {
+      staged_issue_load<R>(buf0, psi, tile_base(gn, P), hoff, P);
+      cp_async_commit();
+    }
+    cur ^= dbuf;
+  }
+  cp_async_wait_group<0>();
+}
+
+static int staged_max_bits(int dtype) { return dtype == TQ_C64 ? 13 : 12; }
+
+template <typename R>
+static int run_staged(void* psi, int n, const tq_tile_pass* passes, int n_passes, const tq_tile_stage* stages,
+                      const tq_tile_op* ops, const double* theta, cudaStream_t s) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  for (int p = 0; p < n_passes; ++p) {
+    const PassArgs P = to_args(passes[p]);
+    if (P.op_end == P.op_begin) continue;
+    const int64_t ntiles = int64_t(1) << (n - P.t);
+    const int dbuf = ntiles > sms ? 1 : 0;
+    const size_t smem = (size_t)(dbuf ? 2 : 1) * padded_len(P.t) * sizeof(cplx<R>) +
+                        (sizeof(int64_t) << (P.t - P.nlow));
+    cudaError_t e = cudaFuncSetAttribute(k_staged_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "tq_sv_run_staged: smem attribute");
+    const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
+    k_staged_forward<R><<<grid, 1 << (P.t - kRB), smem, s>>>((typename C2<R>::T*)psi, n, P, stages, ops, theta, dbuf);
+    TQ_CHECK_LAUNCH("tq_sv_run_staged");
+  }
+  return TQ_OK;
+}
+
+}  // namespace tq
+
+extern "C" int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
+                                const tq_tile_stage* stages, const tq_tile_op* ops, const double* theta,
+                                void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (n_passes < 0) return fail(TQ_ERR_ARG, "tq_sv_run_staged: negative pass count");
+  if (n_passes == 0) return TQ_OK;
+  if (!psi || !passes || !stages || !ops) return fail(TQ_ERR_ARG, "tq_sv_run_staged: NULL pointer");
+  if ((rc = check_passes(n, dtype, passes, n_passes, staged_max_bits(dtype), "tq_sv_run_staged"))) return rc;
+  for (int p = 0; p < n_passes; ++p)
+    if (passes[p].t < 9) return fail(TQ_ERR_ARG, "tq_sv_run_staged: pass %d has t=%d < 9", p, passes[p].t);
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == TQ_C64 ? run_staged<float>(psi, n, passes, n_passes, stages, ops, theta, s)
+                         : run_staged<double>(psi, n, passes, n_passes, stages, ops, theta, s);
 }

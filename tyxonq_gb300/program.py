@@ -168,8 +168,11 @@ def _mat4(g: Gate) -> np.ndarray:
     return {"cx": G.gate_cx_4x4, "cz": G.gate_cz_4x4, "swap": G.gate_swap_4x4}[g.kind]()
 
 
-def fuse_pass(gates: Sequence[Gate]) -> list[Gate]:
-    """Fold single-qubit gates into neighbouring two-qubit gates (forward only)."""
+def fuse_pass(gates: Sequence[Gate], absorb: bool = True) -> list[Gate]:
+    """Merge runs of single-qubit gates; with absorb=True also fold them into
+    neighbouring two-qubit gates (fewer shared-memory sweeps), with
+    absorb=False keep CX/CZ/SWAP as permutations (fewer flops when ops run in
+    registers).  Forward only."""
     out: list[Gate] = []
     pending: dict[int, np.ndarray] = {}
     last: dict[int, int] = {}
@@ -179,6 +182,11 @@ def fuse_pass(gates: Sequence[Gate]) -> list[Gate]:
             q = g.qubits[0]
             M = g.mat if g.kind == "u1" else np.diag(np.diag(g.mat))
             pending[q] = M @ pending[q] if q in pending else M.copy()
+        elif g.kind in ("u2", "cx", "cz", "swap") and not absorb:
+            for q in g.qubits:
+                if q in pending:
+                    out.append(_one_q(q, pending.pop(q)))
+            out.append(g)
         elif g.kind in ("u2", "cx", "cz", "swap"):
             a, b = g.qubits
             pa, pb = pending.pop(a, None), pending.pop(b, None)
@@ -201,7 +209,7 @@ def fuse_pass(gates: Sequence[Gate]) -> list[Gate]:
             for q in g.qubits:
                 last[q] = len(out) - 1
     for q, P in pending.items():
-        j = last.get(q)
+        j = last.get(q) if absorb else None
         if j is not None and out[j].kind in ("u2", "cx", "cz", "swap"):
             tg = out[j]
             M = _mat4(tg)
@@ -447,6 +455,11 @@ class ForwardProgram:
         for kind, obj in self.segments:
             if kind == "gate":
                 execute_plain(psi, [obj])
+            elif kind == "staged":
+                st, ops = obj.device_tables(psi.device)
+                nat.call("tq_sv_run_staged", ctypes.c_void_p(psi.data_ptr()), self.n, dt, obj.passes, obj.n_passes,
+                         ctypes.c_void_p(st.data_ptr()), ctypes.c_void_p(ops.data_ptr()), th,
+                         K.stream_ptr(psi.device))
             else:
                 ops = obj.device_ops(psi.device)
                 nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), self.n, dt, obj.passes, obj.n_passes,
@@ -454,19 +467,151 @@ class ForwardProgram:
         return psi
 
 
+# ---------------------------------------------------------------- register stages
+STAGE_DTYPE = np.dtype({"names": ["bits", "op_begin", "op_end"], "formats": [("<i4", 4), "<i4", "<i4"],
+                        "offsets": [0, 16, 20], "itemsize": 24})
+STAGE_BITS = 4
+STAGED_MIN_T = 9
+
+
+def plan_stages(op_bits: Sequence[tuple], t: int, rb: int = STAGE_BITS) -> list[tuple[list, list]]:
+    """Group ops (given as tuples of local bits, in a valid order) into stages
+    of at most `rb` local bits by greedy DAG scheduling; each stage's bit set
+    is padded to exactly rb bits with the highest unused local bits."""
+    queues: list[deque] = [deque() for _ in range(t)]
+    for i, bs in enumerate(op_bits):
+        for b in set(bs):
+            queues[b].append(i)
+    done = [False] * len(op_bits)
+
+    def is_ready(i):
+        return all(queues[b] and queues[b][0] == i for b in set(op_bits[i]))
+
+    ready = set(i for i in range(len(op_bits)) if is_ready(i))
+    stages = []
+    left = len(op_bits)
+    while left:
+        S: set = set()
+        order: list = []
+        while True:
+            best, bc = None, None
+            for i in ready:
+                new = set(op_bits[i]) - S
+                if len(S) + len(new) > rb:
+                    continue
+                c = len(new)
+                if best is None or c < bc or (c == bc and i < best):
+                    best, bc = i, c
+                    if c == 0:
+                        break
+            if best is None:
+                break
+            S |= set(op_bits[best])
+            order.append(best)
+            done[best] = True
+            left -= 1
+            ready.discard(best)
+            for b in set(op_bits[best]):
+                queues[b].popleft()
+                if queues[b] and not done[queues[b][0]] and is_ready(queues[b][0]):
+                    ready.add(queues[b][0])
+        if not order:  # pragma: no cover - every op has at most rb bits
+            raise RuntimeError("stage planner made no progress")
+        for b in range(t - 1, -1, -1):
+            if len(S) >= rb:
+                break
+            S.add(b)
+        stages.append((sorted(S), order))
+    return stages
+
+
+@dataclass
+class EncodedStaged:
+    passes: ctypes.Array
+    n_passes: int
+    stages_host: np.ndarray
+    ops_host: np.ndarray
+    _dev: tuple | None = None
+
+    def device_tables(self, device):
+        if self._dev is None or self._dev[0].device != torch.device(device):
+            st = torch.frombuffer(bytearray(self.stages_host.tobytes() or bytes(24)), dtype=torch.uint8).to(device)
+            op = torch.frombuffer(bytearray(self.ops_host.tobytes() or bytes(TILE_OP_DTYPE.itemsize)),
+                                  dtype=torch.uint8).to(device)
+            self._dev = (st, op)
+        return self._dev
+
+
+def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], params: dict | None = None
+                  ) -> EncodedStaged:
+    """Encode forward passes as register stages: single-qubit runs merged,
+    two-qubit gates kept as permutations / dense 4x4, parametrised gates as
+    device-side rotations."""
+    fields, stage_rows, passes = [], [], []
+    for pp in plans:
+        qs = pp.qubits
+        loc = {q: j for j, q in enumerate(qs)}
+        t = len(qs)
+        idx = list(pp.gates)
+        gl = [gates[i] for i in idx]
+        items = []  # (gate, pidx, pscale)
+        run = []
+        for gi, g in zip(idx, gl):
+            if params is not None and gi in params:
+                items += [(x, -1, 1.0) for x in fuse_pass(run, absorb=False)]
+                run = []
+                items.append((g, params[gi][0], params[gi][1]))
+            else:
+                run.append(g)
+        items += [(x, -1, 1.0) for x in fuse_pass(run, absorb=False)]
+        op_bits = [tuple(loc[q] for q in g.qubits) for g, _, _ in items]
+        st_begin = len(stage_rows)
+        for bits, order in plan_stages(op_bits, t):
+            reg = {b: k for k, b in enumerate(bits)}
+            qreg = {q: reg[loc[q]] for q in qs if loc[q] in reg}
+            ob = len(fields)
+            for k in order:
+                g, pidx, psc = items[k]
+                fields.append(op_fields(g, qreg, pidx=pidx, pscale=psc, as_rotation=pidx >= 0))
+            stage_rows.append((bits, ob, len(fields)))
+        p = TilePass()
+        p.t = t
+        p.nlow = min(pp.nlow, t)
+        p.op_begin = st_begin
+        p.op_end = len(stage_rows)
+        for j, q in enumerate(qs):
+            p.pos[j] = n - 1 - q
+        passes.append(p)
+    st = np.zeros(len(stage_rows), dtype=STAGE_DTYPE)
+    for i, (bits, b, e) in enumerate(stage_rows):
+        st[i] = (bits, b, e)
+    arr = (TilePass * max(len(passes), 1))(*passes)
+    return EncodedStaged(arr, len(passes), st, pack_ops(fields))
+
+
 def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int | None = None,
-                    nlow: int = DEFAULT_NLOW, fuse: bool = True, params: dict | None = None) -> ForwardProgram:
+                    nlow: int = DEFAULT_NLOW, fuse: bool = True, params: dict | None = None,
+                    staged: bool | None = None) -> ForwardProgram:
     """Plan and encode a forward program.  params: gate index -> (pidx, pscale)
-    for gates whose angle is read from device theta at run time."""
+    for gates whose angle is read from device theta at run time.  staged:
+    register-staged passes (default when the tile has >= 9 bits)."""
     gates = [_canon(g) for g in gates]
     if t is None:
         t = default_tile_bits(n, dtype)
+    t = min(t, n)
+    if staged is None:
+        staged = (fuse and STAGED_MIN_T <= t <= (13 if dtype == torch.complex64 else 12)
+                  and all(len(set(g.qubits)) <= STAGE_BITS for g in gates))
     segs = plan_passes(gates, n, t, nlow)
     out = []
     npass = 0
     for s in segs:
         if s.kind == "gate":
             out.append(("gate", gates[s.gate]))
+        elif staged:
+            enc = encode_staged(n, s.passes, gates, params=params)
+            out.append(("staged", enc))
+            npass += enc.n_passes
         else:
             enc, _ = encode_passes(n, s.passes, gates, fuse=fuse, params=params, nlow=nlow)
             out.append(("tiles", enc))
