@@ -182,12 +182,18 @@ def bench_gate_kernels(args, dev):
         a.record(st)
         evs = []
         for kind, obj in prog.segments:
-            ops_d = obj.device_ops(psi.device)
             for p in range(obj.n_passes):
                 x, y = _events()
                 x.record(st)
-                nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), n2, 0, ctypes.byref(obj.passes[p]), 1,
-                         ctypes.c_void_p(ops_d.data_ptr()), None, K.stream_ptr())
+                if kind == "staged":
+                    st_d, ops_d = obj.device_tables(psi.device)
+                    nat.call("tq_sv_run_staged", ctypes.c_void_p(psi.data_ptr()), n2, 0,
+                             ctypes.byref(obj.passes[p]), 1, ctypes.c_void_p(st_d.data_ptr()),
+                             ctypes.c_void_p(ops_d.data_ptr()), None, K.stream_ptr())
+                else:
+                    ops_d = obj.device_ops(psi.device)
+                    nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), n2, 0, ctypes.byref(obj.passes[p]),
+                             1, ctypes.c_void_p(ops_d.data_ptr()), None, K.stream_ptr())
                 y.record(st)
                 evs.append((x, y))
         b.record(st)

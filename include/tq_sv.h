@@ -305,6 +305,40 @@ TQ_API int tq_batch_run(int dtype, const tq_batch_inst* insts, const int32_t* wo
                         const tq_pauli_term* terms, const double* theta, void* pool, double* energies,
                         double* grads, int32_t* counter, void* stream);
 
+/* ------------------------------------------------------------ batched VQE, L2-resident waves */
+
+/* Large instances of a batch are evaluated in waves whose states fit in L2.
+ * A wave phase is one launch over work items; each item is one tile of one
+ * instance.  Offsets are in amplitudes into the state pool (psi and lam of an
+ * instance live at psi_off and lam_off); theta/grad offsets index the batch's
+ * parameter vector; part_off indexes the FP64 partial-sum buffer. */
+typedef struct {
+  int64_t psi_off;
+  int64_t lam_off;
+  int32_t pass;        /* forward / adjoint: pass-table index (stages in [op_begin, op_end)) */
+  int32_t tile;        /* tile index within the pass (or H psi output tile) */
+  int32_t theta_off;
+  int32_t part_off;    /* adjoint: first partial slot of this item; H psi: energy partial slot */
+  int32_t n;           /* qubits of the instance */
+  int32_t group_begin; /* H psi: Pauli groups of the instance */
+  int32_t group_count;
+  int32_t basis_lo;    /* forward pass 0 of an instance: initial basis index (low 32 bits), else -1 */
+} tq_wave_item;
+
+/* kind 0: staged forward passes (psi), kind 1: H psi (lam = H psi over 2^hbits
+ * output tiles, energy partial per item), kind 2: staged adjoint passes (psi,
+ * lam, gradient partials per item and parameter op). */
+TQ_API int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
+                       const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
+                       const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,
+                       double* partials, int max_pass_ops, void* stream);
+
+/* Fixed-order reductions of wave partials: out[k] (+)= scale[k] * sum of
+ * partials[first[k] + j * stride[k]] for j < count[k]; accumulate != 0 adds. */
+TQ_API int tq_wave_reduce(const double* partials, const int32_t* first, const int32_t* count, const int32_t* stride,
+                          const double* scale, const int32_t* out_index, int n_out, double* out, int accumulate,
+                          void* stream);
+
 /* Re <a|b> into *out_dev (FP64), used by energy = <psi|H psi>. */
 TQ_API size_t tq_sv_inner_workspace_bytes(int n);
 TQ_API int tq_sv_inner_re(const void* a, const void* b, int n, int dtype, double* out_dev, void* ws,

@@ -25,21 +25,28 @@ def _instances(count, seed, n_range, depth_range=(1, 3), terms_range=(10, 60)):
     return batched_vqe(count, seed=seed, n_range=n_range, depth_range=depth_range, terms_range=terms_range)
 
 
+@pytest.mark.parametrize("large", ["waves", "cta"])
 @pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
-def test_batched_matches_oracle_all_classes(dtype):
+def test_batched_matches_oracle_all_classes(dtype, large):
     from tyxonq_gb300.batch import BatchedVQE, Schedule
 
     insts = _instances(40, 5, (3, 13))
-    # small tiles so that 12- and 13-qubit instances take the streamed path too
-    sched = Schedule(res8_max=6, res4_max=8, res2_max=10, res1_max=11, t_fwd=9, t_adj=8)
+    # small tiles so that 11- to 13-qubit instances take the large-instance path too
+    sched = Schedule(res8_max=6, res4_max=8, res2_max=10, res1_max=10, t_fwd=9, t_adj=8, large=large, wave_t=9,
+                     wave_hbits=8, wave_budget=1 << 16)
     if dtype == torch.complex128:
-        sched = Schedule(res8_max=6, res4_max=8, res2_max=9, res1_max=10, t_fwd=8, t_adj=7)
+        sched = Schedule(res8_max=6, res4_max=8, res2_max=9, res1_max=10, t_fwd=8, t_adj=7, large=large, wave_t=9,
+                         wave_hbits=8, wave_budget=1 << 16)
     bv = BatchedVQE(insts, dtype=dtype, schedule=sched)
     theta = np.concatenate([i.theta for i in insts])
     e, g = bv.run(theta)
     e = e.cpu().numpy()
     grads = bv.split_grads(g.cpu().numpy())
-    assert {c.name for c in bv.launch_order} >= {"streamed", "res1", "res8"}
+    assert {c.name for c in bv.launch_order} >= {"res1", "res8"}
+    if large == "waves":
+        assert bv.waves is not None and len(bv.waves.waves) > 1
+    else:
+        assert "streamed" in {c.name for c in bv.launch_order}
     for k, inst in enumerate(insts):
         e_ref, g_ref = _oracle(inst)
         nrm = inst.H.one_norm()

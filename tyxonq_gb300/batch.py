@@ -55,6 +55,11 @@ class Schedule:
     t_fwd: int = 13
     t_adj: int = 12
     max_pass_ops: int = 512
+    large: str = "waves"  # instances above res1_max: "waves" (L2-resident grid-wide phases) or "cta"
+    wave_t: int = 12
+    wave_hbits: int = 12
+    wave_budget: int = 48 << 20
+    wave_max_ops: int = 256
 
     @classmethod
     def default(cls, dtype) -> "Schedule":
@@ -134,11 +139,34 @@ class BatchedVQE:
         S = 8 if dtype == torch.complex64 else 16
         cache: dict = {}
         self._nops = 0
+        wave_entries = []
+        n_groups_total = n_terms_total = 0
+        gate_cache: dict = {}
         for i, inst in enumerate(instances):
             n = int(inst.n)
             cname, G, T = self.sched.class_of(n)
-            gates, params = structure_gates(inst.structure()) if (n, cname == "streamed", tuple(
-                inst.structure())) not in cache else (None, None)
+            skey = tuple(inst.structure())
+            if skey not in gate_cache:
+                gate_cache[skey] = structure_gates(inst.structure())
+            gates, params = gate_cache[skey]
+            H: PauliSum = inst.H
+            g, t = H.pack()
+            if cname == "streamed" and self.sched.large == "waves":
+                wave_entries.append({"idx": i, "n": n, "gates": gates, "params": params, "key": (n, skey),
+                                     "theta_offset": theta_off, "theta_off": theta_off, "grad_offset": theta_off,
+                                     "basis": int(getattr(inst, "basis", 0)), "group_begin": n_groups_total,
+                                     "group_count": len(g)})
+                insts[i]["n"] = n
+                insts[i]["streamed"] = 2
+                theta_off += int(inst.n_params)
+                self.n_params.append(int(inst.n_params))
+                g2 = g.copy()
+                g2["first_term"] += n_terms_total
+                groups_all.append(g2)
+                terms_all.append(t)
+                n_groups_total += len(g)
+                n_terms_total += len(t)
+                continue
             cl = self.classes.setdefault(cname, _Class(cname, G, T))
             streamed = cname == "streamed"
             rec = insts[i]
@@ -160,14 +188,14 @@ class BatchedVQE:
             if streamed:
                 rec["scratch_offset"] = pool_off
                 pool_off += 2 << n
-            H: PauliSum = inst.H
-            g, t = H.pack()
-            rec["group_begin"] = sum(len(x) for x in groups_all)
+            rec["group_begin"] = n_groups_total
             rec["group_count"] = len(g)
             g2 = g.copy()
-            g2["first_term"] += sum(len(x) for x in terms_all)
+            g2["first_term"] += n_terms_total
             groups_all.append(g2)
             terms_all.append(t)
+            n_groups_total += len(g)
+            n_terms_total += len(t)
             cost = (1 << n) * (rec["fwd_count"] + rec["adj_count"] + 4 * H.n_terms)
             cl.work.append((cost, i))
             cl.max_n = max(cl.max_n, n)
@@ -192,6 +220,14 @@ class BatchedVQE:
         self.grads = torch.zeros_like(self.theta)
         self.energies = torch.zeros(self.count, dtype=torch.float64, device=dev)
         self.counters = torch.zeros(max(len(self.classes), 1), dtype=torch.int32, device=dev)
+        self.waves = None
+        if wave_entries:
+            from .waves import WavePlan
+
+            sc = self.sched
+            self.waves = WavePlan(wave_entries, dtype, dev, t=sc.wave_t, hbits=sc.wave_hbits, budget=sc.wave_budget,
+                                  max_ops=sc.wave_max_ops)
+            self.n_structures += self.waves.n_structures
         lib = nat.load()
         order = ["streamed", "res1", "res2", "res4", "res8"]
         self.launch_order = [self.classes[c] for c in order if c in self.classes]
@@ -263,8 +299,17 @@ class BatchedVQE:
         """Enqueue one evaluation (memsets + persistent launches) on the current stream."""
         self.grads.zero_()
         self.counters.zero_()
-        s = K.stream_ptr(self.device)
+        main = torch.cuda.current_stream(self.device)
         P = ctypes.c_void_p
+        # persistent size-class kernels run on a side stream, concurrently with the waves
+        if self.waves is not None and self.launch_order:
+            if getattr(self, "_side", None) is None:
+                self._side = torch.cuda.Stream(self.device)
+            side = self._side
+            side.wait_stream(main)
+        else:
+            side = main
+        s = ctypes.c_void_p(side.cuda_stream)
         for k, cl in enumerate(self.launch_order):
             nat.call("tq_batch_run", self.dt, P(self.insts_dev.data_ptr()), P(cl.work_dev.data_ptr()),
                      int(cl.work_dev.numel()), int(cl.name == "streamed"), cl.groups, cl.threads, self.grid,
@@ -273,6 +318,11 @@ class BatchedVQE:
                      P(self.theta.data_ptr()), P(self.pool.data_ptr()) if self.pool is not None else None,
                      P(self.energies.data_ptr()), P(self.grads.data_ptr()),
                      P(self.counters.data_ptr() + 4 * k), s)
+        if self.waves is not None:
+            self.waves.launch(self.groups_dev, self.terms_dev, self.theta, self.energies, self.grads,
+                              ctypes.c_void_p(main.cuda_stream))
+        if side is not main:
+            main.wait_stream(side)
 
     def capture(self) -> None:
         """Capture launch() into a CUDA graph (replayed by run())."""

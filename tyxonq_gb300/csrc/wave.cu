@@ -1,0 +1,391 @@
+// L2-resident waves of large batched instances.
+//
+// A wave is a set of instances whose psi and lam fit in L2 together.  Each
+// phase of a wave (a forward pass, H psi, an adjoint pass) is one launch over
+// work items = (instance, tile), so every SM works on the same few states and
+// their re-reads (tile passes, the partner reads of H psi) are served by L2.
+//   kind 0  forward: register-staged tile pass on psi (the instance's first
+//           pass also writes the initial basis state, so no separate init);
+//   kind 1  H psi: one output tile of 2^hbits amplitudes per item, partner
+//           amplitudes psi[i ^ flip] read directly, accumulators in registers;
+//           the item's share of <psi|H psi> goes to partials[part_off];
+//   kind 2  adjoint: register-staged un-apply of psi and lam with the
+//           gradient terms Im <lam|G|psi> reduced per warp in a fixed order,
+//           partials[part_off + k] per op k of the pass.
+// Gradient and energy partials are summed by tq_wave_reduce in a fixed order.
+#include "stage.cuh"
+
+namespace tq {
+
+struct WPass {
+  int t, nlow, op_begin, op_end;
+  int pos[TQ_TILE_MAX_BITS];
+};
+
+__device__ __forceinline__ WPass wload_pass(const tq_tile_pass* p) {
+  WPass s;
+  s.t = p->t;
+  s.nlow = p->nlow;
+  s.op_begin = p->op_begin;
+  s.op_end = p->op_end;
+#pragma unroll
+  for (int i = 0; i < TQ_TILE_MAX_BITS; ++i) s.pos[i] = p->pos[i];
+  return s;
+}
+
+__device__ __forceinline__ void w_hoff(int64_t* hoff, const WPass& P) {
+  const int nh = 1 << (P.t - P.nlow);
+  for (int h = threadIdx.x; h < nh; h += blockDim.x) {
+    int64_t off = 0;
+    for (int k = 0; k < P.t - P.nlow; ++k)
+      if ((h >> k) & 1) off |= int64_t(1) << P.pos[P.nlow + k];
+    hoff[h] = off;
+  }
+}
+
+__device__ __forceinline__ int64_t w_base(int64_t g, const WPass& P) {
+  int64_t x = g << P.nlow;
+  for (int k = P.nlow; k < P.t; ++k) x = insert_zero(x, P.pos[k]);
+  return x;
+}
+
+__device__ __forceinline__ void w_commit_wait() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+template <typename R>
+__device__ __forceinline__ void w_load(cplx<R>* s, const typename C2<R>::T* g, int64_t base, const int64_t* hoff,
+                                       const WPass& P) {
+  constexpr int A = 16 / sizeof(cplx<R>);
+  const int nc = (1 << P.t) / A;
+  const int lm = (1 << P.nlow) - 1;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    const int j = c * A;
+    cp_async16(&s[pphys(j)], &g[base + hoff[j >> P.nlow] + (j & lm)]);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void w_store(const cplx<R>* s, typename C2<R>::T* g, int64_t base, const int64_t* hoff,
+                                        const WPass& P) {
+  constexpr int A = 16 / sizeof(cplx<R>);
+  const int nc = (1 << P.t) / A;
+  const int lm = (1 << P.nlow) - 1;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    const int j = c * A;
+    *reinterpret_cast<float4*>(&g[base + hoff[j >> P.nlow] + (j & lm)]) =
+        *reinterpret_cast<const float4*>(&s[pphys(j)]);
+  }
+}
+
+// ------------------------------------------------------------------ forward
+template <typename R>
+__global__ void __launch_bounds__(512) k_wave_forward(const tq_wave_item* __restrict__ items, int n_items,
+                                                      const tq_tile_pass* __restrict__ passes,
+                                                      const tq_tile_stage* __restrict__ stages,
+                                                      const tq_tile_op* __restrict__ ops,
+                                                      const double* __restrict__ theta, void* pool) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  typedef typename C2<R>::T T2;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const tq_wave_item I = items[it];
+    const WPass P = wload_pass(&passes[I.pass]);
+    cplx<R>* s = reinterpret_cast<cplx<R>*>(smem);
+    int64_t* hoff = reinterpret_cast<int64_t*>(smem + padded_len(P.t) * sizeof(cplx<R>));
+    T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
+    __syncthreads();  // previous item's readers of s / hoff are done
+    w_hoff(hoff, P);
+    __syncthreads();
+    const int64_t base = w_base(I.tile, P);
+    if (I.basis_lo >= 0) {
+      // first pass of the instance: the tile of |basis> (psi was never written)
+      const int N = 1 << P.t;
+      const int lm = (1 << P.nlow) - 1;
+      for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+        s[pphys(j)] = cplx<R>(gi == (int64_t)I.basis_lo ? R(1) : R(0), R(0));
+      }
+    } else {
+      w_load<R>(s, psi, base, hoff, P);
+      w_commit_wait();
+    }
+    __syncthreads();
+    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta + I.theta_off, false);
+    w_store<R>(s, psi, base, hoff, P);
+  }
+}
+
+// ------------------------------------------------------------------ H psi
+template <typename R, int PER>
+__global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restrict__ items, int n_items, int hbits,
+                                                   const tq_pauli_group* __restrict__ groups,
+                                                   const tq_pauli_term* __restrict__ terms, void* pool,
+                                                   double* partials) {
+  typedef typename C2<R>::T T2;
+  __shared__ double red[32];
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const tq_wave_item I = items[it];
+    const int hb = I.n < hbits ? I.n : hbits;
+    const int HN = 1 << hb;
+    const T2* psi = reinterpret_cast<const T2*>(pool) + I.psi_off;
+    T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
+    const int64_t t0 = (int64_t)I.tile << hb;
+    cplx<R> acc[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) acc[k] = cplx<R>(0, 0);
+    for (int g = I.group_begin; g < I.group_begin + I.group_count; ++g) {
+      const uint64_t m = __ldg(&groups[g].flip);
+      const int first = __ldg(&groups[g].first_term), cnt = __ldg(&groups[g].n_terms);
+#pragma unroll
+      for (int k = 0; k < PER; ++k) {
+        const int j = threadIdx.x + k * blockDim.x;
+        if (j < HN) {
+          const int64_t src = (t0 + j) ^ (int64_t)m;
+          const T2 v = psi[src];
+          const cplx<R> f = group_f<R>(terms, first, cnt, (uint64_t)src);
+          acc[k] = cfma(f, cplx<R>(v.x, v.y), acc[k]);
+        }
+      }
+    }
+    R eloc = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int j = threadIdx.x + k * blockDim.x;
+      if (j < HN) {
+        const T2 a = psi[t0 + j];
+        eloc += a.x * acc[k].x + a.y * acc[k].y;
+        T2 o;
+        o.x = acc[k].x;
+        o.y = acc[k].y;
+        lam[t0 + j] = o;
+      }
+    }
+    double v = (double)eloc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+      partials[I.part_off] = s;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ adjoint
+// Im <lam|G|psi> over the 16 register amplitudes: G|i> = [i & cm == cm] ph
+// (-1)^{popc(i & zm)} |i ^ XM>  (register-bit masks).
+template <typename R, int XM>
+__device__ __forceinline__ R r_grad(const cplx<R>* x, const cplx<R>* y, uint32_t zm, uint32_t cm, cplx<R> ph) {
+  R acc = 0;
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i & cm) != cm) continue;
+    const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
+    const cplx<R> v = cmul(ph, x[i]);
+    const cplx<R> l = y[i ^ XM];
+    acc += sg * (l.x * v.y - l.y * v.x);
+  }
+  return acc;
+}
+
+template <typename R>
+__device__ __forceinline__ R r_grad_dispatch(const cplx<R>* x, const cplx<R>* y, const tq_tile_op& o) {
+  const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
+  const cplx<R> ph(re[o.gny & 3], im[o.gny & 3]);
+  const uint32_t zm = o.gzm, cm = o.gcm;
+  switch (o.gxm & 15) {
+    case 0: return r_grad<R, 0>(x, y, zm, cm, ph);
+    case 1: return r_grad<R, 1>(x, y, zm, cm, ph);
+    case 2: return r_grad<R, 2>(x, y, zm, cm, ph);
+    case 3: return r_grad<R, 3>(x, y, zm, cm, ph);
+    case 4: return r_grad<R, 4>(x, y, zm, cm, ph);
+    case 5: return r_grad<R, 5>(x, y, zm, cm, ph);
+    case 6: return r_grad<R, 6>(x, y, zm, cm, ph);
+    case 7: return r_grad<R, 7>(x, y, zm, cm, ph);
+    case 8: return r_grad<R, 8>(x, y, zm, cm, ph);
+    case 9: return r_grad<R, 9>(x, y, zm, cm, ph);
+    case 10: return r_grad<R, 10>(x, y, zm, cm, ph);
+    case 11: return r_grad<R, 11>(x, y, zm, cm, ph);
+    case 12: return r_grad<R, 12>(x, y, zm, cm, ph);
+    case 13: return r_grad<R, 13>(x, y, zm, cm, ph);
+    case 14: return r_grad<R, 14>(x, y, zm, cm, ph);
+    default: return r_grad<R, 15>(x, y, zm, cm, ph);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(512) k_wave_adjoint(const tq_wave_item* __restrict__ items, int n_items,
+                                                      const tq_tile_pass* __restrict__ passes,
+                                                      const tq_tile_stage* __restrict__ stages,
+                                                      const tq_tile_op* __restrict__ ops,
+                                                      const double* __restrict__ theta, void* pool,
+                                                      double* partials, int max_ops) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  typedef typename C2<R>::T T2;
+  const int nwarps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const tq_wave_item I = items[it];
+    const WPass P = wload_pass(&passes[I.pass]);
+    const int PT = padded_len(P.t);
+    cplx<R>* sp = reinterpret_cast<cplx<R>*>(smem);
+    cplx<R>* sl = sp + PT;
+    int64_t* hoff = reinterpret_cast<int64_t*>(smem + 2 * PT * sizeof(cplx<R>));
+    double* wpart = reinterpret_cast<double*>(smem + 2 * PT * sizeof(cplx<R>) + (sizeof(int64_t) << (P.t - P.nlow)));
+    T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
+    T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
+    const double* th = theta + I.theta_off;
+    const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
+    const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
+    __syncthreads();
+    w_hoff(hoff, P);
+    for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = 0.0;
+    __syncthreads();
+    const int64_t base = w_base(I.tile, P);
+    w_load<R>(sp, psi, base, hoff, P);
+    w_load<R>(sl, lam, base, hoff, P);
+    w_commit_wait();
+    __syncthreads();
+    for (int si = P.op_begin; si < P.op_end; ++si) {
+      const tq_tile_stage st = stages[si];
+      const StageMap mp = stage_map(st, threadIdx.x);
+      cplx<R> x[kNR], y[kNR];
+#pragma unroll
+      for (int i = 0; i < kNR; ++i) {
+        const int j = pphys(mp.base | mp.off[i]);
+        x[i] = sp[j];
+        y[i] = sl[j];
+      }
+      for (int k = st.op_begin; k < st.op_end; ++k) {
+        const tq_tile_op& o = ops[k];
+        if (o.slot >= 0) {
+          R part = r_grad_dispatch<R>(x, y, o);
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
+          if (lane == 0) wpart[(k - op0) * nwarps + warp] = (double)part;
+        }
+        r_apply<R>(x, o, th, true);
+        r_apply<R>(y, o, th, true);
+      }
+#pragma unroll
+      for (int i = 0; i < kNR; ++i) {
+        const int j = pphys(mp.base | mp.off[i]);
+        sp[j] = x[i];
+        sl[j] = y[i];
+      }
+      __syncthreads();
+    }
+    w_store<R>(sp, psi, base, hoff, P);
+    w_store<R>(sl, lam, base, hoff, P);
+    for (int k = threadIdx.x; k < nops; k += blockDim.x) {
+      double s = 0;
+      for (int w = 0; w < nwarps; ++w) s += wpart[k * nwarps + w];
+      partials[I.part_off + k] = s;
+    }
+  }
+  (void)max_ops;
+}
+
+__global__ void k_wave_reduce(const double* __restrict__ partials, const int32_t* __restrict__ first,
+                              const int32_t* __restrict__ count, const int32_t* __restrict__ stride,
+                              const double* __restrict__ scale, const int32_t* __restrict__ out_index, int n_out,
+                              double* out, int accumulate) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_out; r += gridDim.x * blockDim.x) {
+    double s = 0;
+    const int f = first[r], c = count[r], st = stride[r];
+    for (int j = 0; j < c; ++j) s += partials[(int64_t)f + (int64_t)j * st];
+    s *= scale[r];
+    if (accumulate)
+      out[out_index[r]] += s;
+    else
+      out[out_index[r]] = s;
+  }
+}
+
+template <typename R>
+static size_t fwd_smem(int t) {
+  return padded_len(t) * sizeof(cplx<R>) + (sizeof(int64_t) << (t - 1));
+}
+template <typename R>
+static size_t adj_smem(int t, int max_ops) {
+  return 2 * padded_len(t) * sizeof(cplx<R>) + (sizeof(int64_t) << (t - 1)) +
+         sizeof(double) * (size_t)max_ops * ((1 << (t - kRB)) / 32);
+}
+
+template <typename R>
+static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, int hbits,
+                       const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
+                       const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,
+                       double* partials, int max_ops, cudaStream_t s) {
+  if (kind == 1) {
+    if (hbits < 8 || hbits > 12) return fail(TQ_ERR_ARG, "tq_wave_run: hbits %d outside [8, 12]", hbits);
+    const int grid = n_items;
+    switch (hbits) {
+      case 8: k_wave_hpsi<R, 1><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
+      case 9: k_wave_hpsi<R, 2><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
+      case 10: k_wave_hpsi<R, 4><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
+      case 11: k_wave_hpsi<R, 8><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
+      default: k_wave_hpsi<R, 16><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
+    }
+    TQ_CHECK_LAUNCH("tq_wave_run (H psi)");
+    return TQ_OK;
+  }
+  if (t < 9 || t > (sizeof(R) == 4 ? 13 : 12)) return fail(TQ_ERR_ARG, "tq_wave_run: t=%d", t);
+  const int threads = 1 << (t - kRB);
+  const int grid = n_items;
+  if (kind == 0) {
+    const size_t smem = fwd_smem<R>(t);
+    cudaError_t e = cudaFuncSetAttribute(k_wave_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");
+    k_wave_forward<R><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool);
+  } else {
+    const size_t smem = adj_smem<R>(t, max_ops);
+    if (smem > 227 * 1024) return fail(TQ_ERR_ARG, "tq_wave_run: adjoint needs %zu B shared memory", smem);
+    cudaError_t e = cudaFuncSetAttribute(k_wave_adjoint<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");
+    k_wave_adjoint<R><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool, partials, max_ops);
+  }
+  TQ_CHECK_LAUNCH("tq_wave_run");
+  return TQ_OK;
+}
+
+}  // namespace tq
+
+using namespace tq;
+
+extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
+                           const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
+                           const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,
+                           double* partials, int max_pass_ops, void* stream) {
+  if (dtype != TQ_C64 && dtype != TQ_C128) return fail(TQ_ERR_ARG, "tq_wave_run: bad dtype %d", dtype);
+  if (kind < 0 || kind > 2) return fail(TQ_ERR_ARG, "tq_wave_run: bad kind %d", kind);
+  if (n_items < 0) return fail(TQ_ERR_ARG, "tq_wave_run: negative item count");
+  if (n_items == 0) return TQ_OK;
+  if (!items || !pool) return fail(TQ_ERR_ARG, "tq_wave_run: NULL pointer");
+  if (kind != 1 && (!passes || !stages || !ops || !theta)) return fail(TQ_ERR_ARG, "tq_wave_run: NULL table");
+  if (kind == 1 && (!groups || !terms || !partials)) return fail(TQ_ERR_ARG, "tq_wave_run: NULL Pauli table");
+  if (kind == 2 && (!partials || max_pass_ops < 1)) return fail(TQ_ERR_ARG, "tq_wave_run: adjoint partials");
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == TQ_C64 ? wave_launch<float>(kind, items, n_items, t, hbits, passes, stages, ops, groups, terms,
+                                              theta, pool, partials, max_pass_ops, s)
+                         : wave_launch<double>(kind, items, n_items, t, hbits, passes, stages, ops, groups, terms,
+                                               theta, pool, partials, max_pass_ops, s);
+}
+
+extern "C" int tq_wave_reduce(const double* partials, const int32_t* first, const int32_t* count,
+                              const int32_t* stride, const double* scale, const int32_t* out_index, int n_out,
+                              double* out, int accumulate, void* stream) {
+  if (n_out < 0) return fail(TQ_ERR_ARG, "tq_wave_reduce: negative count");
+  if (n_out == 0) return TQ_OK;
+  if (!partials || !first || !count || !stride || !scale || !out_index || !out)
+    return fail(TQ_ERR_ARG, "tq_wave_reduce: NULL pointer");
+  const int threads = 256;
+  const int grid = (n_out + threads - 1) / threads;
+  k_wave_reduce<<<grid, threads, 0, (cudaStream_t)stream>>>(partials, first, count, stride, scale, out_index, n_out,
+                                                            out, accumulate);
+  TQ_CHECK_LAUNCH("tq_wave_reduce");
+  return TQ_OK;
+}

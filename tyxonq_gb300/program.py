@@ -542,11 +542,13 @@ class EncodedStaged:
         return self._dev
 
 
-def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], params: dict | None = None
-                  ) -> EncodedStaged:
-    """Encode forward passes as register stages: single-qubit runs merged,
-    two-qubit gates kept as permutations / dense 4x4, parametrised gates as
-    device-side rotations."""
+def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], params: dict | None = None,
+                  slots: dict | None = None) -> EncodedStaged:
+    """Encode passes as register stages.  Forward (slots None): single-qubit
+    runs merged, two-qubit gates kept as permutations / dense 4x4,
+    parametrised gates as device-side rotations.  Adjoint (slots given, gates
+    already in reverse order): one op per gate, gradient slot = slots[gate],
+    generator masks and coefficient in register space."""
     fields, stage_rows, passes = [], [], []
     for pp in plans:
         qs = pp.qubits
@@ -554,25 +556,35 @@ def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], para
         t = len(qs)
         idx = list(pp.gates)
         gl = [gates[i] for i in idx]
-        items = []  # (gate, pidx, pscale)
-        run = []
-        for gi, g in zip(idx, gl):
-            if params is not None and gi in params:
-                items += [(x, -1, 1.0) for x in fuse_pass(run, absorb=False)]
-                run = []
-                items.append((g, params[gi][0], params[gi][1]))
-            else:
-                run.append(g)
-        items += [(x, -1, 1.0) for x in fuse_pass(run, absorb=False)]
-        op_bits = [tuple(loc[q] for q in g.qubits) for g, _, _ in items]
+        items = []  # (gate, pidx, pscale, gate index or None)
+        if slots is not None:
+            for gi, g in zip(idx, gl):
+                pidx, psc = params[gi] if (params is not None and gi in params) else (-1, 1.0)
+                items.append((g, pidx, psc, gi))
+        else:
+            run = []
+            for gi, g in zip(idx, gl):
+                if params is not None and gi in params:
+                    items += [(x, -1, 1.0, None) for x in fuse_pass(run, absorb=False)]
+                    run = []
+                    items.append((g, params[gi][0], params[gi][1], gi))
+                else:
+                    run.append(g)
+            items += [(x, -1, 1.0, None) for x in fuse_pass(run, absorb=False)]
+        op_bits = [tuple(loc[q] for q in g.qubits) for g, _, _, _ in items]
         st_begin = len(stage_rows)
         for bits, order in plan_stages(op_bits, t):
             reg = {b: k for k, b in enumerate(bits)}
             qreg = {q: reg[loc[q]] for q in qs if loc[q] in reg}
             ob = len(fields)
             for k in order:
-                g, pidx, psc = items[k]
-                fields.append(op_fields(g, qreg, pidx=pidx, pscale=psc, as_rotation=pidx >= 0))
+                g, pidx, psc, gi = items[k]
+                if slots is not None and gi in slots:
+                    gen = _generator(g, qreg)
+                    fields.append(op_fields(g, qreg, slots[gi], gen, pidx=pidx, pscale=psc, gcoef=gen[4] * psc,
+                                            as_rotation=True))
+                else:
+                    fields.append(op_fields(g, qreg, pidx=pidx, pscale=psc, as_rotation=pidx >= 0 or slots is not None))
             stage_rows.append((bits, ob, len(fields)))
         p = TilePass()
         p.t = t

@@ -1,0 +1,229 @@
+"""L2-resident waves for the large instances of a batch (host side of csrc/wave.cu).
+
+Instances too large for one CTA's shared memory are grouped into waves whose
+psi and lam fit together in L2 (``budget`` bytes).  A wave runs as a short
+sequence of grid-wide launches over (instance, tile) work items:
+
+  forward pass k of every wave instance  (kind 0, register stages; pass 0
+                                          also writes |basis>)
+  lam = H psi, energy partials          (kind 1)
+  adjoint pass k of every wave instance  (kind 2, gradient partials)
+  fixed-order reductions of the partials into energies and gradients.
+
+All tables (passes, stages, ops, items, reduction rows) are built once; the
+state pool and partial buffer are reused by every wave, so device memory is
+one wave's footprint.  Circuit structures are encoded once and shared by all
+instances with the same structure; angles are read from theta on the device.
+"""
+from __future__ import annotations
+
+import ctypes
+from collections import defaultdict
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .program import STAGE_DTYPE, TILE_OP_DTYPE, PassPlan, encode_staged, plan_passes
+
+WAVE_ITEM_DTYPE = np.dtype({
+    "names": ["psi_off", "lam_off", "pass", "tile", "theta_off", "part_off", "n", "group_begin", "group_count",
+              "basis_lo"],
+    "formats": ["<i8", "<i8", "<i4", "<i4", "<i4", "<i4", "<i4", "<i4", "<i4", "<i4"],
+    "offsets": [0, 8, 16, 20, 24, 28, 32, 36, 40, 44],
+    "itemsize": 48,
+})
+PASS_DTYPE = np.dtype({"names": ["t", "nlow", "op_begin", "op_end", "pos"],
+                       "formats": ["<i4", "<i4", "<i4", "<i4", ("<i4", 16)], "itemsize": 80})
+
+
+def _dev(arr: np.ndarray, device) -> torch.Tensor:
+    return torch.frombuffer(bytearray(arr.tobytes() or b"\0" * 16), dtype=torch.uint8).to(device)
+
+
+class WavePlan:
+    def __init__(self, entries, dtype, device, t: int = 12, hbits: int = 12, budget: int = 48 << 20,
+                 max_ops: int = 256):
+        """entries: list of dicts with keys idx (instance index), n, gates,
+        params, key (structure key), theta_off, grad_offset, basis,
+        group_begin, group_count."""
+        self.dtype = dtype
+        self.dt = 0 if dtype == torch.complex64 else 1
+        self.t = t
+        self.hbits = hbits
+        self.max_ops = max_ops
+        S = 8 if dtype == torch.complex64 else 16
+        self.passes, self.stages, self.ops = [], [], []
+        self._np = self._ns = self._no = 0
+        cache = {}
+        for e in entries:
+            if e["key"] not in cache:
+                cache[e["key"]] = self._encode(e["n"], e["gates"], e["params"])
+            e["enc"] = cache[e["key"]]
+        self.n_structures = len(cache)
+        # waves: largest first, packed up to the L2 budget
+        order = sorted(entries, key=lambda e: -e["n"])
+        waves, cur, used = [], [], 0
+        for e in order:
+            need = 2 * S << e["n"]
+            if cur and used + need > budget:
+                waves.append(cur)
+                cur, used = [], 0
+            cur.append(e)
+            used += need
+        if cur:
+            waves.append(cur)
+        self.waves = waves
+        items, launches, rows = [], [], []
+        pool_need = part_need = 0
+        for wv in waves:
+            off = 0
+            for e in wv:
+                e["psi_off"], e["lam_off"] = off, off + (1 << e["n"])
+                off += 2 << e["n"]
+            pool_need = max(pool_need, off)
+            part = 0
+            # energy partial slots first, then gradient partials
+            for e in wv:
+                e["epart"] = part
+                part += 1 << max(0, e["n"] - min(hbits, e["n"]))
+            # forward phases
+            nf = max(len(e["enc"]["fwd"]) for e in wv)
+            for k in range(nf):
+                b = len(items)
+                for e in wv:
+                    if k >= len(e["enc"]["fwd"]):
+                        continue
+                    pid = e["enc"]["fwd"][k]
+                    for tile in range(1 << (e["n"] - self.t)):
+                        items.append((e["psi_off"], e["lam_off"], pid, tile, e["theta_off"], 0, e["n"], 0, 0,
+                                      e["basis"] if k == 0 else -1))
+                launches.append(("run", 0, b, len(items) - b))
+            b = len(items)
+            for e in wv:
+                hb = min(hbits, e["n"])
+                for tile in range(1 << (e["n"] - hb)):
+                    items.append((e["psi_off"], e["lam_off"], 0, tile, e["theta_off"], e["epart"] + tile, e["n"],
+                                  e["group_begin"], e["group_count"], -1))
+            launches.append(("run", 1, b, len(items) - b))
+            na = max(len(e["enc"]["adj"]) for e in wv)
+            grad_rows = []
+            for k in range(na):
+                b = len(items)
+                for e in wv:
+                    if k >= len(e["enc"]["adj"]):
+                        continue
+                    pid, nops, pslots = e["enc"]["adj"][k]
+                    ntile = 1 << (e["n"] - self.t)
+                    base = part
+                    for tile in range(ntile):
+                        items.append((e["psi_off"], e["lam_off"], pid, tile, e["theta_off"], base + tile * nops,
+                                      e["n"], 0, 0, -1))
+                    part += ntile * nops
+                    for kk, slot, coef in pslots:
+                        grad_rows.append((base + kk, ntile, nops, coef, e["grad_offset"] + slot))
+                launches.append(("run", 2, b, len(items) - b))
+            part_need = max(part_need, part)
+            erow = [(e["epart"], 1 << (e["n"] - min(hbits, e["n"])), 1, 1.0, e["idx"]) for e in wv]
+            rb = len(rows)
+            rows += erow
+            launches.append(("reduce_e", rb, len(erow)))
+            # split gradient rows so that no launch writes one output twice
+            seen = defaultdict(int)
+            layers = defaultdict(list)
+            for r in grad_rows:
+                layers[seen[r[4]]].append(r)
+                seen[r[4]] += 1
+            for lay in sorted(layers):
+                rb = len(rows)
+                rows += layers[lay]
+                launches.append(("reduce_g", rb, len(layers[lay])))
+        self.launches = launches
+        self.n_items = len(items)
+        it = np.zeros(len(items), dtype=WAVE_ITEM_DTYPE)
+        if items:
+            cols = list(zip(*items))
+            for name, col in zip(WAVE_ITEM_DTYPE.names, cols):
+                it[name] = col
+        self.items_dev = _dev(it, device)
+        r = np.array(rows, dtype=object) if rows else np.zeros((0, 5))
+        self.r_first = torch.tensor([x[0] for x in rows] or [0], dtype=torch.int32, device=device)
+        self.r_count = torch.tensor([x[1] for x in rows] or [0], dtype=torch.int32, device=device)
+        self.r_stride = torch.tensor([x[2] for x in rows] or [0], dtype=torch.int32, device=device)
+        self.r_scale = torch.tensor([x[3] for x in rows] or [0.0], dtype=torch.float64, device=device)
+        self.r_out = torch.tensor([x[4] for x in rows] or [0], dtype=torch.int32, device=device)
+        del r
+        pa = np.zeros(len(self.passes), dtype=PASS_DTYPE)
+        for k, (tt, nl, b0, e0, pos) in enumerate(self.passes):
+            pa[k] = (tt, nl, b0, e0, pos)
+        self.passes_dev = _dev(pa, device)
+        self.stages_dev = _dev(np.concatenate(self.stages) if self.stages else np.zeros(1, STAGE_DTYPE), device)
+        self.ops_dev = _dev(np.concatenate(self.ops) if self.ops else np.zeros(1, TILE_OP_DTYPE), device)
+        self.pool = torch.empty(max(pool_need, 2), dtype=dtype, device=device)
+        self.partials = torch.zeros(max(part_need, 1), dtype=torch.float64, device=device)
+        self.pool_bytes = self.pool.numel() * S
+
+    # ------------------------------------------------------------ encoding
+    def _add_staged(self, enc) -> list[int]:
+        """Append an EncodedStaged's passes/stages/ops to the global tables; return pass ids."""
+        st = enc.stages_host.copy()
+        st["op_begin"] += self._no
+        st["op_end"] += self._no
+        ids = []
+        for p in range(enc.n_passes):
+            ps = enc.passes[p]
+            self.passes.append((ps.t, ps.nlow, ps.op_begin + self._ns, ps.op_end + self._ns, list(ps.pos)))
+            ids.append(len(self.passes) - 1)
+        self.stages.append(st)
+        self.ops.append(enc.ops_host)
+        self._ns += len(st)
+        self._no += len(enc.ops_host)
+        return ids
+
+    def _encode(self, n, gates, params) -> dict:
+        t = self.t
+        segs = plan_passes(gates, n, t)
+        fwd = []
+        for s in segs:
+            if s.kind != "tiles":
+                raise NotImplementedError("wave path needs tileable gates")
+            fwd += self._add_staged(encode_staged(n, s.passes, gates, params=params))
+        if not fwd:  # no gates: one empty pass writes |basis>
+            qs = list(range(n - 1, n - 1 - t, -1))
+            fwd += self._add_staged(encode_staged(n, [PassPlan(qs, [], 5)], gates))
+        rg = list(reversed(gates))
+        G = len(gates)
+        rparams = {G - 1 - gi: v for gi, v in params.items()}
+        slots = {ri: rparams[ri][0] for ri in rparams}
+        adj = []
+        for s in plan_passes(rg, n, t, max_ops=self.max_ops):
+            for pp in s.passes:
+                enc = encode_staged(n, [pp], rg, params=rparams, slots=slots)
+                pid = self._add_staged(enc)[0]
+                ops = enc.ops_host
+                pslots = [(k, int(ops[k]["slot"]), float(ops[k]["gcoef"])) for k in range(len(ops))
+                          if ops[k]["slot"] >= 0]
+                adj.append((pid, len(ops), pslots))
+        return {"fwd": fwd, "adj": adj}
+
+    # ------------------------------------------------------------ execution
+    def launch(self, groups_dev, terms_dev, theta, energies, grads, stream) -> None:
+        P = ctypes.c_void_p
+        isz = WAVE_ITEM_DTYPE.itemsize
+        for L in self.launches:
+            if L[0] == "run":
+                _, kind, b, c = L
+                if c == 0:
+                    continue
+                nat.call("tq_wave_run", kind, self.dt, P(self.items_dev.data_ptr() + isz * b), c, self.t,
+                         self.hbits, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
+                         P(self.ops_dev.data_ptr()), P(groups_dev.data_ptr()), P(terms_dev.data_ptr()),
+                         P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()), self.max_ops,
+                         stream)
+            else:
+                kind, b, c = L
+                out = energies if kind == "reduce_e" else grads
+                nat.call("tq_wave_reduce", P(self.partials.data_ptr()), P(self.r_first.data_ptr() + 4 * b),
+                         P(self.r_count.data_ptr() + 4 * b), P(self.r_stride.data_ptr() + 4 * b),
+                         P(self.r_scale.data_ptr() + 8 * b), P(self.r_out.data_ptr() + 4 * b), c,
+                         P(out.data_ptr()), 0 if kind == "reduce_e" else 1, stream)
