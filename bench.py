@@ -318,6 +318,20 @@ def main():
     gk = bench_gate_kernels(args, dev)
     peak, peak_kind = _peaks()
 
+    # ---------------- serving: Poisson arrivals, 70% energy / 30% energy+gradient, 10-26 qubits
+    from tyxonq_gb300.serving import VqeServer, make_trace, replay
+
+    serving = []
+    for rate in (20.0, 80.0):
+        trace = make_trace(48, rate=rate, seed=int(rate), n_range=(10, 26), depth_range=(2, 10),
+                           terms_range=(20, 1000), grad_fraction=0.3, iterations=2)
+        srv = VqeServer(max_inflight=8)
+        st = replay(srv, trace)
+        st["rate_rps"] = rate
+        serving.append(st)
+        del srv
+        torch.cuda.empty_cache()
+
     # ---------------- CPU baseline: oracle port, bounded sample, one core
     cpu = None
     if rank == 0:
@@ -347,6 +361,9 @@ def main():
         "plain_gpu": {"value": plain_evals, "unit": "evals/s", "sample": f"{len(sample)} of {len(insts)} (every 8th)",
                       "speedup_batched": value / world / plain_evals, "max_energy_diff_rel": worst},
         "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "latency": {"p50_ms": serving[-1]["p50_ms"], "p99_ms": serving[-1]["p99_ms"], "sweep": serving,
+                    "workload": "Poisson arrivals, 24 sessions x 2 optimizer steps, HEA n~U{10..26} depth~U{2..10}, "
+                                "20-1000 Pauli terms, 30% energy+gradient, complex64"},
         "gate_kernels_28q": gk,
         "roofline": {"kernel": "k_tile_forward (28-qubit complex64 tile pass, 2*N*8 B per launch)", "bound": "hbm",
                      "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,

@@ -32,7 +32,7 @@ def test_batched_matches_oracle_all_classes(dtype, large):
 
     insts = _instances(40, 5, (3, 13))
     # small tiles so that 11- to 13-qubit instances take the large-instance path too
-    sched = Schedule(res8_max=6, res4_max=8, res2_max=10, res1_max=10, t_fwd=9, t_adj=8, large=large, wave_t=9,
+    sched = Schedule(res8_max=6, res4_max=8, res2_max=9, res1_max=10, t_fwd=9, t_adj=8, large=large, wave_t=9,
                      wave_hbits=8, wave_budget=1 << 16)
     if dtype == torch.complex128:
         sched = Schedule(res8_max=6, res4_max=8, res2_max=9, res1_max=10, t_fwd=8, t_adj=7, large=large, wave_t=9,

@@ -106,21 +106,112 @@ def _with_angles(pgates: Sequence[ParamGate], theta: np.ndarray) -> list[ParamGa
     return out
 
 
-def reverse_sweep(prog: AdjointProgram, psi: torch.Tensor, lam: torch.Tensor) -> torch.Tensor:
-    """Run the adjoint passes in place on (psi, lam); returns slot values (device, FP64)."""
+def reverse_sweep(prog: AdjointProgram, psi: torch.Tensor, lam: torch.Tensor,
+                  theta: torch.Tensor | None = None) -> torch.Tensor:
+    """Run the adjoint passes in place on (psi, lam); returns slot values (device, FP64).
+    theta feeds ops compiled with device-side angles."""
     dt = K.dtype_tag(psi)
     out = torch.zeros(max(prog.n_slots, 1), dtype=torch.float64, device=psi.device)
     lib = nat.load()
+    th = ctypes.c_void_p(theta.data_ptr()) if theta is not None else None
     for kind, enc in prog.reverse:
         ops = enc.device_ops(psi.device)
         # slots of this segment only are written; other segments' slots must be kept
         seg_out = torch.empty_like(out)
         p, cap = K._ws(lib.tq_sv_adjoint_tiles_workspace_bytes(prog.n, prog.n_slots), psi.device)
         nat.call("tq_sv_adjoint_tiles", ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), prog.n, dt,
-                 enc.passes, enc.n_passes, ctypes.c_void_p(ops.data_ptr()), None, prog.n_slots,
+                 enc.passes, enc.n_passes, ctypes.c_void_p(ops.data_ptr()), th, prog.n_slots,
                  ctypes.c_void_p(seg_out.data_ptr()), p, cap, K.stream_ptr(psi.device))
         out += seg_out
     return out[: prog.n_slots]
+
+
+def build_parametric(pgates: Sequence[ParamGate], n: int, n_params: int, dtype, t_fwd=None,
+                     t_adj=None) -> AdjointProgram:
+    """Compile once for any angles: parametrised gates read theta[param] * scale
+    on the device, so a new parameter vector needs no re-planning."""
+    from .autotune import tile_bits_for
+
+    gates = [_canon(p.gate) for p in pgates]
+    for g in gates:
+        if not tileable(g):
+            raise NotImplementedError(f"adjoint gradient through a '{g.kind}' gate is not supported")
+    params = {i: (p.param, p.scale) for i, p in enumerate(pgates) if p.param is not None}
+    fwd = compile_forward(gates, n, dtype, t=t_fwd, params=params)
+    t_adj = t_adj or tile_bits_for(n, dtype, adjoint=True)
+    rgates = list(reversed(gates))
+    G = len(gates)
+    rparams = {G - 1 - gi: v for gi, v in params.items()}
+    slots, slot_param, slot_scale = {}, [], []
+    for ri in sorted(rparams):
+        slots[ri] = len(slot_param)
+        slot_param.append(rparams[ri][0])
+        slot_scale.append(rparams[ri][1])
+    rev = []
+    coef = np.zeros(len(slot_param))
+    for s in plan_passes(rgates, n, t_adj, DEFAULT_NLOW):
+        enc, coefs = encode_passes(n, s.passes, rgates, fuse=False, slots=slots, params=rparams)
+        for sl, c in coefs:
+            coef[sl] = c
+        rev.append(("tiles", enc))
+    return AdjointProgram(n, dtype, fwd, rev, len(slot_param), np.asarray(slot_param, dtype=np.int64),
+                          coef * np.asarray(slot_scale, dtype=np.float64), n_params)
+
+
+class ParametricEstimator:
+    """Energy / adjoint gradient of one circuit structure, compiled once; each
+    call takes a parameter vector (host array or float64 device tensor)."""
+
+    def __init__(self, n: int, pgates: Sequence[ParamGate], n_params: int, hamiltonian, dtype=torch.complex64,
+                 device="cuda", init_basis: int = 0):
+        self.n = int(n)
+        self.n_params = int(n_params)
+        self.H = as_pauli_sum(hamiltonian, self.n)
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self.init_basis = int(init_basis)
+        self.prog = build_parametric(pgates, self.n, self.n_params, dtype)
+        self.theta = torch.zeros(max(self.n_params, 1), dtype=torch.float64, device=self.device)
+        self.psi = torch.empty(1 << self.n, dtype=dtype, device=self.device)
+        self.lam = None
+
+    def footprint_bytes(self, grad: bool) -> int:
+        S = 8 if self.dtype == torch.complex64 else 16
+        return (2 if grad else 1) * (S << self.n)
+
+    def _forward(self, theta) -> torch.Tensor:
+        if isinstance(theta, torch.Tensor) and theta.is_cuda:
+            self.theta.copy_(theta.reshape(-1), non_blocking=True)
+        else:
+            self.theta.copy_(torch.as_tensor(np.asarray(theta, dtype=np.float64)).reshape(-1), non_blocking=True)
+        nat.call("tq_sv_init_basis", ctypes.c_void_p(self.psi.data_ptr()), self.n, K.dtype_tag(self.psi),
+                 self.init_basis, K.stream_ptr(self.device))
+        return self.prog.forward.run(self.psi, self.theta)
+
+    def energy_async(self, theta) -> torch.Tensor:
+        """Enqueue an energy evaluation on the current stream; returns a device scalar."""
+        psi = self._forward(theta)
+        return K.pauli_expectation(psi, self.H)
+
+    def energy_and_grad_async(self, theta) -> tuple[torch.Tensor, torch.Tensor]:
+        """Enqueue energy + adjoint gradient; returns (device energy, device slot values)."""
+        psi = self._forward(theta)
+        if self.lam is None:
+            self.lam = torch.empty_like(self.psi)
+        K.apply_pauli_sum(psi, self.H, out=self.lam)
+        e = K.inner_re(psi, self.lam)
+        sv = reverse_sweep(self.prog, psi, self.lam, self.theta)
+        return e, sv
+
+    def grad_from_slots(self, slot_vals: np.ndarray) -> np.ndarray:
+        return slots_to_grad(self.prog, slot_vals)
+
+    def energy(self, theta) -> float:
+        return float(self.energy_async(theta).item())
+
+    def energy_and_grad(self, theta) -> tuple[float, np.ndarray]:
+        e, sv = self.energy_and_grad_async(theta)
+        return float(e.item()), self.grad_from_slots(sv.cpu().numpy())
 
 
 def slots_to_grad(prog: AdjointProgram, slot_vals: np.ndarray) -> np.ndarray:

@@ -1,0 +1,252 @@
+"""Continuous-batching VQE serving on one GPU.
+
+Requests (energy, or energy + adjoint gradient) of 10-26+ qubits arrive
+over time.  The server
+
+  * admits a request when a stream slot is free and its session's device
+    footprint (psi, plus lam for gradients: 2^n * 8 B each in complex64) fits
+    the HBM budget -- evicting idle sessions least-recently-used first;
+  * keeps each session's statevectors and compiled circuit resident across
+    its optimizer iterations (angles are read on the device, so a new
+    parameter vector costs one small copy, no re-planning);
+  * enqueues every admitted request on its own CUDA stream, so the work of
+    requests that arrive while others run overlaps on the device, and
+    completes requests by polling their events;
+  * records arrival / admission / completion times for p50 / p99 latency.
+
+Requests of one session run in arrival order (they share its buffers).  A
+request whose footprint alone exceeds the budget fails with an error instead
+of waiting forever.  The reference has no serving layer; this is new.
+"""
+from __future__ import annotations
+
+import time
+from collections import OrderedDict, deque
+from dataclasses import dataclass, field
+from typing import Callable, Sequence
+
+import numpy as np
+import torch
+
+
+@dataclass
+class VqeRequest:
+    session: str
+    n: int
+    structure: list  # [(gate name, qubits, parameter index or None)]
+    n_params: int
+    H: object  # PauliSum
+    theta: np.ndarray
+    grad: bool = False
+    arrival: float = 0.0
+    # results
+    energy: float | None = None
+    gradient: np.ndarray | None = None
+    error: str | None = None
+    admitted: float | None = None
+    done: float | None = None
+
+    @property
+    def latency(self) -> float | None:
+        return None if self.done is None else self.done - self.arrival
+
+
+def default_estimator_factory(req: VqeRequest, dtype, device):
+    from .adjoint import ParamGate, ParametricEstimator
+    from .batch import structure_gates
+
+    gates, params = structure_gates(req.structure)
+    pg = [ParamGate(g, params[i][0] if i in params else None) for i, g in enumerate(gates)]
+    return ParametricEstimator(req.n, pg, req.n_params, req.H, dtype=dtype, device=device)
+
+
+@dataclass
+class _Session:
+    est: object
+    bytes: int
+    busy: bool = False
+    pending: deque = field(default_factory=deque)
+
+
+class VqeServer:
+    def __init__(self, device="cuda", dtype=torch.complex64, hbm_budget: int | None = None, max_inflight: int = 8,
+                 estimator_factory: Callable | None = None, streams: Sequence | None = None):
+        self.device = torch.device(device)
+        self.dtype = dtype
+        if hbm_budget is None:
+            free, _total = torch.cuda.mem_get_info(self.device)
+            hbm_budget = int(free * 0.8)
+        self.budget = int(hbm_budget)
+        self.factory = estimator_factory or default_estimator_factory
+        self.streams = list(streams) if streams is not None else [torch.cuda.Stream(self.device)
+                                                                   for _ in range(max_inflight)]
+        self.free_streams = deque(range(len(self.streams)))
+        self.sessions: OrderedDict[str, _Session] = OrderedDict()
+        self.queue: deque = deque()
+        self.inflight: list = []
+        self.used = 0
+        self.completed: list[VqeRequest] = []
+
+    # ------------------------------------------------------------ memory
+    def _footprint(self, req: VqeRequest) -> int:
+        S = 8 if self.dtype == torch.complex64 else 16
+        return (2 if req.grad else 1) * (S << req.n)
+
+    def _evict_for(self, need: int) -> bool:
+        for key in list(self.sessions):
+            if self.used + need <= self.budget:
+                break
+            s = self.sessions[key]
+            if not s.busy and not s.pending:
+                self.used -= s.bytes
+                del self.sessions[key]
+        return self.used + need <= self.budget
+
+    # ------------------------------------------------------------ API
+    def submit(self, req: VqeRequest) -> None:
+        if not req.arrival:
+            req.arrival = time.perf_counter()
+        self.queue.append(req)
+
+    def step(self) -> int:
+        """Admit what fits, poll running work; returns the number completed now."""
+        self._admit()
+        return self._poll()
+
+    def drain(self, timeout: float = 600.0) -> None:
+        t0 = time.perf_counter()
+        while self.queue or self.inflight:
+            if not self.step():
+                time.sleep(0.0002)
+            if time.perf_counter() - t0 > timeout:
+                raise TimeoutError("serving loop did not drain")
+
+    # ------------------------------------------------------------ internals
+    def _admit(self) -> None:
+        keep = deque()
+        while self.queue:
+            req = self.queue.popleft()
+            sess = self.sessions.get(req.session)
+            if sess is not None and sess.busy:
+                keep.append(req)  # same-session requests run in order
+                continue
+            if not self.free_streams:
+                keep.append(req)
+                continue
+            need = self._footprint(req)
+            if sess is not None:
+                need = max(0, need - sess.bytes)
+            if self._footprint(req) > self.budget:
+                req.error = f"request needs {self._footprint(req)} B, above the {self.budget} B budget"
+                req.done = time.perf_counter()
+                self.completed.append(req)
+                continue
+            if self.used + need > self.budget and not self._evict_for(need):
+                keep.append(req)
+                continue
+            self._start(req, need)
+        self.queue = keep
+
+    def _start(self, req: VqeRequest, need: int) -> None:
+        sess = self.sessions.get(req.session)
+        si = self.free_streams.popleft()
+        if sess is None:
+            sess = _Session(None, 0)
+            self.sessions[req.session] = sess
+        sess.bytes += need
+        self.used += need
+        self.sessions.move_to_end(req.session)
+        sess.busy = True
+        req.admitted = time.perf_counter()
+        ev, e_h, sv_h = self._launch(sess, req, si)
+        self.inflight.append((req, si, ev, e_h, sv_h, sess))
+
+    def _launch(self, sess: _Session, req: VqeRequest, si: int):
+        """Enqueue the request's device work on stream si; returns (event, host
+        energy buffer, host slot-value buffer or None)."""
+        stream = self.streams[si]
+        stream.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(stream):
+            if sess.est is None:
+                sess.est = self.factory(req, self.dtype, self.device)
+            if req.grad:
+                e, sv = sess.est.energy_and_grad_async(req.theta)
+            else:
+                e, sv = sess.est.energy_async(req.theta), None
+            e_h = torch.empty(1, dtype=torch.float64, pin_memory=True)
+            e_h.copy_(e.reshape(-1)[:1], non_blocking=True)
+            sv_h = None
+            if sv is not None:
+                sv_h = torch.empty(sv.numel(), dtype=torch.float64, pin_memory=True)
+                sv_h.copy_(sv, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return ev, e_h, sv_h
+
+    def _ready(self, ev) -> bool:
+        return ev.query()
+
+    def _poll(self) -> int:
+        done = 0
+        still = []
+        for item in self.inflight:
+            req, si, ev, e_h, sv_h, sess = item
+            if not self._ready(ev):
+                still.append(item)
+                continue
+            req.energy = float(e_h[0])
+            if sv_h is not None:
+                req.gradient = sess.est.grad_from_slots(sv_h.numpy())
+            req.done = time.perf_counter()
+            sess.busy = False
+            self.free_streams.append(si)
+            self.completed.append(req)
+            done += 1
+        self.inflight = still
+        return done
+
+
+def make_trace(count: int, rate: float, seed: int = 5, n_range=(10, 26), depth_range=(2, 10),
+               terms_range=(20, 1000), grad_fraction: float = 0.3, iterations: int = 1) -> list[VqeRequest]:
+    """Poisson arrivals (mean rate `rate` per second) of HEA requests; each
+    session issues `iterations` requests (optimizer steps) in sequence."""
+    from .hamiltonian import random_pauli_sum
+    from .workloads import hea_rz_ops_params
+
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    sessions = max(1, count // iterations)
+    for s in range(sessions):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        d = int(rng.integers(depth_range[0], depth_range[1] + 1))
+        K = int(rng.integers(terms_range[0], terms_range[1] + 1))
+        H = random_pauli_sum(n, K, rng)
+        struct = hea_rz_ops_params(n, d)
+        npar = 2 * n * d
+        grad = bool(rng.random() < grad_fraction)
+        for it in range(iterations):
+            t += float(rng.exponential(1.0 / rate))
+            out.append(VqeRequest(f"s{s}", n, struct, npar, H, rng.uniform(0, 2 * np.pi, npar), grad, arrival=t))
+    return out
+
+
+def replay(server: VqeServer, trace: Sequence[VqeRequest], timeout: float = 600.0) -> dict:
+    """Feed requests at their (relative) arrival times; returns latency stats."""
+    t0 = time.perf_counter()
+    pending = deque(sorted(trace, key=lambda r: r.arrival))
+    for r in pending:
+        r.arrival = t0 + r.arrival
+    while pending or server.queue or server.inflight:
+        now = time.perf_counter()
+        while pending and pending[0].arrival <= now:
+            server.submit(pending.popleft())
+        if not server.step():
+            time.sleep(0.0001)
+        if now - t0 > timeout:
+            raise TimeoutError("trace replay did not finish")
+    wall = time.perf_counter() - t0
+    lat = np.array([r.latency for r in trace if r.error is None])
+    return {"requests": len(trace), "errors": sum(r.error is not None for r in trace), "wall_s": wall,
+            "throughput_rps": len(trace) / wall, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3)}
