@@ -219,6 +219,38 @@ def bench_gate_kernels(args, dev):
             "plain_gbs_equiv": len(gates) * 2 * N * S / (plain_ms * 1e-3) / 1e9}
 
 
+def run_case(args):
+    """One part of the benchmark alone (used for profiler captures)."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    torch.cuda.set_device(0)
+    if args.case == "gates":
+        print(json.dumps({"case": "gates", **bench_gate_kernels(args, 0)}))
+        return
+    from tyxonq_gb300.batch import BatchedVQE
+    from tyxonq_gb300.workloads import batched_vqe
+
+    insts = batched_vqe(args.count, seed=3)
+    bv = BatchedVQE(insts, dtype=torch.complex64)
+    bv.set_theta(np.concatenate([i.theta for i in insts]))
+    for _ in range(args.warmup):
+        bv.run()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        a, b = _events()
+        a.record()
+        bv.run()
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    print(json.dumps({"case": "batched", "count": len(insts), "ms_per_step": sum(ms) / len(ms)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -226,10 +258,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--case", default="full", choices=["full", "gates", "batched"],
+                    help="gates / batched: run only that part (profiling captures); full: the benchmark line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.case != "full":
+        return run_case(args)
 
     import numpy as np
     import torch

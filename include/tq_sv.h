@@ -216,6 +216,10 @@ typedef struct {
                                (kind 7: Pauli rotation; kind 2: phase diag(1, e^{ia})) */
   double pscale;
   double gcoef;             /* dE/d(angle) = gcoef * Im <lam|G|psi> (batched kernel) */
+  uint32_t zo;              /* kind 7 in register stages: Z factors on local bits outside the stage */
+  int32_t reserved;
+  uint64_t zg;              /* kind 7: Z factors on non-local (global) bits; with zo they contribute
+                               one sign per tile / thread, so only X/Y qubits need to be local */
   float mf[32];             /* matrix, complex64 kernels: row-major (re, im) */
   double md[32];            /* matrix, complex128 kernels */
 } tq_tile_op;

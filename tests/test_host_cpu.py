@@ -55,7 +55,8 @@ class _CTileOp(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32), ("slot", ctypes.c_int32),
                 ("xm", ctypes.c_uint32), ("zm", ctypes.c_uint32), ("cm", ctypes.c_uint32), ("gxm", ctypes.c_uint32),
                 ("gzm", ctypes.c_uint32), ("gcm", ctypes.c_uint32), ("gny", ctypes.c_int32), ("pidx", ctypes.c_int32),
-                ("pscale", ctypes.c_double), ("gcoef", ctypes.c_double), ("mf", ctypes.c_float * 32),
+                ("pscale", ctypes.c_double), ("gcoef", ctypes.c_double), ("zo", ctypes.c_uint32),
+                ("reserved", ctypes.c_int32), ("zg", ctypes.c_uint64), ("mf", ctypes.c_float * 32),
                 ("md", ctypes.c_double * 32)]
 
 
@@ -135,7 +136,7 @@ def _emulate_tiles(psi, n, enc):
             idx = np.array([base + sum(((j >> k) & 1) << pos[k] for k in range(t)) for j in range(1 << t)])
             s = psi[idx]
             for o in ops[pa.op_begin:pa.op_end]:
-                s = _apply_local(s, o, t)
+                s = _apply_local(s, o, t, _zs(o, base))
             psi[idx] = s
     return psi
 
@@ -161,13 +162,18 @@ def _emulate_staged(psi, n, enc):
                     ridx = np.array([b0 + sum(((i >> k) & 1) << bits[k] for k in range(4)) for i in range(16)])
                     v = s[ridx]
                     for o in enc.ops_host[st["op_begin"]:st["op_end"]]:
-                        v = _apply_local(v, o, 4)
+                        v = _apply_local(v, o, 4, _zs(o, base, b0))
                     s[ridx] = v
             psi[idx] = s
     return psi
 
 
-def _apply_local(s, o, t):
+def _zs(o, gbase, tbase=0):
+    par = (bin(int(gbase) & int(o["zg"])).count("1") + bin(int(tbase) & int(o["zo"])).count("1")) & 1
+    return -1.0 if par else 1.0
+
+
+def _apply_local(s, o, t, zs=1.0):
     s = s.copy()
     if True:
         if True:
@@ -201,7 +207,7 @@ def _apply_local(s, o, t):
                         s[base4 | (1 << a) | (1 << b)] *= -1
                 elif o["kind"] == 7:
                     xm, zm, cm = int(o["xm"]), int(o["zm"]), int(o["cm"])
-                    c, w = m[0], m[1]
+                    c, w = m[0], m[1] * zs
                     sgn = np.array([-1 if bin(int(x) & zm).count("1") % 2 else 1 for x in j])
                     on = (j & cm) == cm
                     new = c * s + w * sgn[j ^ xm] * s[j ^ xm]
@@ -281,6 +287,45 @@ def test_staged_adjoint_encoding_emulated_matches_oracle_gradient():
                         sp[ridx], sl[ridx] = x, y
                 psi[idx], lam[idx] = sp, sl
     np.testing.assert_allclose(grad, g_ref, atol=1e-10)
+
+
+@pytest.mark.parametrize("staged", [False, True])
+def test_wide_pauli_rotations_with_nonlocal_z_emulated(staged):
+    """UCC rotations carry long Z strings: only their X/Y qubits are made
+    local, the other Z factors enter as per-tile / per-thread signs."""
+    from tyxonq_gb300 import chem
+    from tyxonq_gb300.ir import pauli_rotation
+
+    n_orb = 5
+    n = 2 * n_orb
+    pg, npar, ex = chem.uccsd_param_gates(n_orb, 2)
+    rng = np.random.default_rng(3)
+    th = rng.uniform(-0.7, 0.7, npar)
+    gates = [pauli_rotation(p.gate.pauli, p.scale * th[p.param]) for p in pg][:120]
+    psi0 = sv.init_state(n, chem.hf_basis(n, 1))
+    ref = psi0.copy()
+    for g in gates:
+        M = np.array([[1.0 + 0j]])
+        for q, s in g.pauli:
+            M = np.kron(M, sv.PAULI[s])
+        a = g.rot[1]
+        ref = sv.apply_kq(ref, np.cos(a / 2) * np.eye(M.shape[0]) - 1j * np.sin(a / 2) * M, [q for q, _ in g.pauli], n)
+    t = 9 if staged else 6
+    segs = P.plan_passes(gates, n, t, nlow=2)
+    assert all(s.kind == "tiles" for s in segs)
+    psi = psi0.copy()
+    wide = 0
+    for s in segs:
+        if staged:
+            enc = P.encode_staged(n, s.passes, gates)
+            wide += int((enc.ops_host["zg"] != 0).sum() + (enc.ops_host["zo"] != 0).sum())
+            psi = _emulate_staged(psi, n, enc)
+        else:
+            enc, _ = P.encode_passes(n, s.passes, gates, fuse=False, nlow=2)
+            wide += int((enc.ops_host["zg"] != 0).sum())
+            psi = _emulate_tiles(psi, n, enc)
+    assert wide > 0
+    np.testing.assert_allclose(psi, ref, atol=1e-12)
 
 
 def test_staged_encoding_emulated_matches_oracle():

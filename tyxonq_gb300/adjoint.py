@@ -150,6 +150,8 @@ def build_parametric(pgates: Sequence[ParamGate], n: int, n_params: int, dtype, 
     rev = []
     coef = np.zeros(len(slot_param))
     for s in plan_passes(rgates, n, t_adj, DEFAULT_NLOW):
+        if s.kind != "tiles":
+            raise NotImplementedError("every gate of an adjoint program must fit a tile")
         enc, coefs = encode_passes(n, s.passes, rgates, fuse=False, slots=slots, params=rparams)
         for sl, c in coefs:
             coef[sl] = c

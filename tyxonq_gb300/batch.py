@@ -277,6 +277,8 @@ class BatchedVQE:
             segs = plan_passes(gl, n, t, max_ops=self.sched.max_pass_ops)
             begin = len(passes_all)
             for s in segs:
+                if s.kind != "tiles":
+                    raise NotImplementedError("batched instances need tileable gates")
                 enc, _ = encode_passes(n, s.passes, gl, fuse=(which == "fwd"), slots=sl, params=pr)
                 base = self._add_ops(ops_all, enc.ops_host)
                 for p in range(enc.n_passes):

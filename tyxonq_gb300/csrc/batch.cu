@@ -220,7 +220,7 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
       s_tile_load<R>(s, psiG, base, hoff, P);
       __syncthreads();
       for (int k = P.op_begin; k < P.op_end; ++k) {
-        tile_apply<R>(s, P.t, A.ops[k], tid, nt, false, th);
+        tile_apply<R>(s, P.t, A.ops[k], tid, nt, false, th, (uint64_t)base);
         __syncthreads();
       }
       s_tile_store<R>(s, psiG, base, hoff, P);
@@ -305,7 +305,8 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
       for (int k = 0; k < nops; ++k) {
         const tq_tile_op& o = A.ops[P.op_begin + k];
         if (o.slot >= 0) {
-          const R part = tile_grad_partial<R>(sp, sl, P.t, o.gxm, o.gzm, o.gcm, gen_phase<R>(o.gny), tid, nt);
+          const R part = zsign<R>(o, (uint64_t)base, 0) *
+                         tile_grad_partial<R>(sp, sl, P.t, o.gxm, o.gzm, o.gcm, gen_phase<R>(o.gny), tid, nt);
           double v = (double)part;
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
@@ -318,8 +319,8 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
           }
           __syncthreads();
         }
-        tile_apply<R>(sp, P.t, o, tid, nt, true, th);
-        tile_apply<R>(sl, P.t, o, tid, nt, true, th);
+        tile_apply<R>(sp, P.t, o, tid, nt, true, th, (uint64_t)base);
+        tile_apply<R>(sl, P.t, o, tid, nt, true, th, (uint64_t)base);
         __syncthreads();
       }
       s_tile_store<R>(sp, psiG, base, hoff, P);

@@ -111,7 +111,7 @@ __global__ void k_tile_forward(typename C2<R>::T* psi, int n, const PassArgs P, 
     tile_load<R>(s, psi, base, hoff, P);
     __syncthreads();
     for (int k = P.op_begin; k < P.op_end; ++k) {
-      tile_apply<R>(s, P.t, ops[k], threadIdx.x, blockDim.x, false, theta);
+      tile_apply<R>(s, P.t, ops[k], threadIdx.x, blockDim.x, false, theta, (uint64_t)base);
       __syncthreads();
     }
     tile_store<R>(s, psi, base, hoff, P);
@@ -147,7 +147,8 @@ __global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, i
       if (o.slot >= 0) {
         const R phr[4] = {R(1), R(0), R(-1), R(0)}, phi[4] = {R(0), R(1), R(0), R(-1)};
         const cplx<R> ph(phr[o.gny & 3], phi[o.gny & 3]);
-        const R part = tile_grad_partial<R>(sp, sl, P.t, o.gxm, o.gzm, o.gcm, ph, threadIdx.x, blockDim.x);
+        const R part = zsign<R>(o, (uint64_t)base, 0) *
+                       tile_grad_partial<R>(sp, sl, P.t, o.gxm, o.gzm, o.gcm, ph, threadIdx.x, blockDim.x);
         double v = (double)part;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
@@ -160,8 +161,8 @@ __global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, i
         }
         __syncthreads();
       }
-      tile_apply<R>(sp, P.t, o, threadIdx.x, blockDim.x, true, theta);
-      tile_apply<R>(sl, P.t, o, threadIdx.x, blockDim.x, true, theta);
+      tile_apply<R>(sp, P.t, o, threadIdx.x, blockDim.x, true, theta, (uint64_t)base);
+      tile_apply<R>(sl, P.t, o, threadIdx.x, blockDim.x, true, theta, (uint64_t)base);
       __syncthreads();
     }
     tile_store<R>(sp, psi, base, hoff, P);
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(512, 1)
       cp_async_wait_group<0>();
     }
     __syncthreads();
-    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta, false);
+    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta, false, (uint64_t)tile_base(g, P));
     staged_store<R>(s, psi, tile_base(g, P), hoff, P);
     __syncthreads();
     if (!dbuf && gn < ntiles) {

@@ -152,7 +152,8 @@ __device__ __forceinline__ void r_u2_dispatch(cplx<R>* x, const tq_tile_op& o, c
 
 // Apply one op (bit indices in register space 0..3) to the 16 registers.
 template <typename R>
-__device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const double* theta, bool adj) {
+__device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const double* theta, bool adj,
+                                        R zs = R(1)) {
   switch (o.kind) {
     case TOP_U1: {
       cplx<R> u0 = op_m<R>(o, 0), u1 = op_m<R>(o, 1), u2 = op_m<R>(o, 2), u3 = op_m<R>(o, 3);
@@ -211,7 +212,9 @@ __device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const d
     case TOP_PROT: {
       cplx<R> c, w;
       prot_coeffs<R>(o, theta, c, w);
-      if (adj) w = cplx<R>(-w.x, -w.y);
+      // zs: sign of the Z factors outside the stage (zsign); adjoint flips the sin term
+      const R ws = adj ? -zs : zs;
+      w = cplx<R>(ws * w.x, ws * w.y);
       const uint32_t zm = o.zm, cm = o.cm;
       switch (o.xm & 15) {
         case 0: r_prot<R, 0>(x, zm, cm, c, w); break;
@@ -264,7 +267,8 @@ __device__ __forceinline__ StageMap stage_map(const tq_tile_stage& st, int tid) 
 // Run stages[s0..s1) on the padded tile s (2^(t-4) threads).
 template <typename R>
 __device__ __forceinline__ void run_stages(cplx<R>* s, const tq_tile_stage* __restrict__ stages, int s0, int s1,
-                                           const tq_tile_op* __restrict__ ops, const double* theta, bool adj) {
+                                           const tq_tile_op* __restrict__ ops, const double* theta, bool adj,
+                                           uint64_t gbase) {
   const int tid = threadIdx.x;
   for (int si = s0; si < s1; ++si) {
     const tq_tile_stage st = stages[si];
@@ -272,7 +276,10 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, const tq_tile_stage* __re
     cplx<R> x[kNR];
 #pragma unroll
     for (int i = 0; i < kNR; ++i) x[i] = s[pphys(m.base | m.off[i])];
-    for (int k = st.op_begin; k < st.op_end; ++k) r_apply<R>(x, ops[k], theta, adj);
+    for (int k = st.op_begin; k < st.op_end; ++k) {
+      const tq_tile_op& o = ops[k];
+      r_apply<R>(x, o, theta, adj, zsign<R>(o, gbase, m.base));
+    }
 #pragma unroll
     for (int i = 0; i < kNR; ++i) s[pphys(m.base | m.off[i])] = x[i];
     __syncthreads();

@@ -56,12 +56,23 @@ __device__ __forceinline__ void prot_coeffs(const tq_tile_op& o, const double* t
   m1 = cplx<R>(re[ny], im[ny]);
 }
 
+// Sign of a Pauli rotation's Z factors that lie outside the amplitudes being
+// updated together: zg over the tile's non-local bits (fixed by the tile base
+// index gbase) and zo over local bits outside a register stage (fixed by the
+// thread's local base index tbase).
+template <typename R>
+__device__ __forceinline__ R zsign(const tq_tile_op& o, uint64_t gbase, int tbase) {
+  const int par = (__popcll(gbase & o.zg) + __popc((unsigned)tbase & o.zo)) & 1;
+  return par ? R(-1) : R(1);
+}
+
 // Apply one op to tile s[0..2^t) with `nt` cooperating threads (index tid).
 // `adj` = apply the inverse (U^dagger).  No barrier inside: the caller syncs.
-// theta: device angles for ops with pidx >= 0 (may be NULL otherwise).
+// theta: device angles for ops with pidx >= 0 (may be NULL otherwise);
+// gbase: global index of the tile's first amplitude (non-local Z signs).
 template <typename R>
 __device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& o, int tid, int nt, bool adj,
-                                           const double* theta = nullptr) {
+                                           const double* theta = nullptr, uint64_t gbase = 0) {
   const int kind = o.kind;
   const int a = o.a, b = o.b;
   if (kind == TOP_U1) {
@@ -144,7 +155,9 @@ __device__ __forceinline__ void tile_apply(cplx<R>* s, int t, const tq_tile_op& 
     // psi_i <- c psi_i + w * (-1)^{popc(j & zm)} psi_j  with j = i ^ xm, on (i & cm) == cm
     cplx<R> c, w;
     prot_coeffs<R>(o, theta, c, w);
-    if (adj) w = cplx<R>(-w.x, -w.y);  // exp(+i t/2 P): the sin term flips sign
+    // exp(+i t/2 P): the sin term flips sign; non-local Z factors give one sign per tile
+    const R zs = zsign<R>(o, gbase, 0) * (adj ? R(-1) : R(1));
+    w = cplx<R>(zs * w.x, zs * w.y);
     const uint32_t xm = o.xm, zm = o.zm, cm = o.cm;
     if (xm == 0) {
       const int N = 1 << t;

@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(512) k_wave_forward(const tq_wave_item* __rest
       w_commit_wait();
     }
     __syncthreads();
-    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta + I.theta_off, false);
+    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta + I.theta_off, false, (uint64_t)base);
     w_store<R>(s, psi, base, hoff, P);
   }
 }
@@ -261,14 +261,15 @@ __global__ void __launch_bounds__(512) k_wave_adjoint(const tq_wave_item* __rest
       }
       for (int k = st.op_begin; k < st.op_end; ++k) {
         const tq_tile_op& o = ops[k];
+        const R zs = zsign<R>(o, (uint64_t)base, mp.base);
         if (o.slot >= 0) {
-          R part = r_grad_dispatch<R>(x, y, o);
+          R part = zs * r_grad_dispatch<R>(x, y, o);
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
           if (lane == 0) wpart[(k - op0) * nwarps + warp] = (double)part;
         }
-        r_apply<R>(x, o, th, true);
-        r_apply<R>(y, o, th, true);
+        r_apply<R>(x, o, th, true, zs);
+        r_apply<R>(y, o, th, true, zs);
       }
 #pragma unroll
       for (int i = 0; i < kNR; ++i) {

@@ -26,12 +26,20 @@ from .ir import Gate
 
 TILE_OP_DTYPE = np.dtype({
     "names": ["kind", "a", "b", "slot", "xm", "zm", "cm", "gxm", "gzm", "gcm", "gny", "pidx", "pscale", "gcoef",
-              "mf", "md"],
+              "zo", "reserved", "zg", "mf", "md"],
     "formats": ["<i4", "<i4", "<i4", "<i4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<i4", "<i4", "<f8", "<f8",
-                ("<f4", 32), ("<f8", 32)],
-    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44, 48, 56, 64, 192],
-    "itemsize": 448,
+                "<u4", "<i4", "<u8", ("<f4", 32), ("<f8", 32)],
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44, 48, 56, 64, 68, 72, 80, 208],
+    "itemsize": 464,
 })
+
+
+def active_qubits(g: Gate) -> tuple:
+    """Qubits that must be local for g to run inside a tile: a Pauli rotation
+    needs only its X/Y qubits (its Z factors elsewhere become a sign)."""
+    if g.kind == "prot":
+        return tuple(q for q, p in g.pauli if p in ("X", "Y"))
+    return tuple(g.qubits)
 TOP = {"u1": 1, "d1": 2, "u2": 3, "cx": 4, "cz": 5, "swap": 6, "prot": 7}
 TILE_KINDS = {"u1", "d1", "u2", "cx", "cz", "swap", "prot"}
 MAX_BITS = 16
@@ -79,10 +87,10 @@ def plan_passes(gates: Sequence[Gate], n: int, t: int, nlow: int = DEFAULT_NLOW,
     t = min(t, n)
 
     def fits(g: Gate) -> bool:
-        return tileable(g) and (len(set(g.qubits)) <= t - 1 or t == n)
+        return tileable(g) and (len(set(active_qubits(g))) <= t - 1 or t == n)
 
     # keep room for the widest tile gate next to the always-local low bits
-    maxw = max([len(set(g.qubits)) for g in gates if fits(g)] or [1])
+    maxw = max([len(set(active_qubits(g))) for g in gates if fits(g)] or [1])
     nlow = n if t == n else max(1, min(nlow, t - maxw))
     low = set(range(n - nlow, n))  # qubits whose bits are 0..nlow-1
     queues: list[deque] = [deque() for _ in range(n)]
@@ -126,7 +134,7 @@ def plan_passes(gates: Sequence[Gate], n: int, t: int, nlow: int = DEFAULT_NLOW,
                 g = gates[i]
                 if not fits(g):
                     continue
-                new = set(g.qubits) - L
+                new = set(active_qubits(g)) - L
                 if len(L) + len(new) > t:
                     continue
                 c = len(new)
@@ -136,7 +144,7 @@ def plan_passes(gates: Sequence[Gate], n: int, t: int, nlow: int = DEFAULT_NLOW,
                         break
             if best is None:
                 break
-            L |= set(gates[best].qubits)
+            L |= set(active_qubits(gates[best]))
             order.append(best)
             execute(best)
         if not order:  # pragma: no cover - a ready tileable gate always fits an empty pass
@@ -254,8 +262,11 @@ def _generator(g: Gate, loc: dict) -> tuple[int, int, int, int, float] | None:
     if name == "phase":
         return 0, 0, 1 << loc[g.qubits[0]], 0, -2.0
     if name == "prot":
+        # Z factors outside `loc` enter through the op's zo / zg sign
         xm = zm = ny = 0
         for q, p in g.pauli:
+            if q not in loc:
+                continue
             b = 1 << loc[q]
             if p in "XY":
                 xm |= b
@@ -266,8 +277,10 @@ def _generator(g: Gate, loc: dict) -> tuple[int, int, int, int, float] | None:
     return None
 
 
-def _rotation_masks(g: Gate, loc: dict) -> tuple[int, int, int, int] | None:
-    """(xm, zm, cm, ny) of a Pauli-rotation gate (rx/ry/rz/rxx/ryy/rzz/cry/prot)."""
+def _rotation_masks(g: Gate, loc: dict, outer: dict | None = None, n: int | None = None) -> tuple | None:
+    """(xm, zm, cm, ny, zo, zg) of a Pauli-rotation gate (rx/ry/rz/rxx/ryy/rzz/cry/prot).
+    X/Y qubits must be in `loc`; Z qubits outside it go to zo (local bit via
+    `outer`, for register stages) or zg (global basis-index bit)."""
     from .ir import ROTATION_GENERATORS
 
     if g.rot is None:
@@ -284,51 +297,66 @@ def _rotation_masks(g: Gate, loc: dict) -> tuple[int, int, int, int] | None:
         cm = 1 << loc[g.qubits[0]]
     else:
         return None
-    xm = zm = ny = 0
+    xm = zm = ny = zo = zg = 0
     for q, p in pairs:
+        if q not in loc:
+            if p != "Z":
+                raise ValueError(f"qubit {q} ({p}) of a rotation is not local")
+            if outer is not None and q in outer:
+                zo |= 1 << outer[q]
+            else:
+                if n is None:
+                    raise ValueError("a non-local Z factor needs the qubit count")
+                zg |= 1 << (n - 1 - q)
+            continue
         b = 1 << loc[q]
         if p in "XY":
             xm |= b
         if p in "YZ":
             zm |= b
         ny += p == "Y"
-    return xm, zm, cm, ny
+    return xm, zm, cm, ny, zo, zg
 
 
 def op_fields(g: Gate, loc: dict, slot: int = -1, gen=None, pidx: int = -1, pscale: float = 1.0,
-              gcoef: float = 0.0, as_rotation: bool = False) -> tuple:
+              gcoef: float = 0.0, as_rotation: bool = False, outer: dict | None = None,
+              n: int | None = None) -> tuple:
     """Field values of one tq_tile_op: (kind, a, b, slot, xm, zm, cm, gxm, gzm,
-    gcm, gny, pidx, pscale, gcoef, matrix entries or None).  as_rotation=True
-    encodes Pauli rotations (and cry) as kind 7, which is cheaper than a dense
-    4x4 sweep; pidx >= 0 makes the device build the rotation from
-    theta[pidx] * pscale."""
+    gcm, gny, pidx, pscale, gcoef, zo, zg, matrix entries or None).
+    as_rotation=True encodes Pauli rotations (and cry) as kind 7, which is
+    cheaper than a dense 4x4 sweep; pidx >= 0 makes the device build the
+    rotation from theta[pidx] * pscale.  `outer` (local bits, for register
+    stages) and `n` place Z factors of Pauli rotations outside `loc`."""
     g = _canon(g)
-    rm = _rotation_masks(g, loc) if (as_rotation or pidx >= 0 or g.kind == "prot") else None
-    a = loc[g.qubits[0]]
-    b = loc[g.qubits[1]] if len(g.qubits) > 1 else 0
-    xm = zm = cm = 0
+    rm = _rotation_masks(g, loc, outer, n) if (as_rotation or pidx >= 0 or g.kind == "prot") else None
+    xm = zm = cm = zo = zg = 0
     if rm is not None:
-        xm, zm, cm, ny = rm
+        a = b = 0
+        xm, zm, cm, ny, zo, zg = rm
         kind = TOP["prot"]
         ang = g.rot[1]
         c, s = np.cos(0.5 * ang), np.sin(0.5 * ang)
         m = np.array([c, -1j * s * _PH[ny & 3]], dtype=np.complex128)
-    elif g.kind in ("u1", "u2"):
-        kind = TOP[g.kind]
-        m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
-    elif g.kind == "d1":
-        kind = TOP["d1"]
-        m = np.array([g.mat[0, 0], g.mat[1, 1]], dtype=np.complex128)
     else:
-        kind = TOP[g.kind]
-        m = None
+        a = loc[g.qubits[0]]
+        b = loc[g.qubits[1]] if len(g.qubits) > 1 else 0
+        if g.kind in ("u1", "u2"):
+            kind = TOP[g.kind]
+            m = np.asarray(g.mat, dtype=np.complex128).reshape(-1)
+        elif g.kind == "d1":
+            kind = TOP["d1"]
+            m = np.array([g.mat[0, 0], g.mat[1, 1]], dtype=np.complex128)
+        else:
+            kind = TOP[g.kind]
+            m = None
     if pidx >= 0 and rm is None and not (g.rot is not None and g.rot[0] == "phase"):
         raise ValueError(f"gate '{g.kind}' cannot take a device-side angle")
     gx, gz, gc, gn = gen[:4] if gen is not None else (0, 0, 0, 0)
-    return (kind, a, b, slot, xm, zm, cm, gx, gz, gc, gn, pidx, pscale, gcoef, m)
+    return (kind, a, b, slot, xm, zm, cm, gx, gz, gc, gn, pidx, pscale, gcoef, zo, zg, m)
 
 
-_SCALAR_FIELDS = ["kind", "a", "b", "slot", "xm", "zm", "cm", "gxm", "gzm", "gcm", "gny", "pidx", "pscale", "gcoef"]
+_SCALAR_FIELDS = ["kind", "a", "b", "slot", "xm", "zm", "cm", "gxm", "gzm", "gcm", "gny", "pidx", "pscale", "gcoef",
+                  "zo", "zg"]
 
 
 def pack_ops(fields: list) -> np.ndarray:
@@ -339,9 +367,9 @@ def pack_ops(fields: list) -> np.ndarray:
     for k, name in enumerate(_SCALAR_FIELDS):
         arr[name] = [f[k] for f in fields]
     for size in (2, 4, 16):
-        idx = [i for i, f in enumerate(fields) if f[14] is not None and f[14].size == size]
+        idx = [i for i, f in enumerate(fields) if f[16] is not None and f[16].size == size]
         if idx:
-            M = np.stack([fields[i][14] for i in idx])
+            M = np.stack([fields[i][16] for i in idx])
             flat = np.stack([M.real, M.imag], axis=-1).reshape(len(idx), -1)
             arr["md"][idx, : 2 * size] = flat
             arr["mf"][idx, : 2 * size] = flat.astype(np.float32)
@@ -403,10 +431,10 @@ def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, f
         if fuse and not reverse:
             for g, gi in _fuse_around_params(gl, idx, params):
                 if gi is None:
-                    fields.append(op_fields(g, loc))
+                    fields.append(op_fields(g, loc, n=n))
                 else:
                     pidx, psc = params[gi]
-                    fields.append(op_fields(g, loc, pidx=pidx, pscale=psc, as_rotation=True))
+                    fields.append(op_fields(g, loc, pidx=pidx, pscale=psc, as_rotation=True, n=n))
         else:
             for gi, g in zip(idx, gl):
                 slot = -1
@@ -418,7 +446,8 @@ def encode_passes(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], *, f
                     gen = _generator(g, loc)
                     coefs.append((slot, gen[4]))
                     gcoef = gen[4] * psc
-                fields.append(op_fields(g, loc, slot, gen, pidx=pidx, pscale=psc, gcoef=gcoef, as_rotation=True))
+                fields.append(op_fields(g, loc, slot, gen, pidx=pidx, pscale=psc, gcoef=gcoef, as_rotation=True,
+                                        n=n))
         p = TilePass()
         p.t = t
         p.nlow = min(pp.nlow, t)
@@ -474,18 +503,22 @@ STAGE_BITS = 4
 STAGED_MIN_T = 9
 
 
-def plan_stages(op_bits: Sequence[tuple], t: int, rb: int = STAGE_BITS) -> list[tuple[list, list]]:
+def plan_stages(op_bits: Sequence[tuple], t: int, rb: int = STAGE_BITS,
+                dep_bits: Sequence[tuple] | None = None) -> list[tuple[list, list]]:
     """Group ops (given as tuples of local bits, in a valid order) into stages
     of at most `rb` local bits by greedy DAG scheduling; each stage's bit set
-    is padded to exactly rb bits with the highest unused local bits."""
+    is padded to exactly rb bits with the highest unused local bits.
+    dep_bits (default op_bits): the bits that order an op against others (a
+    Pauli rotation's Z qubits order it but need not be in the stage)."""
+    dep = list(dep_bits) if dep_bits is not None else list(op_bits)
     queues: list[deque] = [deque() for _ in range(t)]
-    for i, bs in enumerate(op_bits):
+    for i, bs in enumerate(dep):
         for b in set(bs):
             queues[b].append(i)
     done = [False] * len(op_bits)
 
     def is_ready(i):
-        return all(queues[b] and queues[b][0] == i for b in set(op_bits[i]))
+        return all(queues[b] and queues[b][0] == i for b in set(dep[i]))
 
     ready = set(i for i in range(len(op_bits)) if is_ready(i))
     stages = []
@@ -511,7 +544,7 @@ def plan_stages(op_bits: Sequence[tuple], t: int, rb: int = STAGE_BITS) -> list[
             done[best] = True
             left -= 1
             ready.discard(best)
-            for b in set(op_bits[best]):
+            for b in set(dep[best]):
                 queues[b].popleft()
                 if queues[b] and not done[queues[b][0]] and is_ready(queues[b][0]):
                     ready.add(queues[b][0])
@@ -571,9 +604,11 @@ def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], para
                 else:
                     run.append(g)
             items += [(x, -1, 1.0, None) for x in fuse_pass(run, absorb=False)]
-        op_bits = [tuple(loc[q] for q in g.qubits) for g, _, _, _ in items]
+        # stage bits: qubits that must sit in registers; dependency bits: every local qubit touched
+        op_bits = [tuple(loc[q] for q in active_qubits(g)) for g, _, _, _ in items]
+        dep_bits = [tuple(loc[q] for q in g.qubits if q in loc) for g, _, _, _ in items]
         st_begin = len(stage_rows)
-        for bits, order in plan_stages(op_bits, t):
+        for bits, order in plan_stages(op_bits, t, dep_bits=dep_bits):
             reg = {b: k for k, b in enumerate(bits)}
             qreg = {q: reg[loc[q]] for q in qs if loc[q] in reg}
             ob = len(fields)
@@ -582,9 +617,10 @@ def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], para
                 if slots is not None and gi in slots:
                     gen = _generator(g, qreg)
                     fields.append(op_fields(g, qreg, slots[gi], gen, pidx=pidx, pscale=psc, gcoef=gen[4] * psc,
-                                            as_rotation=True))
+                                            as_rotation=True, outer=loc, n=n))
                 else:
-                    fields.append(op_fields(g, qreg, pidx=pidx, pscale=psc, as_rotation=pidx >= 0 or slots is not None))
+                    fields.append(op_fields(g, qreg, pidx=pidx, pscale=psc, as_rotation=pidx >= 0 or slots is not None,
+                                            outer=loc, n=n))
             stage_rows.append((bits, ob, len(fields)))
         p = TilePass()
         p.t = t
@@ -613,12 +649,14 @@ def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int
     t = min(t, n)
     if staged is None:
         staged = (fuse and STAGED_MIN_T <= t <= (13 if dtype == torch.complex64 else 12)
-                  and all(len(set(g.qubits)) <= STAGE_BITS for g in gates))
+                  and all(len(set(active_qubits(g))) <= STAGE_BITS for g in gates))
     segs = plan_passes(gates, n, t, nlow)
     out = []
     npass = 0
     for s in segs:
         if s.kind == "gate":
+            if params is not None and s.gate in params:
+                raise NotImplementedError("a device-angle gate must fit a tile (X/Y support <= t-1 qubits)")
             out.append(("gate", gates[s.gate]))
         elif staged:
             enc = encode_staged(n, s.passes, gates, params=params)

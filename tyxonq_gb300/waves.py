@@ -197,6 +197,8 @@ class WavePlan:
         slots = {ri: rparams[ri][0] for ri in rparams}
         adj = []
         for s in plan_passes(rg, n, t, max_ops=self.max_ops):
+            if s.kind != "tiles":
+                raise NotImplementedError("wave path needs tileable gates")
             for pp in s.passes:
                 enc = encode_staged(n, [pp], rg, params=rparams, slots=slots)
                 pid = self._add_staged(enc)[0]
