@@ -47,7 +47,7 @@ __device__ __forceinline__ void r_d1(cplx<R>* x, cplx<R> d0, cplx<R> d1, bool lo
 }
 
 template <typename R, int A, int B>
-__device__ __forceinline__ void r_u2(cplx<R>* x, const cplx<R>* u) {
+__device__ __forceinline__ void r_u2(cplx<R>* x, const tq_tile_op& o, bool adj) {
 #pragma unroll
   for (int i = 0; i < kNR; ++i) {
     if (((i >> A) & 1) || ((i >> B) & 1)) continue;
@@ -55,10 +55,16 @@ __device__ __forceinline__ void r_u2(cplx<R>* x, const cplx<R>* u) {
     const cplx<R> v0 = x[id[0]], v1 = x[id[1]], v2 = x[id[2]], v3 = x[id[3]];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      cplx<R> acc = cmul(u[4 * r], v0);
-      acc = cfma(u[4 * r + 1], v1, acc);
-      acc = cfma(u[4 * r + 2], v2, acc);
-      acc = cfma(u[4 * r + 3], v3, acc);
+      cplx<R> u[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        u[c] = adj ? op_m<R>(o, 4 * c + r) : op_m<R>(o, 4 * r + c);
+        if (adj) u[c].y = -u[c].y;
+      }
+      cplx<R> acc = cmul(u[0], v0);
+      acc = cfma(u[1], v1, acc);
+      acc = cfma(u[2], v2, acc);
+      acc = cfma(u[3], v3, acc);
       x[id[r]] = acc;
     }
   }
@@ -132,20 +138,20 @@ __device__ __forceinline__ void r_prot(cplx<R>* x, uint32_t zm, uint32_t cm, cpl
   }
 
 template <typename R>
-__device__ __forceinline__ void r_u2_dispatch(cplx<R>* x, const tq_tile_op& o, const cplx<R>* u) {
+__device__ __forceinline__ void r_u2_dispatch(cplx<R>* x, const tq_tile_op& o, bool adj) {
   switch (o.a * 4 + o.b) {
-    case 1: r_u2<R, 0, 1>(x, u); break;
-    case 2: r_u2<R, 0, 2>(x, u); break;
-    case 3: r_u2<R, 0, 3>(x, u); break;
-    case 4: r_u2<R, 1, 0>(x, u); break;
-    case 6: r_u2<R, 1, 2>(x, u); break;
-    case 7: r_u2<R, 1, 3>(x, u); break;
-    case 8: r_u2<R, 2, 0>(x, u); break;
-    case 9: r_u2<R, 2, 1>(x, u); break;
-    case 11: r_u2<R, 2, 3>(x, u); break;
-    case 12: r_u2<R, 3, 0>(x, u); break;
-    case 13: r_u2<R, 3, 1>(x, u); break;
-    case 14: r_u2<R, 3, 2>(x, u); break;
+    case 1: r_u2<R, 0, 1>(x, o, adj); break;
+    case 2: r_u2<R, 0, 2>(x, o, adj); break;
+    case 3: r_u2<R, 0, 3>(x, o, adj); break;
+    case 4: r_u2<R, 1, 0>(x, o, adj); break;
+    case 6: r_u2<R, 1, 2>(x, o, adj); break;
+    case 7: r_u2<R, 1, 3>(x, o, adj); break;
+    case 8: r_u2<R, 2, 0>(x, o, adj); break;
+    case 9: r_u2<R, 2, 1>(x, o, adj); break;
+    case 11: r_u2<R, 2, 3>(x, o, adj); break;
+    case 12: r_u2<R, 3, 0>(x, o, adj); break;
+    case 13: r_u2<R, 3, 1>(x, o, adj); break;
+    case 14: r_u2<R, 3, 2>(x, o, adj); break;
     default: break;
   }
 }
@@ -193,19 +199,9 @@ __device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const d
       }
       break;
     }
-    case TOP_U2: {
-      cplx<R> u[16];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          cplx<R> v = adj ? op_m<R>(o, 4 * c + r) : op_m<R>(o, 4 * r + c);
-          if (adj) v.y = -v.y;
-          u[4 * r + c] = v;
-        }
-      r_u2_dispatch<R>(x, o, u);
+    case TOP_U2:
+      r_u2_dispatch<R>(x, o, adj);
       break;
-    }
     case TOP_CX: TQ_CASE_AB(r_perm, R, 0) break;
     case TOP_SWAP: TQ_CASE_AB(r_perm, R, 1) break;
     case TOP_CZ: TQ_CASE_AB(r_perm, R, 2) break;
@@ -243,8 +239,11 @@ __device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const d
 // Per-thread register <-> padded shared-memory index of register i for a stage
 // with register bits b[0..3] (ascending local positions).
 struct StageMap {
-  int base;     // local index with all register bits zero
-  int off[kNR]; // local offset of register i
+  int base;       // local index with all register bits zero
+  int m[kRB];     // 1 << bits[k]
+  __device__ __forceinline__ int idx(int i) const {  // i is a compile-time constant at every call
+    return base | ((i & 1) ? m[0] : 0) | ((i & 2) ? m[1] : 0) | ((i & 4) ? m[2] : 0) | ((i & 8) ? m[3] : 0);
+  }
 };
 
 __device__ __forceinline__ StageMap stage_map(const tq_tile_stage& st, int tid) {
@@ -254,13 +253,7 @@ __device__ __forceinline__ StageMap stage_map(const tq_tile_stage& st, int tid) 
   for (int k = 0; k < kRB; ++k) b = insz(b, st.bits[k]);
   m.base = b;
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
-    int o = 0;
-#pragma unroll
-    for (int k = 0; k < kRB; ++k)
-      if ((i >> k) & 1) o |= 1 << st.bits[k];
-    m.off[i] = o;
-  }
+  for (int k = 0; k < kRB; ++k) m.m[k] = 1 << st.bits[k];
   return m;
 }
 
@@ -275,13 +268,13 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, const tq_tile_stage* __re
     const StageMap m = stage_map(st, tid);
     cplx<R> x[kNR];
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) x[i] = s[pphys(m.base | m.off[i])];
+    for (int i = 0; i < kNR; ++i) x[i] = s[pphys(m.idx(i))];
     for (int k = st.op_begin; k < st.op_end; ++k) {
       const tq_tile_op& o = ops[k];
       r_apply<R>(x, o, theta, adj, zsign<R>(o, gbase, m.base));
     }
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) s[pphys(m.base | m.off[i])] = x[i];
+    for (int i = 0; i < kNR; ++i) s[pphys(m.idx(i))] = x[i];
     __syncthreads();
   }
 }

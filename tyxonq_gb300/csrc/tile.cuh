@@ -49,11 +49,10 @@ __device__ __forceinline__ void prot_coeffs(const tq_tile_op& o, const double* t
   R c, s;
   rot_cs(o.pscale * theta[o.pidx], c, s);
   const int ny = __popc(o.xm & o.zm) & 3;
-  // -i s i^ny
-  const R re[4] = {R(0), s, R(0), -s};
-  const R im[4] = {-s, R(0), s, R(0)};
+  // -i s i^ny: ny = 0 -> (0, -s), 1 -> (s, 0), 2 -> (0, s), 3 -> (-s, 0)
+  const R sg = (ny >= 2) ? -s : s;
   m0 = cplx<R>(c, R(0));
-  m1 = cplx<R>(re[ny], im[ny]);
+  m1 = (ny & 1) ? cplx<R>(sg, R(0)) : cplx<R>(R(0), -sg);
 }
 
 // Sign of a Pauli rotation's Z factors that lie outside the amplitudes being

@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(512) k_wave_adjoint(const tq_wave_item* __rest
       cplx<R> x[kNR], y[kNR];
 #pragma unroll
       for (int i = 0; i < kNR; ++i) {
-        const int j = pphys(mp.base | mp.off[i]);
+        const int j = pphys(mp.idx(i));
         x[i] = sp[j];
         y[i] = sl[j];
       }
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(512) k_wave_adjoint(const tq_wave_item* __rest
       }
 #pragma unroll
       for (int i = 0; i < kNR; ++i) {
-        const int j = pphys(mp.base | mp.off[i]);
+        const int j = pphys(mp.idx(i));
         sp[j] = x[i];
         sl[j] = y[i];
       }
