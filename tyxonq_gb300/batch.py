@@ -57,7 +57,7 @@ class Schedule:
     max_pass_ops: int = 512
     large: str = "waves"  # instances above res1_max: "waves" (L2-resident grid-wide phases) or "cta"
     wave_t: int = 12
-    wave_hbits: int = 12
+    wave_hbits: int = 10
     wave_budget: int = 48 << 20
     wave_max_ops: int = 256
 

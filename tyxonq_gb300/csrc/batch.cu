@@ -68,17 +68,58 @@ __device__ void eval_resident(const BatchArgs& A, const tq_batch_inst& I, int in
     tile_apply<R>(psi, n, A.ops[k], gtid, gsize, false, th);
     gsync(bar, gsize);
   }
-  // lam = H psi, and E = Re <psi|lam>
+  // lam = H psi, and E = Re <psi|lam>.  Thread owns j = gtid + k * gsize (k < N / gsize
+  // <= 8 for every size class); the term sign parity splits as in k_wave_hpsi.
   R eloc = 0;
-  for (int j = gtid; j < N; j += gsize) {
-    cplx<R> acc(0, 0);
+  const int lg = 31 - __clz(gsize);
+  const int per = N >> lg;
+  if (per >= 1 && per <= 8 && (gsize << lg) != 0) {
+    cplx<R> acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = cplx<R>(0, 0);
     for (int g = I.group_begin; g < I.group_begin + I.group_count; ++g) {
-      const int k = j ^ (int)__ldg(&A.pgroups[g].flip);
-      const cplx<R> f = group_f<R>(A.terms, __ldg(&A.pgroups[g].first_term), __ldg(&A.pgroups[g].n_terms), (uint64_t)k);
-      acc = cfma(f, psi[k], acc);
+      const int m = (int)__ldg(&A.pgroups[g].flip);
+      const int first = __ldg(&A.pgroups[g].first_term), cnt = __ldg(&A.pgroups[g].n_terms);
+      cplx<R> f[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) f[k] = cplx<R>(0, 0);
+      const int sbase = gtid ^ m;
+      for (int tt = 0; tt < cnt; ++tt) {
+        const int zy = (int)__ldg(&A.terms[first + tt].zy);
+        const R wr = (R)__ldg(&A.terms[first + tt].w_re), wi = (R)__ldg(&A.terms[first + tt].w_im);
+        const int p0 = __popc(sbase & zy) & 1;
+        const int kz = zy >> lg;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int kp = k & kz;
+          const int par = p0 ^ ((kp ^ (kp >> 1) ^ (kp >> 2)) & 1);
+          f[k].x += par ? -wr : wr;
+          f[k].y += par ? -wi : wi;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (k < per) acc[k] = cfma(f[k], psi[(gtid + (k << lg)) ^ m], acc[k]);
     }
-    lam[j] = acc;
-    eloc += psi[j].x * acc.x + psi[j].y * acc.y;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (k < per) {
+        const int j = gtid + (k << lg);
+        lam[j] = acc[k];
+        eloc += psi[j].x * acc[k].x + psi[j].y * acc[k].y;
+      }
+  } else {
+    for (int j = gtid; j < N; j += gsize) {
+      cplx<R> acc(0, 0);
+      for (int g = I.group_begin; g < I.group_begin + I.group_count; ++g) {
+        const int k = j ^ (int)__ldg(&A.pgroups[g].flip);
+        const cplx<R> f =
+            group_f<R>(A.terms, __ldg(&A.pgroups[g].first_term), __ldg(&A.pgroups[g].n_terms), (uint64_t)k);
+        acc = cfma(f, psi[k], acc);
+      }
+      lam[j] = acc;
+      eloc += psi[j].x * acc.x + psi[j].y * acc.y;
+    }
   }
   const double E = group_sum((double)eloc, red, gtid, gsize, bar);
   // reverse sweep

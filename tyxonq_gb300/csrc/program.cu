@@ -414,7 +414,7 @@ __device__ __forceinline__ void staged_store(const cplx<R>* s, typename C2<R>::T
 }
 
 template <typename R>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, 1)
     k_staged_forward(typename C2<R>::T* psi, int n, const PassArgs P, const tq_tile_stage* __restrict__ stages,
                      const tq_tile_op* __restrict__ ops, const double* __restrict__ theta, int dbuf) {
   extern __shared__ __align__(16) unsigned char smem[];

@@ -80,7 +80,7 @@ __device__ __forceinline__ void w_store(const cplx<R>* s, typename C2<R>::T* g, 
 
 // ------------------------------------------------------------------ forward
 template <typename R>
-__global__ void __launch_bounds__(512) k_wave_forward(const tq_wave_item* __restrict__ items, int n_items,
+__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_forward(const tq_wave_item* __restrict__ items, int n_items,
                                                       const tq_tile_pass* __restrict__ passes,
                                                       const tq_tile_stage* __restrict__ stages,
                                                       const tq_tile_op* __restrict__ ops,
@@ -133,19 +133,38 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
     cplx<R> acc[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) acc[k] = cplx<R>(0, 0);
+    const bool full = (HN >= PER * (int)blockDim.x);
     for (int g = I.group_begin; g < I.group_begin + I.group_count; ++g) {
       const uint64_t m = __ldg(&groups[g].flip);
       const int first = __ldg(&groups[g].first_term), cnt = __ldg(&groups[g].n_terms);
+      // partner amplitudes first (independent loads in flight), then each term once for all of them
+      cplx<R> pv[PER], f[PER];
 #pragma unroll
       for (int k = 0; k < PER; ++k) {
         const int j = threadIdx.x + k * blockDim.x;
-        if (j < HN) {
-          const int64_t src = (t0 + j) ^ (int64_t)m;
-          const T2 v = psi[src];
-          const cplx<R> f = group_f<R>(terms, first, cnt, (uint64_t)src);
-          acc[k] = cfma(f, cplx<R>(v.x, v.y), acc[k]);
+        const T2 v = (full || j < HN) ? psi[(t0 + j) ^ (int64_t)m] : T2();
+        pv[k] = cplx<R>(v.x, v.y);
+        f[k] = cplx<R>(0, 0);
+      }
+      // src_k = (t0 | tid | k << 8) ^ m with disjoint bit fields (t0 is a multiple of
+      // 2^hb = PER * 256), so parity(src_k & zy) = parity((t0 | tid) ^ m) & zy)
+      // XOR parity(k & (zy >> 8)): one popc per term and thread, not one per amplitude.
+      const uint64_t sbase = (uint64_t)((t0 | (int64_t)threadIdx.x) ^ (int64_t)m);
+      for (int tt = 0; tt < cnt; ++tt) {
+        const uint64_t zy = __ldg(&terms[first + tt].zy);
+        const R wr = (R)__ldg(&terms[first + tt].w_re), wi = (R)__ldg(&terms[first + tt].w_im);
+        const int p0 = __popcll(sbase & zy) & 1;
+        const int kz = (int)(zy >> 8);
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+          const int kp = k & kz;
+          const int par = p0 ^ ((kp ^ (kp >> 1) ^ (kp >> 2) ^ (kp >> 3)) & 1);
+          f[k].x += par ? -wr : wr;
+          f[k].y += par ? -wi : wi;
         }
       }
+#pragma unroll
+      for (int k = 0; k < PER; ++k) acc[k] = cfma(f[k], pv[k], acc[k]);
     }
     R eloc = 0;
 #pragma unroll
@@ -217,7 +236,7 @@ __device__ __forceinline__ R r_grad_dispatch(const cplx<R>* x, const cplx<R>* y,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(512) k_wave_adjoint(const tq_wave_item* __restrict__ items, int n_items,
+__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_adjoint(const tq_wave_item* __restrict__ items, int n_items,
                                                       const tq_tile_pass* __restrict__ passes,
                                                       const tq_tile_stage* __restrict__ stages,
                                                       const tq_tile_op* __restrict__ ops,
