@@ -413,6 +413,15 @@ __device__ __forceinline__ void staged_store(const cplx<R>* s, typename C2<R>::T
   }
 }
 
+// Compiled ops of one pass kept in shared memory for all its tiles.
+constexpr int kStagedRopCap = 256;
+
+// Offset-table bytes of a staged pass, rounded up to 16 (the compiled ops follow it).
+__host__ __device__ __forceinline__ size_t staged_hoff_bytes(int t, int nlow) {
+  return ((sizeof(int64_t) << (t - nlow)) + 15) & ~size_t(15);
+}
+
+// Shared memory: one or two padded tiles | offset table | compiled ops.
 template <typename R>
 __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, 1)
     k_staged_forward(typename C2<R>::T* psi, int n, const PassArgs P, const tq_tile_stage* __restrict__ stages,
@@ -422,7 +431,13 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, 1)
   cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem);
   cplx<R>* buf1 = buf0 + (dbuf ? PT : 0);
   int64_t* hoff = reinterpret_cast<int64_t*>(smem + (size_t)(dbuf ? 2 : 1) * PT * sizeof(cplx<R>));
+  ROp<R>* rops = reinterpret_cast<ROp<R>*>(reinterpret_cast<unsigned char*>(hoff) + staged_hoff_bytes(P.t, P.nlow));
   build_hoff(hoff, P);
+  // compile the whole pass once when it fits, else stage by stage per tile
+  const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
+  const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
+  const bool resident = nops <= kStagedRopCap;
+  if (resident) rops_build<R>(rops, ops, op0, op0 + nops, theta, false, false);
   __syncthreads();
   const int64_t ntiles = int64_t(1) << (n - P.t);
   int64_t g = blockIdx.x;
@@ -440,7 +455,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, 1)
       cp_async_wait_group<0>();
     }
     __syncthreads();
-    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta, false, (uint64_t)tile_base(g, P));
+    run_stages<R>(s, rops, resident, op0, stages, P.op_begin, P.op_end, ops, theta, (uint64_t)tile_base(g, P));
     staged_store<R>(s, psi, tile_base(g, P), hoff, P);
     __syncthreads();
     if (!dbuf && gn < ntiles) {
@@ -465,7 +480,7 @@ static int run_staged(void* psi, int n, const tq_tile_pass* passes, int n_passes
     const int64_t ntiles = int64_t(1) << (n - P.t);
     const int dbuf = ntiles > sms ? 1 : 0;
     const size_t smem = (size_t)(dbuf ? 2 : 1) * padded_len(P.t) * sizeof(cplx<R>) +
-                        (sizeof(int64_t) << (P.t - P.nlow));
+                        staged_hoff_bytes(P.t, P.nlow) + kStagedRopCap * sizeof(ROp<R>);
     cudaError_t e = cudaFuncSetAttribute(k_staged_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "tq_sv_run_staged: smem attribute");
     const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);

@@ -4,9 +4,15 @@
 // a 2^(t-4)-thread CTA holds the 16 amplitudes whose other local bits spell
 // tid; every op of the stage acts on register bits only, so it is applied to
 // those 16 registers without touching shared memory.  Shared memory is read
-// and written once per stage instead of once per op.  Register-bit indices
-// are runtime values; each op kind dispatches to code instantiated for every
-// bit combination so the register array is only ever indexed by constants.
+// and written once per stage instead of once per op.
+//
+// Before a stage runs, its ops are compiled (one thread per op) into compact
+// shared-memory records (ROp): angles are turned into coefficients, the
+// adjoint is folded in, and the op's shape picks a specialised routine --
+// a real or imaginary single-bit rotation costs 8 FMAs per amplitude pair
+// instead of a dense complex 2x2.  Register-bit indices are runtime values;
+// each routine is instantiated for every bit (combination) and the record's
+// code selects one, so the register array is only ever indexed by constants.
 //
 // Shared-memory tiles are padded by 2 amplitudes per 16 (phys = j + 2*(j>>4)):
 // the pad keeps 16-byte chunks aligned for cp.async and spreads the
@@ -19,10 +25,12 @@ namespace tq {
 
 constexpr int kRB = 4;            // register bits per stage
 constexpr int kNR = 1 << kRB;     // amplitudes per thread
+constexpr int kRopCap = 64;       // compiled ops held in shared memory at once
 
 __device__ __forceinline__ int pphys(int j) { return j + ((j >> 4) << 1); }
 __host__ __device__ __forceinline__ int padded_len(int t) { return (1 << t) + ((1 << t) >> 3); }
 
+// ------------------------------------------------------------------ register routines
 template <typename R, int K>
 __device__ __forceinline__ void r_u1(cplx<R>* x, cplx<R> u0, cplx<R> u1, cplx<R> u2, cplx<R> u3) {
 #pragma unroll
@@ -35,15 +43,43 @@ __device__ __forceinline__ void r_u1(cplx<R>* x, cplx<R> u0, cplx<R> u1, cplx<R>
   }
 }
 
+// [[c, a01], [a10, c]] with real entries
 template <typename R, int K>
-__device__ __forceinline__ void r_d1(cplx<R>* x, cplx<R> d0, cplx<R> d1, bool lo_id) {
+__device__ __forceinline__ void r_rr(cplx<R>* x, R c, R a01, R a10) {
 #pragma unroll
   for (int i = 0; i < kNR; ++i) {
-    if ((i >> K) & 1)
-      x[i] = cmul(d1, x[i]);
-    else if (!lo_id)
-      x[i] = cmul(d0, x[i]);
+    if ((i >> K) & 1) continue;
+    const int j = i | (1 << K);
+    const cplx<R> u = x[i], v = x[j];
+    x[i] = cplx<R>(fma(a01, v.x, c * u.x), fma(a01, v.y, c * u.y));
+    x[j] = cplx<R>(fma(a10, u.x, c * v.x), fma(a10, u.y, c * v.y));
   }
+}
+
+// [[c, i b01], [i b10, c]] with c, b01, b10 real
+template <typename R, int K>
+__device__ __forceinline__ void r_ri(cplx<R>* x, R c, R b01, R b10) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i >> K) & 1) continue;
+    const int j = i | (1 << K);
+    const cplx<R> u = x[i], v = x[j];
+    x[i] = cplx<R>(fma(-b01, v.y, c * u.x), fma(b01, v.x, c * u.y));
+    x[j] = cplx<R>(fma(-b10, u.y, c * v.x), fma(b10, u.x, c * v.y));
+  }
+}
+
+template <typename R, int K>
+__device__ __forceinline__ void r_d1(cplx<R>* x, cplx<R> d0, cplx<R> d1) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) x[i] = cmul(((i >> K) & 1) ? d1 : d0, x[i]);
+}
+
+template <typename R, int K>
+__device__ __forceinline__ void r_dh(cplx<R>* x, cplx<R> d1) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i)
+    if ((i >> K) & 1) x[i] = cmul(d1, x[i]);
 }
 
 template <typename R, int A, int B>
@@ -120,23 +156,6 @@ __device__ __forceinline__ void r_prot(cplx<R>* x, uint32_t zm, uint32_t cm, cpl
   }
 }
 
-#define TQ_CASE_AB(FN, ...)                                          \
-  switch (o.a * 4 + o.b) {                                            \
-    case 1: FN<__VA_ARGS__, 0, 1>(x); break;                          \
-    case 2: FN<__VA_ARGS__, 0, 2>(x); break;                          \
-    case 3: FN<__VA_ARGS__, 0, 3>(x); break;                          \
-    case 4: FN<__VA_ARGS__, 1, 0>(x); break;                          \
-    case 6: FN<__VA_ARGS__, 1, 2>(x); break;                          \
-    case 7: FN<__VA_ARGS__, 1, 3>(x); break;                          \
-    case 8: FN<__VA_ARGS__, 2, 0>(x); break;                          \
-    case 9: FN<__VA_ARGS__, 2, 1>(x); break;                          \
-    case 11: FN<__VA_ARGS__, 2, 3>(x); break;                         \
-    case 12: FN<__VA_ARGS__, 3, 0>(x); break;                         \
-    case 13: FN<__VA_ARGS__, 3, 1>(x); break;                         \
-    case 14: FN<__VA_ARGS__, 3, 2>(x); break;                         \
-    default: break;                                                   \
-  }
-
 template <typename R>
 __device__ __forceinline__ void r_u2_dispatch(cplx<R>* x, const tq_tile_op& o, bool adj) {
   switch (o.a * 4 + o.b) {
@@ -156,10 +175,156 @@ __device__ __forceinline__ void r_u2_dispatch(cplx<R>* x, const tq_tile_op& o, b
   }
 }
 
-// Apply one op (bit indices in register space 0..3) to the 16 registers.
 template <typename R>
-__device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const double* theta, bool adj,
-                                        R zs = R(1)) {
+__device__ __forceinline__ void r_prot_dispatch(cplx<R>* x, uint32_t xm, uint32_t zm, uint32_t cm, cplx<R> c,
+                                                cplx<R> w) {
+  switch (xm & 15) {
+    case 0: r_prot<R, 0>(x, zm, cm, c, w); break;
+    case 1: r_prot<R, 1>(x, zm, cm, c, w); break;
+    case 2: r_prot<R, 2>(x, zm, cm, c, w); break;
+    case 3: r_prot<R, 3>(x, zm, cm, c, w); break;
+    case 4: r_prot<R, 4>(x, zm, cm, c, w); break;
+    case 5: r_prot<R, 5>(x, zm, cm, c, w); break;
+    case 6: r_prot<R, 6>(x, zm, cm, c, w); break;
+    case 7: r_prot<R, 7>(x, zm, cm, c, w); break;
+    case 8: r_prot<R, 8>(x, zm, cm, c, w); break;
+    case 9: r_prot<R, 9>(x, zm, cm, c, w); break;
+    case 10: r_prot<R, 10>(x, zm, cm, c, w); break;
+    case 11: r_prot<R, 11>(x, zm, cm, c, w); break;
+    case 12: r_prot<R, 12>(x, zm, cm, c, w); break;
+    case 13: r_prot<R, 13>(x, zm, cm, c, w); break;
+    case 14: r_prot<R, 14>(x, zm, cm, c, w); break;
+    default: r_prot<R, 15>(x, zm, cm, c, w); break;
+  }
+}
+
+// ------------------------------------------------------------------ gradient routines
+// Im <lam|G|psi> over the 16 register amplitudes (x = psi, y = lam):
+// G|i> = [i & cm == cm] ph (-1)^{popc(i & zm)} |i ^ XM>  (register-bit masks).
+template <typename R, int XM>
+__device__ __forceinline__ R r_grad(const cplx<R>* x, const cplx<R>* y, uint32_t zm, uint32_t cm, cplx<R> ph) {
+  R acc = 0;
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i & cm) != cm) continue;
+    const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
+    const cplx<R> v = cmul(ph, x[i]);
+    const cplx<R> l = y[i ^ XM];
+    acc += sg * (l.x * v.y - l.y * v.x);
+  }
+  return acc;
+}
+
+template <typename R>
+__device__ __forceinline__ R r_grad_dispatch(const cplx<R>* x, const cplx<R>* y, const tq_tile_op& o) {
+  const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
+  const cplx<R> ph(re[o.gny & 3], im[o.gny & 3]);
+  const uint32_t zm = o.gzm, cm = o.gcm;
+  switch (o.gxm & 15) {
+    case 0: return r_grad<R, 0>(x, y, zm, cm, ph);
+    case 1: return r_grad<R, 1>(x, y, zm, cm, ph);
+    case 2: return r_grad<R, 2>(x, y, zm, cm, ph);
+    case 3: return r_grad<R, 3>(x, y, zm, cm, ph);
+    case 4: return r_grad<R, 4>(x, y, zm, cm, ph);
+    case 5: return r_grad<R, 5>(x, y, zm, cm, ph);
+    case 6: return r_grad<R, 6>(x, y, zm, cm, ph);
+    case 7: return r_grad<R, 7>(x, y, zm, cm, ph);
+    case 8: return r_grad<R, 8>(x, y, zm, cm, ph);
+    case 9: return r_grad<R, 9>(x, y, zm, cm, ph);
+    case 10: return r_grad<R, 10>(x, y, zm, cm, ph);
+    case 11: return r_grad<R, 11>(x, y, zm, cm, ph);
+    case 12: return r_grad<R, 12>(x, y, zm, cm, ph);
+    case 13: return r_grad<R, 13>(x, y, zm, cm, ph);
+    case 14: return r_grad<R, 14>(x, y, zm, cm, ph);
+    default: return r_grad<R, 15>(x, y, zm, cm, ph);
+  }
+}
+
+// G flips bit K, Z factors only on K (sign w1 on the bit-K-set half):
+// Im(ph (sum conj(y_j) x_i + w1 sum conj(y_i) x_j)), i = j ^ (1 << K), bit K of i clear.
+template <typename R, int K>
+__device__ __forceinline__ R g_pair(const cplx<R>* x, const cplx<R>* y, cplx<R> ph, R w1) {
+  R ax = 0, ay = 0, bx = 0, by = 0;
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i >> K) & 1) continue;
+    const int j = i | (1 << K);
+    ax = fma(y[j].x, x[i].x, fma(y[j].y, x[i].y, ax));
+    ay = fma(y[j].x, x[i].y, fma(-y[j].y, x[i].x, ay));
+    bx = fma(y[i].x, x[j].x, fma(y[i].y, x[j].y, bx));
+    by = fma(y[i].x, x[j].y, fma(-y[i].y, x[j].x, by));
+  }
+  const R zx = fma(w1, bx, ax), zy = fma(w1, by, ay);
+  return ph.x * zy + ph.y * zx;
+}
+
+// Diagonal G: weight w0 where bit K is clear, w1 where it is set.
+template <typename R, int K>
+__device__ __forceinline__ R g_diag(const cplx<R>* x, const cplx<R>* y, cplx<R> ph, R w0, R w1) {
+  R s0x = 0, s0y = 0, s1x = 0, s1y = 0;
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i >> K) & 1) {
+      s1x = fma(y[i].x, x[i].x, fma(y[i].y, x[i].y, s1x));
+      s1y = fma(y[i].x, x[i].y, fma(-y[i].y, x[i].x, s1y));
+    } else {
+      s0x = fma(y[i].x, x[i].x, fma(y[i].y, x[i].y, s0x));
+      s0y = fma(y[i].x, x[i].y, fma(-y[i].y, x[i].x, s0y));
+    }
+  }
+  const R zx = fma(w1, s1x, w0 * s0x), zy = fma(w1, s1y, w0 * s0y);
+  return ph.x * zy + ph.y * zx;
+}
+
+// ------------------------------------------------------------------ compiled ops
+enum RCode : int32_t {
+  RC_NOP = 0,
+  RC_U1 = 1,     // + K: dense 2x2 m0..m3; the per-thread sign scales m1, m2
+  RC_RR = 5,     // + K: [[c, a01], [a10, c]] real: m0.x, m1.x, m2.x
+  RC_RI = 9,     // + K: [[c, i b01], [i b10, c]]: m0.x, m1.y, m2.y
+  RC_D = 13,     // + K: diag(m0, m1); a negative sign swaps the two
+  RC_DH = 17,    // + K: diag(1, m1)
+  RC_CX = 21,    // + pair index (12 ordered pairs)
+  RC_SWAP = 33,
+  RC_CZ = 45,
+  RC_U2 = 57,    // dense 4x4 read from the op table
+  RC_PROT = 58,  // general Pauli rotation: c = m0, w = m1, masks from the op table
+};
+enum RGCode : int32_t { RG_NONE = -1, RG_GEN = 0, RG_PAIR = 1, RG_DIAG = 5 };
+
+template <typename R>
+struct __align__(16) ROp {
+  int32_t code;   // RCode (+ register bit or pair index)
+  int32_t gcode;  // RGCode (+ register bit); RG_NONE: no gradient slot
+  int32_t op;     // index of the source op in the op table
+  uint32_t zo;    // local bits outside the stage whose parity signs the op
+  uint64_t zg;    // global bits outside the tile whose parity signs the op
+  cplx<R> m[4];
+  cplx<R> gph;    // i^ny of the generator
+  R gw0, gw1;
+};
+
+// ordered pair (a, b), a != b, of register bits -> 0..11
+__device__ __forceinline__ int pair_index(int a, int b) { return a * 3 + (b < a ? b : b - 1); }
+
+__device__ __forceinline__ bool one_bit(uint32_t m) { return m != 0 && (m & (m - 1)) == 0; }
+
+// Compile op o (table index k) into r.  adj: the record applies o^dagger;
+// grad: fill the gradient routine of an op with a slot.
+template <typename R>
+__device__ __forceinline__ void rop_build(ROp<R>& r, const tq_tile_op& o, int k, const double* theta, bool adj,
+                                          bool grad) {
+  ROp<R> q;
+  q.code = RC_NOP;
+  q.gcode = RG_NONE;
+  q.op = k;
+  q.zo = o.zo;
+  q.zg = o.zg;
+  const cplx<R> z(R(0), R(0));
+  q.m[0] = q.m[1] = q.m[2] = q.m[3] = z;
+  q.gph = z;
+  q.gw0 = q.gw1 = R(0);
+  const int a = o.a & 3, b = o.b & 3;
   switch (o.kind) {
     case TOP_U1: {
       cplx<R> u0 = op_m<R>(o, 0), u1 = op_m<R>(o, 1), u2 = op_m<R>(o, 2), u3 = op_m<R>(o, 3);
@@ -170,17 +335,16 @@ __device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const d
         u2 = cplx<R>(t1.x, -t1.y);
         u3 = cplx<R>(u3.x, -u3.y);
       }
-      switch (o.a) {
-        case 0: r_u1<R, 0>(x, u0, u1, u2, u3); break;
-        case 1: r_u1<R, 1>(x, u0, u1, u2, u3); break;
-        case 2: r_u1<R, 2>(x, u0, u1, u2, u3); break;
-        default: r_u1<R, 3>(x, u0, u1, u2, u3); break;
-      }
+      q.code = RC_U1 + a;
+      q.m[0] = u0;
+      q.m[1] = u1;
+      q.m[2] = u2;
+      q.m[3] = u3;
       break;
     }
     case TOP_D1: {
       cplx<R> d0 = op_m<R>(o, 0), d1 = op_m<R>(o, 1);
-      if (o.pidx >= 0 && theta != nullptr) {
+      if (o.pidx >= 0 && theta != nullptr) {  // phase(a) = diag(1, e^{ia})
         R c, sn;
         rot_cs(2.0 * o.pscale * theta[o.pidx], c, sn);
         d0 = cplx<R>(R(1), R(0));
@@ -190,52 +354,147 @@ __device__ __forceinline__ void r_apply(cplx<R>* x, const tq_tile_op& o, const d
         d0.y = -d0.y;
         d1.y = -d1.y;
       }
-      const bool lo_id = (d0.x == R(1) && d0.y == R(0));
-      switch (o.a) {
-        case 0: r_d1<R, 0>(x, d0, d1, lo_id); break;
-        case 1: r_d1<R, 1>(x, d0, d1, lo_id); break;
-        case 2: r_d1<R, 2>(x, d0, d1, lo_id); break;
-        default: r_d1<R, 3>(x, d0, d1, lo_id); break;
-      }
+      q.code = (d0.x == R(1) && d0.y == R(0)) ? RC_DH + a : RC_D + a;
+      q.m[0] = d0;
+      q.m[1] = d1;
       break;
     }
-    case TOP_U2:
-      r_u2_dispatch<R>(x, o, adj);
-      break;
-    case TOP_CX: TQ_CASE_AB(r_perm, R, 0) break;
-    case TOP_SWAP: TQ_CASE_AB(r_perm, R, 1) break;
-    case TOP_CZ: TQ_CASE_AB(r_perm, R, 2) break;
+    case TOP_U2: q.code = RC_U2; break;
+    case TOP_CX: q.code = a != b ? RC_CX + pair_index(a, b) : RC_NOP; break;
+    case TOP_SWAP: q.code = a != b ? RC_SWAP + pair_index(a, b) : RC_NOP; break;
+    case TOP_CZ: q.code = a != b ? RC_CZ + pair_index(a, b) : RC_NOP; break;
     case TOP_PROT: {
       cplx<R> c, w;
       prot_coeffs<R>(o, theta, c, w);
-      // zs: sign of the Z factors outside the stage (zsign); adjoint flips the sin term
-      const R ws = adj ? -zs : zs;
-      w = cplx<R>(ws * w.x, ws * w.y);
-      const uint32_t zm = o.zm, cm = o.cm;
-      switch (o.xm & 15) {
-        case 0: r_prot<R, 0>(x, zm, cm, c, w); break;
-        case 1: r_prot<R, 1>(x, zm, cm, c, w); break;
-        case 2: r_prot<R, 2>(x, zm, cm, c, w); break;
-        case 3: r_prot<R, 3>(x, zm, cm, c, w); break;
-        case 4: r_prot<R, 4>(x, zm, cm, c, w); break;
-        case 5: r_prot<R, 5>(x, zm, cm, c, w); break;
-        case 6: r_prot<R, 6>(x, zm, cm, c, w); break;
-        case 7: r_prot<R, 7>(x, zm, cm, c, w); break;
-        case 8: r_prot<R, 8>(x, zm, cm, c, w); break;
-        case 9: r_prot<R, 9>(x, zm, cm, c, w); break;
-        case 10: r_prot<R, 10>(x, zm, cm, c, w); break;
-        case 11: r_prot<R, 11>(x, zm, cm, c, w); break;
-        case 12: r_prot<R, 12>(x, zm, cm, c, w); break;
-        case 13: r_prot<R, 13>(x, zm, cm, c, w); break;
-        case 14: r_prot<R, 14>(x, zm, cm, c, w); break;
-        default: r_prot<R, 15>(x, zm, cm, c, w); break;
+      if (adj) w = cplx<R>(-w.x, -w.y);  // exp(+i t/2 P): the sin term flips sign
+      const uint32_t xm = o.xm & 15, zm = o.zm & 15, cm = o.cm & 15;
+      if (cm == 0 && one_bit(xm) && (zm & ~xm) == 0) {
+        // pair (i, j = i | bit K): x_i' = c x_i + w (-1)^{zK} x_j, x_j' = w x_i + c x_j
+        const int K = __ffs(xm) - 1;
+        const cplx<R> w01 = (zm & xm) ? cplx<R>(-w.x, -w.y) : w;
+        q.m[0] = c;
+        q.m[1] = w01;
+        q.m[2] = w;
+        q.m[3] = c;
+        if (c.y == R(0) && w.y == R(0))
+          q.code = RC_RR + K;
+        else if (c.y == R(0) && w.x == R(0))
+          q.code = RC_RI + K;
+        else
+          q.code = RC_U1 + K;
+      } else if (cm == 0 && xm == 0 && one_bit(zm)) {
+        // diag(c + w, c - w) on bit K
+        q.code = RC_D + (__ffs(zm) - 1);
+        q.m[0] = cplx<R>(c.x + w.x, c.y + w.y);
+        q.m[1] = cplx<R>(c.x - w.x, c.y - w.y);
+      } else {
+        q.code = RC_PROT;
+        q.m[0] = c;
+        q.m[1] = w;
       }
+      break;
+    }
+    default: break;
+  }
+  if (grad && o.slot >= 0) {
+    const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
+    q.gph = cplx<R>(re[o.gny & 3], im[o.gny & 3]);
+    const uint32_t gx = o.gxm, gz = o.gzm, gc = o.gcm;
+    if (gc == 0 && one_bit(gx) && gx < 16 && (gz & ~gx) == 0) {
+      q.gcode = RG_PAIR + (__ffs(gx) - 1);
+      q.gw0 = (gz & gx) ? R(-1) : R(1);
+    } else if (gx == 0 && gc == 0 && one_bit(gz) && gz < 16) {
+      q.gcode = RG_DIAG + (__ffs(gz) - 1);
+      q.gw0 = R(1);
+      q.gw1 = R(-1);
+    } else if (gx == 0 && gz == 0 && one_bit(gc) && gc < 16) {
+      q.gcode = RG_DIAG + (__ffs(gc) - 1);
+      q.gw0 = R(0);
+      q.gw1 = R(1);
+    } else {
+      q.gcode = RG_GEN;
+    }
+  }
+  r = q;
+}
+
+// Compile ops [k0, k1) into rops[0 .. k1-k0) (all threads of the CTA).
+template <typename R>
+__device__ __forceinline__ void rops_build(ROp<R>* rops, const tq_tile_op* __restrict__ ops, int k0, int k1,
+                                           const double* theta, bool adj, bool grad) {
+  for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x) rop_build<R>(rops[k - k0], ops[k], k, theta, adj, grad);
+}
+
+// Sign of the op's Z factors outside the registers: tile base gbase, thread base tbase.
+template <typename R>
+__device__ __forceinline__ R rop_sign(const ROp<R>& r, uint64_t gbase, int tbase) {
+  const int par = (__popcll(gbase & r.zg) + __popc((unsigned)tbase & r.zo)) & 1;
+  return par ? R(-1) : R(1);
+}
+
+#define TQ_RK_CASES(BASE, FN, ...)                          \
+  case BASE + 0: FN<R, 0>(x, __VA_ARGS__); if (NA == 2) FN<R, 0>(y, __VA_ARGS__); break; \
+  case BASE + 1: FN<R, 1>(x, __VA_ARGS__); if (NA == 2) FN<R, 1>(y, __VA_ARGS__); break; \
+  case BASE + 2: FN<R, 2>(x, __VA_ARGS__); if (NA == 2) FN<R, 2>(y, __VA_ARGS__); break; \
+  case BASE + 3: FN<R, 3>(x, __VA_ARGS__); if (NA == 2) FN<R, 3>(y, __VA_ARGS__); break;
+
+#define TQ_PAIR_CASE(BASE, I, MODE, A, B) \
+  case BASE + I: r_perm<R, MODE, A, B>(x); if (NA == 2) r_perm<R, MODE, A, B>(y); break;
+#define TQ_PAIR_CASES(BASE, MODE)                                                                      \
+  TQ_PAIR_CASE(BASE, 0, MODE, 0, 1) TQ_PAIR_CASE(BASE, 1, MODE, 0, 2) TQ_PAIR_CASE(BASE, 2, MODE, 0, 3)  \
+  TQ_PAIR_CASE(BASE, 3, MODE, 1, 0) TQ_PAIR_CASE(BASE, 4, MODE, 1, 2) TQ_PAIR_CASE(BASE, 5, MODE, 1, 3)  \
+  TQ_PAIR_CASE(BASE, 6, MODE, 2, 0) TQ_PAIR_CASE(BASE, 7, MODE, 2, 1) TQ_PAIR_CASE(BASE, 8, MODE, 2, 3)  \
+  TQ_PAIR_CASE(BASE, 9, MODE, 3, 0) TQ_PAIR_CASE(BASE, 10, MODE, 3, 1) TQ_PAIR_CASE(BASE, 11, MODE, 3, 2)
+
+// Apply compiled op r to x (and to y when NA == 2) with sign s.
+template <typename R, int NA>
+__device__ __forceinline__ void rop_apply(cplx<R>* x, cplx<R>* y, const ROp<R>& r,
+                                          const tq_tile_op* __restrict__ ops, bool adj, R s) {
+  switch (r.code) {
+    TQ_RK_CASES(RC_U1, r_u1, r.m[0], cplx<R>(s * r.m[1].x, s * r.m[1].y), cplx<R>(s * r.m[2].x, s * r.m[2].y),
+                r.m[3])
+    TQ_RK_CASES(RC_RR, r_rr, r.m[0].x, s * r.m[1].x, s * r.m[2].x)
+    TQ_RK_CASES(RC_RI, r_ri, r.m[0].x, s * r.m[1].y, s * r.m[2].y)
+    TQ_RK_CASES(RC_D, r_d1, s < R(0) ? r.m[1] : r.m[0], s < R(0) ? r.m[0] : r.m[1])
+    TQ_RK_CASES(RC_DH, r_dh, r.m[1])
+    TQ_PAIR_CASES(RC_CX, 0)
+    TQ_PAIR_CASES(RC_SWAP, 1)
+    TQ_PAIR_CASES(RC_CZ, 2)
+    case RC_U2: {
+      const tq_tile_op& o = ops[r.op];
+      r_u2_dispatch<R>(x, o, adj);
+      if (NA == 2) r_u2_dispatch<R>(y, o, adj);
+      break;
+    }
+    case RC_PROT: {
+      const tq_tile_op& o = ops[r.op];
+      const cplx<R> w(s * r.m[1].x, s * r.m[1].y);
+      r_prot_dispatch<R>(x, o.xm, o.zm, o.cm, r.m[0], w);
+      if (NA == 2) r_prot_dispatch<R>(y, o.xm, o.zm, o.cm, r.m[0], w);
       break;
     }
     default: break;
   }
 }
 
+// Gradient partial Im <y|G|x> of compiled op r (unsigned; the caller applies the op's sign).
+template <typename R>
+__device__ __forceinline__ R rop_grad(const cplx<R>* x, const cplx<R>* y, const ROp<R>& r,
+                                      const tq_tile_op* __restrict__ ops) {
+  switch (r.gcode) {
+    case RG_PAIR + 0: return g_pair<R, 0>(x, y, r.gph, r.gw0);
+    case RG_PAIR + 1: return g_pair<R, 1>(x, y, r.gph, r.gw0);
+    case RG_PAIR + 2: return g_pair<R, 2>(x, y, r.gph, r.gw0);
+    case RG_PAIR + 3: return g_pair<R, 3>(x, y, r.gph, r.gw0);
+    case RG_DIAG + 0: return g_diag<R, 0>(x, y, r.gph, r.gw0, r.gw1);
+    case RG_DIAG + 1: return g_diag<R, 1>(x, y, r.gph, r.gw0, r.gw1);
+    case RG_DIAG + 2: return g_diag<R, 2>(x, y, r.gph, r.gw0, r.gw1);
+    case RG_DIAG + 3: return g_diag<R, 3>(x, y, r.gph, r.gw0, r.gw1);
+    default: return r_grad_dispatch<R>(x, y, ops[r.op]);
+  }
+}
+
+// ------------------------------------------------------------------ stage mapping
 // Per-thread register <-> padded shared-memory index of register i for a stage
 // with register bits b[0..3] (ascending local positions).
 struct StageMap {
@@ -257,21 +516,228 @@ __device__ __forceinline__ StageMap stage_map(const tq_tile_stage& st, int tid) 
   return m;
 }
 
-// Run stages[s0..s1) on the padded tile s (2^(t-4) threads).
+// ------------------------------------------------------------------ out-of-place forms
+// The forward path alternates between two register arrays: every op reads
+// array a and writes all 16 amplitudes of array b.  No value has to be moved
+// back into its input register after a dispatch, which an in-place update of
+// a register pair cannot avoid.
+template <typename R, int K>
+__device__ __forceinline__ void t_u1(const cplx<R>* a, cplx<R>* b, cplx<R> u0, cplx<R> u1, cplx<R> u2, cplx<R> u3) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i >> K) & 1) continue;
+    const int j = i | (1 << K);
+    b[i] = cfma(u1, a[j], cmul(u0, a[i]));
+    b[j] = cfma(u3, a[j], cmul(u2, a[i]));
+  }
+}
+
+template <typename R, int K>
+__device__ __forceinline__ void t_rr(const cplx<R>* a, cplx<R>* b, R c, R a01, R a10) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i >> K) & 1) continue;
+    const int j = i | (1 << K);
+    b[i] = cplx<R>(fma(a01, a[j].x, c * a[i].x), fma(a01, a[j].y, c * a[i].y));
+    b[j] = cplx<R>(fma(a10, a[i].x, c * a[j].x), fma(a10, a[i].y, c * a[j].y));
+  }
+}
+
+template <typename R, int K>
+__device__ __forceinline__ void t_ri(const cplx<R>* a, cplx<R>* b, R c, R b01, R b10) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if ((i >> K) & 1) continue;
+    const int j = i | (1 << K);
+    b[i] = cplx<R>(fma(-b01, a[j].y, c * a[i].x), fma(b01, a[j].x, c * a[i].y));
+    b[j] = cplx<R>(fma(-b10, a[i].y, c * a[j].x), fma(b10, a[i].x, c * a[j].y));
+  }
+}
+
+template <typename R, int K>
+__device__ __forceinline__ void t_d1(const cplx<R>* a, cplx<R>* b, cplx<R> d0, cplx<R> d1) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) b[i] = cmul(((i >> K) & 1) ? d1 : d0, a[i]);
+}
+
+template <typename R, int K>
+__device__ __forceinline__ void t_dh(const cplx<R>* a, cplx<R>* b, cplx<R> d1) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) b[i] = ((i >> K) & 1) ? cmul(d1, a[i]) : a[i];
+}
+
+// MODE 0 CX (control A, target B), 1 SWAP, 2 CZ
+template <typename R, int MODE, int A, int B>
+__device__ __forceinline__ void t_perm(const cplx<R>* a, cplx<R>* b) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    const int ba = (i >> A) & 1, bb = (i >> B) & 1;
+    if (MODE == 0) {
+      b[i] = a[ba ? i ^ (1 << B) : i];
+    } else if (MODE == 1) {
+      b[i] = a[ba != bb ? i ^ (1 << A) ^ (1 << B) : i];
+    } else {
+      b[i] = (ba && bb) ? cplx<R>(-a[i].x, -a[i].y) : a[i];
+    }
+  }
+}
+
+template <typename R, int A, int B>
+__device__ __forceinline__ void t_u2(const cplx<R>* a, cplx<R>* b, const tq_tile_op& o) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if (((i >> A) & 1) || ((i >> B) & 1)) continue;
+    const int id[4] = {i, i | (1 << B), i | (1 << A), i | (1 << A) | (1 << B)};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      cplx<R> acc = cmul(op_m<R>(o, 4 * r), a[id[0]]);
+      acc = cfma(op_m<R>(o, 4 * r + 1), a[id[1]], acc);
+      acc = cfma(op_m<R>(o, 4 * r + 2), a[id[2]], acc);
+      acc = cfma(op_m<R>(o, 4 * r + 3), a[id[3]], acc);
+      b[id[r]] = acc;
+    }
+  }
+}
+
+template <typename R, int XM>
+__device__ __forceinline__ void t_prot(const cplx<R>* a, cplx<R>* b, uint32_t zm, uint32_t cm, cplx<R> c,
+                                       cplx<R> w) {
+  if (XM == 0) {
+#pragma unroll
+    for (int i = 0; i < kNR; ++i) {
+      const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
+      b[i] = ((i & cm) == cm) ? cmul(cplx<R>(c.x + sg * w.x, sg * w.y), a[i]) : a[i];
+    }
+  } else {
+    constexpr int H = (XM & 8) ? 3 : (XM & 4) ? 2 : (XM & 2) ? 1 : 0;
+#pragma unroll
+    for (int i = 0; i < kNR; ++i) {
+      if ((i >> H) & 1) continue;
+      const int j = i ^ XM;
+      const bool on = (i & cm) == cm;
+      const R si = (__popc(i & zm) & 1) ? R(-1) : R(1);
+      const R sj = (__popc(j & zm) & 1) ? R(-1) : R(1);
+      const cplx<R> ni = cfma(cplx<R>(w.x * sj, w.y * sj), a[j], cplx<R>(c.x * a[i].x, c.x * a[i].y));
+      const cplx<R> nj = cfma(cplx<R>(w.x * si, w.y * si), a[i], cplx<R>(c.x * a[j].x, c.x * a[j].y));
+      b[i] = on ? ni : a[i];
+      b[j] = on ? nj : a[j];
+    }
+  }
+}
+
+#define TQ_TK_CASES(BASE, FN, ...)                       \
+  case BASE + 0: FN<R, 0>(a, b, __VA_ARGS__); break;     \
+  case BASE + 1: FN<R, 1>(a, b, __VA_ARGS__); break;     \
+  case BASE + 2: FN<R, 2>(a, b, __VA_ARGS__); break;     \
+  case BASE + 3: FN<R, 3>(a, b, __VA_ARGS__); break;
+#define TQ_TPAIR_CASE(BASE, I, MODE, A, B) case BASE + I: t_perm<R, MODE, A, B>(a, b); break;
+#define TQ_TPAIR_CASES(BASE, MODE)                                                                         \
+  TQ_TPAIR_CASE(BASE, 0, MODE, 0, 1) TQ_TPAIR_CASE(BASE, 1, MODE, 0, 2) TQ_TPAIR_CASE(BASE, 2, MODE, 0, 3)  \
+  TQ_TPAIR_CASE(BASE, 3, MODE, 1, 0) TQ_TPAIR_CASE(BASE, 4, MODE, 1, 2) TQ_TPAIR_CASE(BASE, 5, MODE, 1, 3)  \
+  TQ_TPAIR_CASE(BASE, 6, MODE, 2, 0) TQ_TPAIR_CASE(BASE, 7, MODE, 2, 1) TQ_TPAIR_CASE(BASE, 8, MODE, 2, 3)  \
+  TQ_TPAIR_CASE(BASE, 9, MODE, 3, 0) TQ_TPAIR_CASE(BASE, 10, MODE, 3, 1) TQ_TPAIR_CASE(BASE, 11, MODE, 3, 2)
+
+// b = (compiled forward op r) a, with sign s.
 template <typename R>
-__device__ __forceinline__ void run_stages(cplx<R>* s, const tq_tile_stage* __restrict__ stages, int s0, int s1,
-                                           const tq_tile_op* __restrict__ ops, const double* theta, bool adj,
+__device__ __forceinline__ void rop_apply_to(const cplx<R>* a, cplx<R>* b, const ROp<R>& r,
+                                             const tq_tile_op* __restrict__ ops, R s) {
+  switch (r.code) {
+    TQ_TK_CASES(RC_U1, t_u1, r.m[0], cplx<R>(s * r.m[1].x, s * r.m[1].y), cplx<R>(s * r.m[2].x, s * r.m[2].y),
+                r.m[3])
+    TQ_TK_CASES(RC_RR, t_rr, r.m[0].x, s * r.m[1].x, s * r.m[2].x)
+    TQ_TK_CASES(RC_RI, t_ri, r.m[0].x, s * r.m[1].y, s * r.m[2].y)
+    TQ_TK_CASES(RC_D, t_d1, s < R(0) ? r.m[1] : r.m[0], s < R(0) ? r.m[0] : r.m[1])
+    TQ_TK_CASES(RC_DH, t_dh, r.m[1])
+    TQ_TPAIR_CASES(RC_CX, 0)
+    TQ_TPAIR_CASES(RC_SWAP, 1)
+    TQ_TPAIR_CASES(RC_CZ, 2)
+    case RC_U2: {
+      const tq_tile_op& o = ops[r.op];
+      switch (o.a * 4 + o.b) {
+        case 1: t_u2<R, 0, 1>(a, b, o); break;
+        case 2: t_u2<R, 0, 2>(a, b, o); break;
+        case 3: t_u2<R, 0, 3>(a, b, o); break;
+        case 4: t_u2<R, 1, 0>(a, b, o); break;
+        case 6: t_u2<R, 1, 2>(a, b, o); break;
+        case 7: t_u2<R, 1, 3>(a, b, o); break;
+        case 8: t_u2<R, 2, 0>(a, b, o); break;
+        case 9: t_u2<R, 2, 1>(a, b, o); break;
+        case 11: t_u2<R, 2, 3>(a, b, o); break;
+        case 12: t_u2<R, 3, 0>(a, b, o); break;
+        case 13: t_u2<R, 3, 1>(a, b, o); break;
+        case 14: t_u2<R, 3, 2>(a, b, o); break;
+        default:
+#pragma unroll
+          for (int i = 0; i < kNR; ++i) b[i] = a[i];
+          break;
+      }
+      break;
+    }
+    case RC_PROT: {
+      const tq_tile_op& o = ops[r.op];
+      const cplx<R> w(s * r.m[1].x, s * r.m[1].y), c = r.m[0];
+      const uint32_t zm = o.zm, cm = o.cm;
+      switch (o.xm & 15) {
+        case 0: t_prot<R, 0>(a, b, zm, cm, c, w); break;
+        case 1: t_prot<R, 1>(a, b, zm, cm, c, w); break;
+        case 2: t_prot<R, 2>(a, b, zm, cm, c, w); break;
+        case 3: t_prot<R, 3>(a, b, zm, cm, c, w); break;
+        case 4: t_prot<R, 4>(a, b, zm, cm, c, w); break;
+        case 5: t_prot<R, 5>(a, b, zm, cm, c, w); break;
+        case 6: t_prot<R, 6>(a, b, zm, cm, c, w); break;
+        case 7: t_prot<R, 7>(a, b, zm, cm, c, w); break;
+        case 8: t_prot<R, 8>(a, b, zm, cm, c, w); break;
+        case 9: t_prot<R, 9>(a, b, zm, cm, c, w); break;
+        case 10: t_prot<R, 10>(a, b, zm, cm, c, w); break;
+        case 11: t_prot<R, 11>(a, b, zm, cm, c, w); break;
+        case 12: t_prot<R, 12>(a, b, zm, cm, c, w); break;
+        case 13: t_prot<R, 13>(a, b, zm, cm, c, w); break;
+        case 14: t_prot<R, 14>(a, b, zm, cm, c, w); break;
+        default: t_prot<R, 15>(a, b, zm, cm, c, w); break;
+      }
+      break;
+    }
+    default:
+#pragma unroll
+      for (int i = 0; i < kNR; ++i) b[i] = a[i];
+      break;
+  }
+}
+
+// Run stages[s0..s1) forward on the padded tile s (2^(t-4) threads).
+// rops: the pass's compiled ops when `resident` (rops[k - op0] is op k),
+// else room for kRopCap ops compiled chunk by chunk.  The caller
+// synchronises before the first stage.
+template <typename R>
+__device__ __forceinline__ void run_stages(cplx<R>* s, ROp<R>* rops, bool resident, int op0,
+                                           const tq_tile_stage* __restrict__ stages, int s0, int s1,
+                                           const tq_tile_op* __restrict__ ops, const double* theta,
                                            uint64_t gbase) {
-  const int tid = threadIdx.x;
   for (int si = s0; si < s1; ++si) {
     const tq_tile_stage st = stages[si];
-    const StageMap m = stage_map(st, tid);
-    cplx<R> x[kNR];
+    const StageMap m = stage_map(st, threadIdx.x);
+    cplx<R> x[kNR], x2[kNR];
 #pragma unroll
     for (int i = 0; i < kNR; ++i) x[i] = s[pphys(m.idx(i))];
-    for (int k = st.op_begin; k < st.op_end; ++k) {
-      const tq_tile_op& o = ops[k];
-      r_apply<R>(x, o, theta, adj, zsign<R>(o, gbase, m.base));
+    const int step = resident ? (st.op_end - st.op_begin) : kRopCap;
+    for (int k0 = st.op_begin; k0 < st.op_end; k0 += step) {
+      const int k1 = min(k0 + step, st.op_end);
+      const ROp<R>* rr = rops - (resident ? op0 : k0);
+      if (!resident) {
+        if (k0 != st.op_begin) __syncthreads();  // readers of the previous chunk are done
+        rops_build<R>(rops, ops, k0, k1, theta, false, false);
+        __syncthreads();
+      }
+      int k = k0;
+      for (; k + 1 < k1; k += 2) {
+        rop_apply_to<R>(x, x2, rr[k], ops, rop_sign<R>(rr[k], gbase, m.base));
+        rop_apply_to<R>(x2, x, rr[k + 1], ops, rop_sign<R>(rr[k + 1], gbase, m.base));
+      }
+      if (k < k1) {
+        rop_apply_to<R>(x, x2, rr[k], ops, rop_sign<R>(rr[k], gbase, m.base));
+#pragma unroll
+        for (int i = 0; i < kNR; ++i) x[i] = x2[i];
+      }
     }
 #pragma unroll
     for (int i = 0; i < kNR; ++i) s[pphys(m.idx(i))] = x[i];

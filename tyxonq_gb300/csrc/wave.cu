@@ -43,6 +43,11 @@ __device__ __forceinline__ void w_hoff(int64_t* hoff, const WPass& P) {
   }
 }
 
+// Passes of a wave keep at least kWaveMinNlow contiguous low bits, so the
+// offset table has at most 2^(t - kWaveMinNlow) entries.
+constexpr int kWaveMinNlow = 4;
+__host__ __device__ __forceinline__ size_t w_hoff_bytes(int t) { return sizeof(int64_t) << (t - kWaveMinNlow); }
+
 __device__ __forceinline__ int64_t w_base(int64_t g, const WPass& P) {
   int64_t x = g << P.nlow;
   for (int k = P.nlow; k < P.t; ++k) x = insert_zero(x, P.pos[k]);
@@ -79,21 +84,23 @@ __device__ __forceinline__ void w_store(const cplx<R>* s, typename C2<R>::T* g, 
 }
 
 // ------------------------------------------------------------------ forward
+// Shared memory: padded tile | offset table (8 << (t - kWaveMinNlow) bytes) | compiled ops.
 template <typename R>
-__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_forward(const tq_wave_item* __restrict__ items, int n_items,
-                                                      const tq_tile_pass* __restrict__ passes,
-                                                      const tq_tile_stage* __restrict__ stages,
-                                                      const tq_tile_op* __restrict__ ops,
-                                                      const double* __restrict__ theta, void* pool) {
+__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
+    k_wave_forward(const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes,
+                   const tq_tile_stage* __restrict__ stages, const tq_tile_op* __restrict__ ops,
+                   const double* __restrict__ theta, void* pool) {
   extern __shared__ __align__(16) unsigned char smem[];
   typedef typename C2<R>::T T2;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
     const WPass P = wload_pass(&passes[I.pass]);
+    if (P.nlow < kWaveMinNlow) continue;  // the offset table would not fit (the host never plans such passes)
     cplx<R>* s = reinterpret_cast<cplx<R>*>(smem);
     int64_t* hoff = reinterpret_cast<int64_t*>(smem + padded_len(P.t) * sizeof(cplx<R>));
+    ROp<R>* rops = reinterpret_cast<ROp<R>*>(smem + padded_len(P.t) * sizeof(cplx<R>) + w_hoff_bytes(P.t));
     T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
-    __syncthreads();  // previous item's readers of s / hoff are done
+    __syncthreads();  // previous item's readers of s / hoff / rops are done
     w_hoff(hoff, P);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
@@ -110,7 +117,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_forward(con
       w_commit_wait();
     }
     __syncthreads();
-    run_stages<R>(s, stages, P.op_begin, P.op_end, ops, theta + I.theta_off, false, (uint64_t)base);
+    run_stages<R>(s, rops, false, 0, stages, P.op_begin, P.op_end, ops, theta + I.theta_off, (uint64_t)base);
     w_store<R>(s, psi, base, hoff, P);
   }
 }
@@ -194,54 +201,13 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
 }
 
 // ------------------------------------------------------------------ adjoint
-// Im <lam|G|psi> over the 16 register amplitudes: G|i> = [i & cm == cm] ph
-// (-1)^{popc(i & zm)} |i ^ XM>  (register-bit masks).
-template <typename R, int XM>
-__device__ __forceinline__ R r_grad(const cplx<R>* x, const cplx<R>* y, uint32_t zm, uint32_t cm, cplx<R> ph) {
-  R acc = 0;
-#pragma unroll
-  for (int i = 0; i < kNR; ++i) {
-    if ((i & cm) != cm) continue;
-    const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
-    const cplx<R> v = cmul(ph, x[i]);
-    const cplx<R> l = y[i ^ XM];
-    acc += sg * (l.x * v.y - l.y * v.x);
-  }
-  return acc;
-}
-
+// Shared memory: psi tile | lam tile | offset table | compiled ops | per-warp
+// gradient partials (max_ops x warps doubles).
 template <typename R>
-__device__ __forceinline__ R r_grad_dispatch(const cplx<R>* x, const cplx<R>* y, const tq_tile_op& o) {
-  const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
-  const cplx<R> ph(re[o.gny & 3], im[o.gny & 3]);
-  const uint32_t zm = o.gzm, cm = o.gcm;
-  switch (o.gxm & 15) {
-    case 0: return r_grad<R, 0>(x, y, zm, cm, ph);
-    case 1: return r_grad<R, 1>(x, y, zm, cm, ph);
-    case 2: return r_grad<R, 2>(x, y, zm, cm, ph);
-    case 3: return r_grad<R, 3>(x, y, zm, cm, ph);
-    case 4: return r_grad<R, 4>(x, y, zm, cm, ph);
-    case 5: return r_grad<R, 5>(x, y, zm, cm, ph);
-    case 6: return r_grad<R, 6>(x, y, zm, cm, ph);
-    case 7: return r_grad<R, 7>(x, y, zm, cm, ph);
-    case 8: return r_grad<R, 8>(x, y, zm, cm, ph);
-    case 9: return r_grad<R, 9>(x, y, zm, cm, ph);
-    case 10: return r_grad<R, 10>(x, y, zm, cm, ph);
-    case 11: return r_grad<R, 11>(x, y, zm, cm, ph);
-    case 12: return r_grad<R, 12>(x, y, zm, cm, ph);
-    case 13: return r_grad<R, 13>(x, y, zm, cm, ph);
-    case 14: return r_grad<R, 14>(x, y, zm, cm, ph);
-    default: return r_grad<R, 15>(x, y, zm, cm, ph);
-  }
-}
-
-template <typename R>
-__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_adjoint(const tq_wave_item* __restrict__ items, int n_items,
-                                                      const tq_tile_pass* __restrict__ passes,
-                                                      const tq_tile_stage* __restrict__ stages,
-                                                      const tq_tile_op* __restrict__ ops,
-                                                      const double* __restrict__ theta, void* pool,
-                                                      double* partials, int max_ops) {
+__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
+    k_wave_adjoint(const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes,
+                   const tq_tile_stage* __restrict__ stages, const tq_tile_op* __restrict__ ops,
+                   const double* __restrict__ theta, void* pool, double* partials, int max_ops) {
   extern __shared__ __align__(16) unsigned char smem[];
   typedef typename C2<R>::T T2;
   const int nwarps = blockDim.x >> 5;
@@ -249,16 +215,20 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_adjoint(con
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
     const WPass P = wload_pass(&passes[I.pass]);
+    const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
+    const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
+    // tables that would not fit the shared memory sized by the host (never planned)
+    if (P.nlow < kWaveMinNlow || nops > max_ops) continue;
     const int PT = padded_len(P.t);
     cplx<R>* sp = reinterpret_cast<cplx<R>*>(smem);
     cplx<R>* sl = sp + PT;
-    int64_t* hoff = reinterpret_cast<int64_t*>(smem + 2 * PT * sizeof(cplx<R>));
-    double* wpart = reinterpret_cast<double*>(smem + 2 * PT * sizeof(cplx<R>) + (sizeof(int64_t) << (P.t - P.nlow)));
+    unsigned char* tail = smem + 2 * PT * sizeof(cplx<R>);
+    int64_t* hoff = reinterpret_cast<int64_t*>(tail);
+    ROp<R>* rops = reinterpret_cast<ROp<R>*>(tail + w_hoff_bytes(P.t));
+    double* wpart = reinterpret_cast<double*>(tail + w_hoff_bytes(P.t) + kRopCap * sizeof(ROp<R>));
     T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
     T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
     const double* th = theta + I.theta_off;
-    const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
-    const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
     __syncthreads();
     w_hoff(hoff, P);
     for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = 0.0;
@@ -278,17 +248,22 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_adjoint(con
         x[i] = sp[j];
         y[i] = sl[j];
       }
-      for (int k = st.op_begin; k < st.op_end; ++k) {
-        const tq_tile_op& o = ops[k];
-        const R zs = zsign<R>(o, (uint64_t)base, mp.base);
-        if (o.slot >= 0) {
-          R part = zs * r_grad_dispatch<R>(x, y, o);
+      for (int k0 = st.op_begin; k0 < st.op_end; k0 += kRopCap) {
+        const int k1 = min(k0 + kRopCap, st.op_end);
+        if (k0 != st.op_begin) __syncthreads();  // readers of the previous chunk are done
+        rops_build<R>(rops, ops, k0, k1, th, true, true);
+        __syncthreads();
+        for (int k = k0; k < k1; ++k) {
+          const ROp<R>& r = rops[k - k0];
+          const R zs = rop_sign<R>(r, (uint64_t)base, mp.base);
+          if (r.gcode != RG_NONE) {
+            R part = zs * rop_grad<R>(x, y, r, ops);
 #pragma unroll
-          for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
-          if (lane == 0) wpart[(k - op0) * nwarps + warp] = (double)part;
+            for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
+            if (lane == 0) wpart[(k - op0) * nwarps + warp] = (double)part;
+          }
+          rop_apply<R, 2>(x, y, r, ops, true, zs);
         }
-        r_apply<R>(x, o, th, true, zs);
-        r_apply<R>(y, o, th, true, zs);
       }
 #pragma unroll
       for (int i = 0; i < kNR; ++i) {
@@ -306,7 +281,6 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256) k_wave_adjoint(con
       partials[I.part_off + k] = s;
     }
   }
-  (void)max_ops;
 }
 
 __global__ void k_wave_reduce(const double* __restrict__ partials, const int32_t* __restrict__ first,
@@ -327,11 +301,11 @@ __global__ void k_wave_reduce(const double* __restrict__ partials, const int32_t
 
 template <typename R>
 static size_t fwd_smem(int t) {
-  return padded_len(t) * sizeof(cplx<R>) + (sizeof(int64_t) << (t - 1));
+  return padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + kRopCap * sizeof(ROp<R>);
 }
 template <typename R>
 static size_t adj_smem(int t, int max_ops) {
-  return 2 * padded_len(t) * sizeof(cplx<R>) + (sizeof(int64_t) << (t - 1)) +
+  return 2 * padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + kRopCap * sizeof(ROp<R>) +
          sizeof(double) * (size_t)max_ops * ((1 << (t - kRB)) / 32);
 }
 

@@ -33,6 +33,9 @@ WAVE_ITEM_DTYPE = np.dtype({
     "offsets": [0, 8, 16, 20, 24, 28, 32, 36, 40, 44],
     "itemsize": 48,
 })
+# passes of a wave keep at least this many contiguous low bits (the kernels'
+# offset table holds 2^(t - WAVE_MIN_NLOW) entries)
+WAVE_MIN_NLOW = 4
 PASS_DTYPE = np.dtype({"names": ["t", "nlow", "op_begin", "op_end", "pos"],
                        "formats": ["<i4", "<i4", "<i4", "<i4", ("<i4", 16)], "itemsize": 80})
 
@@ -54,6 +57,7 @@ class WavePlan:
         self.max_ops = max_ops
         S = 8 if dtype == torch.complex64 else 16
         self.passes, self.stages, self.ops = [], [], []
+        self.adj_max_ops = 1
         self._np = self._ns = self._no = 0
         cache = {}
         for e in entries:
@@ -206,6 +210,11 @@ class WavePlan:
                 pslots = [(k, int(ops[k]["slot"]), float(ops[k]["gcoef"])) for k in range(len(ops))
                           if ops[k]["slot"] >= 0]
                 adj.append((pid, len(ops), pslots))
+                self.adj_max_ops = max(self.adj_max_ops, len(ops))
+        for pid in fwd + [a[0] for a in adj]:
+            if self.passes[pid][1] < WAVE_MIN_NLOW:
+                raise NotImplementedError(f"wave pass keeps {self.passes[pid][1]} contiguous low bits "
+                                          f"(at least {WAVE_MIN_NLOW} needed)")
         return {"fwd": fwd, "adj": adj}
 
     # ------------------------------------------------------------ execution
@@ -220,8 +229,8 @@ class WavePlan:
                 nat.call("tq_wave_run", kind, self.dt, P(self.items_dev.data_ptr() + isz * b), c, self.t,
                          self.hbits, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
                          P(self.ops_dev.data_ptr()), P(groups_dev.data_ptr()), P(terms_dev.data_ptr()),
-                         P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()), self.max_ops,
-                         stream)
+                         P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()),
+                         self.adj_max_ops, stream)
             else:
                 kind, b, c = L
                 out = energies if kind == "reduce_e" else grads
