@@ -23,6 +23,10 @@ if str(ROOT) not in sys.path:
 
 METRIC = "VQE energy+grad evals/s batched vs plain GPU; p50/p99 latency; gate HBM GB/s"
 
+# DRAM bytes read + written by one k_staged_forward launch of the 28-qubit pass,
+# from the ncu capture summarised in profiles/k_staged_forward_28q_c64.txt
+STAGED_PASS_DRAM_BYTES = 4.2455e9
+
 
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
@@ -215,8 +219,59 @@ def bench_gate_kernels(args, dev):
     avg_launch = sum(launch_ms) / len(launch_ms)
     return {"fused_ms": sum(step_ms) / len(step_ms), "plain_ms": plain_ms, "passes": prog.n_passes,
             "gates": len(gates), "avg_pass_ms": avg_launch, "pass_alg_bytes": 2 * N * S,
-            "pass_gbs": 2 * N * S / (avg_launch * 1e-3) / 1e9,
-            "plain_gbs_equiv": len(gates) * 2 * N * S / (plain_ms * 1e-3) / 1e9}
+            "pass_gbs": 2 * N * S / (avg_launch * 1e-3) / 1e9, "single_gate": bench_single_gates(n2)}
+
+
+def bench_single_gates(n: int, reps: int = 4) -> dict:
+    """One launch per gate on an n-qubit complex64 state (2 GiB at 28 qubits, far
+    above L2): device time per launch and GB/s over the algorithmic bytes of the
+    gate (amplitudes it can change, read and written once)."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from tyxonq_gb300 import _native as nat
+    from tyxonq_gb300 import kernels as K
+
+    N, S = 1 << n, 8
+    psi = K.init_statevector(n, dtype=torch.complex64)
+    P = ctypes.c_void_p(psi.data_ptr())
+    st = K.stream_ptr()
+    h = np.array([[1, 1], [1, -1]]) / np.sqrt(2)
+    u2 = np.linalg.qr(np.random.default_rng(5).normal(size=(4, 4)) + 1j)[0]
+    qs = [0, n // 4, n // 2, 3 * n // 4, n - 1]
+    d_rz = (ctypes.c_double * 4)(np.cos(0.3), -np.sin(0.3), np.cos(0.3), np.sin(0.3))
+    d_ph = (ctypes.c_double * 4)(1.0, 0.0, np.cos(0.7), np.sin(0.7))
+    mh, m2 = K._mat(h, 2), K._mat(u2, 4)
+    kinds = {
+        "dense_1q": (2 * N * S, lambda q, r: nat.call("tq_sv_apply_1q", P, n, 0, q, mh, st)),
+        "diag_1q": (2 * N * S, lambda q, r: nat.call("tq_sv_apply_diag1", P, n, 0, q, d_rz, st)),
+        "phase_1q": (N * S, lambda q, r: nat.call("tq_sv_apply_diag1", P, n, 0, q, d_ph, st)),
+        "cx": (N * S, lambda q, r: nat.call("tq_sv_apply_cx", P, n, 0, q, r, st)),
+        "cz": (N * S // 2, lambda q, r: nat.call("tq_sv_apply_cz", P, n, 0, q, r, st)),
+        "dense_2q": (2 * N * S, lambda q, r: nat.call("tq_sv_apply_2q", P, n, 0, q, r, m2, st)),
+    }
+    out = {}
+    for name, (alg, fn) in kinds.items():
+        pairs = [(q, qs[(i + 2) % len(qs)]) for i, q in enumerate(qs)]
+        for q, r in pairs:  # warm-up
+            fn(q, r)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(reps):
+            for q, r in pairs:
+                a, b = _events()
+                a.record()
+                fn(q, r)
+                b.record()
+                torch.cuda.synchronize()
+                times.append(a.elapsed_time(b))
+        ms = sum(times) / len(times)
+        out[name] = {"ms": ms, "alg_bytes": alg, "gbs": alg / (ms * 1e-3) / 1e9, "launches": len(times)}
+    del psi
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_case(args):
@@ -358,6 +413,11 @@ def main():
     from tyxonq_gb300.serving import VqeServer, make_trace, replay
 
     serving = []
+    # warm-up trace (not reported): first use of every kernel and of the per-request streams
+    warm = make_trace(16, rate=80.0, seed=99, n_range=(10, 26), depth_range=(2, 10), terms_range=(20, 1000),
+                      grad_fraction=0.5, iterations=2)
+    replay(VqeServer(max_inflight=8), warm)
+    torch.cuda.empty_cache()
     for rate in (20.0, 80.0):
         trace = make_trace(48, rate=rate, seed=int(rate), n_range=(10, 26), depth_range=(2, 10),
                            terms_range=(20, 1000), grad_fraction=0.3, iterations=2)
@@ -384,7 +444,7 @@ def main():
         cpu = {"value": len(pick) / dt_cpu, "unit": "evals/s", "cores": 1, "kind": "port",
                "sample": f"{len(pick)} random instances with n<=14 of the 4096 (energy + adjoint gradient, c128)"}
 
-    launches_per_step = len(bv.launch_order)
+    launches_per_step = bv.kernel_launches()
     line = {
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -401,9 +461,10 @@ def main():
                     "workload": "Poisson arrivals, 24 sessions x 2 optimizer steps, HEA n~U{10..26} depth~U{2..10}, "
                                 "20-1000 Pauli terms, 30% energy+gradient, complex64"},
         "gate_kernels_28q": gk,
-        "roofline": {"kernel": "k_tile_forward (28-qubit complex64 tile pass, 2*N*8 B per launch)", "bound": "hbm",
+        "roofline": {"kernel": "k_staged_forward (28-qubit complex64 fused pass of the depth-40 random circuit, "
+                               "2*N*8 B per launch)", "bound": "hbm",
                      "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,
-                     "traffic": None, "peak_kind": peak_kind},
+                     "traffic": STAGED_PASS_DRAM_BYTES, "peak_kind": peak_kind},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches_per_step * args.steps,

@@ -217,7 +217,9 @@ typedef struct {
   double pscale;
   double gcoef;             /* dE/d(angle) = gcoef * Im <lam|G|psi> (batched kernel) */
   uint32_t zo;              /* kind 7 in register stages: Z factors on local bits outside the stage */
-  int32_t reserved;
+  int32_t fuse_next;        /* forward register stages: the next fuse_next ops act on the same single
+                               register bit a with no zo / zg sign (kinds 1, 2, 7) and are multiplied
+                               into this op on the device; 0 = none */
   uint64_t zg;              /* kind 7: Z factors on non-local (global) bits; with zo they contribute
                                one sign per tile / thread, so only X/Y qubits need to be local */
   float mf[32];             /* matrix, complex64 kernels: row-major (re, im) */

@@ -56,7 +56,7 @@ class _CTileOp(ctypes.Structure):
                 ("xm", ctypes.c_uint32), ("zm", ctypes.c_uint32), ("cm", ctypes.c_uint32), ("gxm", ctypes.c_uint32),
                 ("gzm", ctypes.c_uint32), ("gcm", ctypes.c_uint32), ("gny", ctypes.c_int32), ("pidx", ctypes.c_int32),
                 ("pscale", ctypes.c_double), ("gcoef", ctypes.c_double), ("zo", ctypes.c_uint32),
-                ("reserved", ctypes.c_int32), ("zg", ctypes.c_uint64), ("mf", ctypes.c_float * 32),
+                ("fuse_next", ctypes.c_int32), ("zg", ctypes.c_uint64), ("mf", ctypes.c_float * 32),
                 ("md", ctypes.c_double * 32)]
 
 

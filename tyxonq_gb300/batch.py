@@ -58,7 +58,7 @@ class Schedule:
     large: str = "waves"  # instances above res1_max: "waves" (L2-resident grid-wide phases) or "cta"
     wave_t: int = 12
     wave_hbits: int = 10
-    wave_budget: int = 48 << 20
+    wave_budget: int = 96 << 20
     wave_max_ops: int = 256
 
     @classmethod
@@ -325,6 +325,14 @@ class BatchedVQE:
                               ctypes.c_void_p(main.cuda_stream))
         if side is not main:
             main.wait_stream(side)
+
+    def kernel_launches(self) -> int:
+        """Kernel launches of one evaluation (persistent class kernels, wave passes,
+        wave reductions)."""
+        n = len(self.launch_order)
+        if self.waves is not None:
+            n += sum(1 for L in self.waves.launches if L[0] != "run" or L[3] > 0)
+        return n
 
     def capture(self) -> None:
         """Capture launch() into a CUDA graph (replayed by run())."""

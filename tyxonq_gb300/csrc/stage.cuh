@@ -299,6 +299,8 @@ struct __align__(16) ROp {
   int32_t op;     // index of the source op in the op table
   uint32_t zo;    // local bits outside the stage whose parity signs the op
   uint64_t zg;    // global bits outside the tile whose parity signs the op
+  int32_t skip;   // 1 + ops folded into this one (the next op to run is op + skip)
+  int32_t pad;
   cplx<R> m[4];
   cplx<R> gph;    // i^ny of the generator
   R gw0, gw1;
@@ -309,17 +311,72 @@ __device__ __forceinline__ int pair_index(int a, int b) { return a * 3 + (b < a 
 
 __device__ __forceinline__ bool one_bit(uint32_t m) { return m != 0 && (m & (m - 1)) == 0; }
 
-// Compile op o (table index k) into r.  adj: the record applies o^dagger;
-// grad: fill the gradient routine of an op with a slot.
+// Forward 2x2 matrix u (row-major) and register bit K of an op that acts on
+// one register bit with no sign from outside the stage; false otherwise.
 template <typename R>
-__device__ __forceinline__ void rop_build(ROp<R>& r, const tq_tile_op& o, int k, const double* theta, bool adj,
-                                          bool grad) {
+__device__ __forceinline__ bool op_mat2(const tq_tile_op& o, const double* theta, cplx<R>* u, int& K) {
+  if (o.zo != 0u || o.zg != 0ull) return false;
+  const cplx<R> z(R(0), R(0));
+  switch (o.kind) {
+    case TOP_U1:
+      K = o.a & 3;
+      for (int e = 0; e < 4; ++e) u[e] = op_m<R>(o, e);
+      return true;
+    case TOP_D1: {
+      K = o.a & 3;
+      cplx<R> d0 = op_m<R>(o, 0), d1 = op_m<R>(o, 1);
+      if (o.pidx >= 0 && theta != nullptr) {
+        R c, sn;
+        rot_cs(2.0 * o.pscale * theta[o.pidx], c, sn);
+        d0 = cplx<R>(R(1), R(0));
+        d1 = cplx<R>(c, sn);
+      }
+      u[0] = d0;
+      u[1] = u[2] = z;
+      u[3] = d1;
+      return true;
+    }
+    case TOP_PROT: {
+      const uint32_t xm = o.xm & 15, zm = o.zm & 15;
+      if ((o.cm & 15) != 0) return false;
+      cplx<R> c, w;
+      prot_coeffs<R>(o, theta, c, w);
+      if (one_bit(xm) && (zm & ~xm) == 0) {
+        K = __ffs(xm) - 1;
+        u[0] = u[3] = c;
+        u[1] = (zm & xm) ? cplx<R>(-w.x, -w.y) : w;
+        u[2] = w;
+        return true;
+      }
+      if (xm == 0 && one_bit(zm)) {
+        K = __ffs(zm) - 1;
+        u[0] = cplx<R>(c.x + w.x, c.y + w.y);
+        u[1] = u[2] = z;
+        u[3] = cplx<R>(c.x - w.x, c.y - w.y);
+        return true;
+      }
+      return false;
+    }
+    default: return false;
+  }
+}
+
+// Compile op k of the table into r.  adj: the record applies ops[k]^dagger;
+// grad: fill the gradient routine of an op with a slot.  Forward records of
+// an op with fuse_next = m > 0 multiply in the next m ops (same register bit)
+// and skip them.
+template <typename R>
+__device__ __forceinline__ void rop_build(ROp<R>& r, const tq_tile_op* __restrict__ ops, int k, const double* theta,
+                                          bool adj, bool grad) {
+  const tq_tile_op& o = ops[k];
   ROp<R> q;
   q.code = RC_NOP;
   q.gcode = RG_NONE;
   q.op = k;
   q.zo = o.zo;
   q.zg = o.zg;
+  q.skip = 1;
+  q.pad = 0;
   const cplx<R> z(R(0), R(0));
   q.m[0] = q.m[1] = q.m[2] = q.m[3] = z;
   q.gph = z;
@@ -396,6 +453,27 @@ __device__ __forceinline__ void rop_build(ROp<R>& r, const tq_tile_op& o, int k,
     }
     default: break;
   }
+  if (!adj && o.fuse_next > 0) {
+    cplx<R> u[4];
+    int K = -1;
+    if (op_mat2<R>(o, theta, u, K)) {
+      int j = 1;
+      for (; j <= o.fuse_next && j < 16; ++j) {
+        cplx<R> v[4];
+        int Kj = -1;
+        if (!op_mat2<R>(ops[k + j], theta, v, Kj) || Kj != K) break;
+        const cplx<R> p0 = cfma(v[1], u[2], cmul(v[0], u[0])), p1 = cfma(v[1], u[3], cmul(v[0], u[1]));
+        const cplx<R> p2 = cfma(v[3], u[2], cmul(v[2], u[0])), p3 = cfma(v[3], u[3], cmul(v[2], u[1]));
+        u[0] = p0;
+        u[1] = p1;
+        u[2] = p2;
+        u[3] = p3;
+      }
+      q.code = RC_U1 + K;
+      for (int e = 0; e < 4; ++e) q.m[e] = u[e];
+      q.skip = j;
+    }
+  }
   if (grad && o.slot >= 0) {
     const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
     q.gph = cplx<R>(re[o.gny & 3], im[o.gny & 3]);
@@ -422,7 +500,7 @@ __device__ __forceinline__ void rop_build(ROp<R>& r, const tq_tile_op& o, int k,
 template <typename R>
 __device__ __forceinline__ void rops_build(ROp<R>* rops, const tq_tile_op* __restrict__ ops, int k0, int k1,
                                            const double* theta, bool adj, bool grad) {
-  for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x) rop_build<R>(rops[k - k0], ops[k], k, theta, adj, grad);
+  for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x) rop_build<R>(rops[k - k0], ops, k, theta, adj, grad);
 }
 
 // Sign of the op's Z factors outside the registers: tile base gbase, thread base tbase.
@@ -719,25 +797,30 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, ROp<R>* rops, bool reside
     cplx<R> x[kNR], x2[kNR];
 #pragma unroll
     for (int i = 0; i < kNR; ++i) x[i] = s[pphys(m.idx(i))];
-    const int step = resident ? (st.op_end - st.op_begin) : kRopCap;
-    for (int k0 = st.op_begin; k0 < st.op_end; k0 += step) {
-      const int k1 = min(k0 + step, st.op_end);
+    for (int k0 = st.op_begin; k0 < st.op_end;) {
+      const int k1 = resident ? st.op_end : min(k0 + kRopCap, st.op_end);
       const ROp<R>* rr = rops - (resident ? op0 : k0);
       if (!resident) {
         if (k0 != st.op_begin) __syncthreads();  // readers of the previous chunk are done
         rops_build<R>(rops, ops, k0, k1, theta, false, false);
         __syncthreads();
       }
+      // a fused record may reach past k1; the next chunk starts after it
       int k = k0;
-      for (; k + 1 < k1; k += 2) {
-        rop_apply_to<R>(x, x2, rr[k], ops, rop_sign<R>(rr[k], gbase, m.base));
-        rop_apply_to<R>(x2, x, rr[k + 1], ops, rop_sign<R>(rr[k + 1], gbase, m.base));
-      }
-      if (k < k1) {
-        rop_apply_to<R>(x, x2, rr[k], ops, rop_sign<R>(rr[k], gbase, m.base));
+      while (k < k1) {
+        const ROp<R>& ra = rr[k];
+        rop_apply_to<R>(x, x2, ra, ops, rop_sign<R>(ra, gbase, m.base));
+        k += ra.skip;
+        if (k >= k1) {
 #pragma unroll
-        for (int i = 0; i < kNR; ++i) x[i] = x2[i];
+          for (int i = 0; i < kNR; ++i) x[i] = x2[i];
+          break;
+        }
+        const ROp<R>& rb = rr[k];
+        rop_apply_to<R>(x2, x, rb, ops, rop_sign<R>(rb, gbase, m.base));
+        k += rb.skip;
       }
+      k0 = k;
     }
 #pragma unroll
     for (int i = 0; i < kNR; ++i) s[pphys(m.idx(i))] = x[i];

@@ -26,7 +26,7 @@ from .ir import Gate
 
 TILE_OP_DTYPE = np.dtype({
     "names": ["kind", "a", "b", "slot", "xm", "zm", "cm", "gxm", "gzm", "gcm", "gny", "pidx", "pscale", "gcoef",
-              "zo", "reserved", "zg", "mf", "md"],
+              "zo", "fuse_next", "zg", "mf", "md"],
     "formats": ["<i4", "<i4", "<i4", "<i4", "<u4", "<u4", "<u4", "<u4", "<u4", "<u4", "<i4", "<i4", "<f8", "<f8",
                 "<u4", "<i4", "<u8", ("<f4", 32), ("<f8", 32)],
     "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44, 48, 56, 64, 68, 72, 80, 208],
@@ -360,12 +360,14 @@ _SCALAR_FIELDS = ["kind", "a", "b", "slot", "xm", "zm", "cm", "gxm", "gzm", "gcm
 
 
 def pack_ops(fields: list) -> np.ndarray:
-    """Column-wise fill of a tq_tile_op array from op_fields tuples."""
+    """Column-wise fill of a tq_tile_op array from op_fields tuples (an optional
+    18th entry is fuse_next)."""
     arr = np.zeros(len(fields), dtype=TILE_OP_DTYPE)
     if not fields:
         return arr
     for k, name in enumerate(_SCALAR_FIELDS):
         arr[name] = [f[k] for f in fields]
+    arr["fuse_next"] = [f[17] if len(f) > 17 else 0 for f in fields]
     for size in (2, 4, 16):
         idx = [i for i, f in enumerate(fields) if f[16] is not None and f[16].size == size]
         if idx:
@@ -527,16 +529,18 @@ def plan_stages(op_bits: Sequence[tuple], t: int, rb: int = STAGE_BITS,
         S: set = set()
         order: list = []
         while True:
-            best, bc = None, None
+            # fewest new bits first; among equals prefer an op on the same bits as
+            # the last one (runs of single-qubit ops on one qubit can be fused), then
+            # the lowest index
+            best, bk = None, None
+            last = tuple(sorted(set(op_bits[order[-1]]))) if order else None
             for i in ready:
                 new = set(op_bits[i]) - S
                 if len(S) + len(new) > rb:
                     continue
-                c = len(new)
-                if best is None or c < bc or (c == bc and i < best):
-                    best, bc = i, c
-                    if c == 0:
-                        break
+                key = (len(new), 0 if tuple(sorted(set(op_bits[i]))) == last else 1, i)
+                if best is None or key < bk:
+                    best, bk = i, key
             if best is None:
                 break
             S |= set(op_bits[best])
@@ -556,6 +560,38 @@ def plan_stages(op_bits: Sequence[tuple], t: int, rb: int = STAGE_BITS,
             S.add(b)
         stages.append((sorted(S), order))
     return stages
+
+
+def _single_bit(f: tuple) -> int | None:
+    """Register bit of an op (op_fields tuple) that acts on one register bit with
+    no sign from outside the stage, else None (the device's op_mat2 rule)."""
+    kind, a, _, _, xm, zm, cm = f[:7]
+    zo, zg = f[14], f[15]
+    if zo or zg:
+        return None
+    if kind in (TOP["u1"], TOP["d1"]):
+        return a
+    if kind == TOP["prot"] and cm == 0:
+        if xm and xm & (xm - 1) == 0 and zm & ~xm == 0:
+            return xm.bit_length() - 1
+        if xm == 0 and zm and zm & (zm - 1) == 0:
+            return zm.bit_length() - 1
+    return None
+
+
+def _mark_fusion(fields: list, b: int, e: int) -> None:
+    """Set fuse_next on the first op of each run of consecutive single-bit ops on
+    the same register bit in fields[b:e] (one stage, forward order)."""
+    k = b
+    while k < e:
+        K = _single_bit(fields[k])
+        j = k + 1
+        if K is not None:
+            while j < e and j - k < 16 and _single_bit(fields[j]) == K:
+                j += 1
+        if j - k > 1:
+            fields[k] = fields[k][:17] + (j - k - 1,)
+        k = j
 
 
 @dataclass
@@ -621,6 +657,8 @@ def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], para
                 else:
                     fields.append(op_fields(g, qreg, pidx=pidx, pscale=psc, as_rotation=pidx >= 0 or slots is not None,
                                             outer=loc, n=n))
+            if slots is None:
+                _mark_fusion(fields, ob, len(fields))
             stage_rows.append((bits, ob, len(fields)))
         p = TilePass()
         p.t = t
