@@ -334,8 +334,9 @@ typedef struct {
 /* kind 0: staged forward passes (psi), kind 1: H psi (lam = H psi over 2^hbits
  * output tiles, energy partial per item), kind 2: staged adjoint passes (psi,
  * lam, gradient partials per item and parameter op).  Every pass keeps at
- * least 4 contiguous low bits (nlow >= 4); an adjoint pass holds at most
- * max_pass_ops ops.  Items whose pass breaks either rule are skipped. */
+ * least 4 contiguous low bits (nlow >= 4); a forward (kind 0) or adjoint
+ * (kind 2) pass holds at most max_pass_ops ops, which sizes the shared memory
+ * of the launch.  Items whose pass breaks either rule are skipped. */
 TQ_API int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
                        const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
                        const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,

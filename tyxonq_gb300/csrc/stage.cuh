@@ -506,7 +506,10 @@ __device__ __forceinline__ void rops_build(ROp<R>* rops, const tq_tile_op* __res
 // Sign of the op's Z factors outside the registers: tile base gbase, thread base tbase.
 template <typename R>
 __device__ __forceinline__ R rop_sign(const ROp<R>& r, uint64_t gbase, int tbase) {
-  const int par = (__popcll(gbase & r.zg) + __popc((unsigned)tbase & r.zo)) & 1;
+  const uint32_t zo = r.zo;
+  const uint64_t zg = r.zg;
+  if ((zo | zg) == 0) return R(1);
+  const int par = (__popcll(gbase & zg) + __popc((unsigned)tbase & zo)) & 1;
   return par ? R(-1) : R(1);
 }
 

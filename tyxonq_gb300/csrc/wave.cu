@@ -84,24 +84,30 @@ __device__ __forceinline__ void w_store(const cplx<R>* s, typename C2<R>::T* g, 
 }
 
 // ------------------------------------------------------------------ forward
-// Shared memory: padded tile | offset table (8 << (t - kWaveMinNlow) bytes) | compiled ops.
+// Shared memory: padded tile | offset table (8 << (t - kWaveMinNlow) bytes) |
+// the pass's compiled ops (max_ops records, built once per item before any
+// register holds amplitudes).
 template <typename R>
 __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
     k_wave_forward(const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes,
                    const tq_tile_stage* __restrict__ stages, const tq_tile_op* __restrict__ ops,
-                   const double* __restrict__ theta, void* pool) {
+                   const double* __restrict__ theta, void* pool, int max_ops) {
   extern __shared__ __align__(16) unsigned char smem[];
   typedef typename C2<R>::T T2;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
     const WPass P = wload_pass(&passes[I.pass]);
-    if (P.nlow < kWaveMinNlow) continue;  // the offset table would not fit (the host never plans such passes)
+    const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
+    const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
+    // tables that would not fit the shared memory sized by the host (never planned)
+    if (P.nlow < kWaveMinNlow || nops > max_ops) continue;
     cplx<R>* s = reinterpret_cast<cplx<R>*>(smem);
     int64_t* hoff = reinterpret_cast<int64_t*>(smem + padded_len(P.t) * sizeof(cplx<R>));
     ROp<R>* rops = reinterpret_cast<ROp<R>*>(smem + padded_len(P.t) * sizeof(cplx<R>) + w_hoff_bytes(P.t));
     T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
     __syncthreads();  // previous item's readers of s / hoff / rops are done
     w_hoff(hoff, P);
+    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, false, false);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
     if (I.basis_lo >= 0) {
@@ -117,7 +123,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
       w_commit_wait();
     }
     __syncthreads();
-    run_stages<R>(s, rops, false, 0, stages, P.op_begin, P.op_end, ops, theta + I.theta_off, (uint64_t)base);
+    run_stages<R>(s, rops, true, op0, stages, P.op_begin, P.op_end, ops, theta + I.theta_off, (uint64_t)base);
     w_store<R>(s, psi, base, hoff, P);
   }
 }
@@ -201,8 +207,9 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
 }
 
 // ------------------------------------------------------------------ adjoint
-// Shared memory: psi tile | lam tile | offset table | compiled ops | per-warp
-// gradient partials (max_ops x warps doubles).
+// Shared memory: psi tile | lam tile | offset table | the pass's compiled ops
+// (max_ops records, built at item start) | per-warp gradient partials
+// (max_ops x warps doubles).
 template <typename R>
 __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
     k_wave_adjoint(const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes,
@@ -225,13 +232,14 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
     unsigned char* tail = smem + 2 * PT * sizeof(cplx<R>);
     int64_t* hoff = reinterpret_cast<int64_t*>(tail);
     ROp<R>* rops = reinterpret_cast<ROp<R>*>(tail + w_hoff_bytes(P.t));
-    double* wpart = reinterpret_cast<double*>(tail + w_hoff_bytes(P.t) + kRopCap * sizeof(ROp<R>));
+    double* wpart = reinterpret_cast<double*>(tail + w_hoff_bytes(P.t) + (size_t)max_ops * sizeof(ROp<R>));
     T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
     T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
     const double* th = theta + I.theta_off;
     __syncthreads();
     w_hoff(hoff, P);
     for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = 0.0;
+    rops_build<R>(rops, ops, op0, op0 + nops, th, true, true);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
     w_load<R>(sp, psi, base, hoff, P);
@@ -248,22 +256,16 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
         x[i] = sp[j];
         y[i] = sl[j];
       }
-      for (int k0 = st.op_begin; k0 < st.op_end; k0 += kRopCap) {
-        const int k1 = min(k0 + kRopCap, st.op_end);
-        if (k0 != st.op_begin) __syncthreads();  // readers of the previous chunk are done
-        rops_build<R>(rops, ops, k0, k1, th, true, true);
-        __syncthreads();
-        for (int k = k0; k < k1; ++k) {
-          const ROp<R>& r = rops[k - k0];
-          const R zs = rop_sign<R>(r, (uint64_t)base, mp.base);
-          if (r.gcode != RG_NONE) {
-            R part = zs * rop_grad<R>(x, y, r, ops);
+      for (int k = st.op_begin; k < st.op_end; ++k) {
+        const ROp<R>& r = rops[k - op0];
+        const R zs = rop_sign<R>(r, (uint64_t)base, mp.base);
+        if (r.gcode != RG_NONE) {
+          R part = zs * rop_grad<R>(x, y, r, ops);
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
-            if (lane == 0) wpart[(k - op0) * nwarps + warp] = (double)part;
-          }
-          rop_apply<R, 2>(x, y, r, ops, true, zs);
+          for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
+          if (lane == 0) wpart[(k - op0) * nwarps + warp] = (double)part;
         }
+        rop_apply<R, 2>(x, y, r, ops, true, zs);
       }
 #pragma unroll
       for (int i = 0; i < kNR; ++i) {
@@ -300,12 +302,12 @@ __global__ void k_wave_reduce(const double* __restrict__ partials, const int32_t
 }
 
 template <typename R>
-static size_t fwd_smem(int t) {
-  return padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + kRopCap * sizeof(ROp<R>);
+static size_t fwd_smem(int t, int max_ops) {
+  return padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + (size_t)max_ops * sizeof(ROp<R>);
 }
 template <typename R>
 static size_t adj_smem(int t, int max_ops) {
-  return 2 * padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + kRopCap * sizeof(ROp<R>) +
+  return 2 * padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + (size_t)max_ops * sizeof(ROp<R>) +
          sizeof(double) * (size_t)max_ops * ((1 << (t - kRB)) / 32);
 }
 
@@ -331,10 +333,11 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
   const int threads = 1 << (t - kRB);
   const int grid = n_items;
   if (kind == 0) {
-    const size_t smem = fwd_smem<R>(t);
+    const size_t smem = fwd_smem<R>(t, max_ops);
+    if (smem > 227 * 1024) return fail(TQ_ERR_ARG, "tq_wave_run: forward needs %zu B shared memory", smem);
     cudaError_t e = cudaFuncSetAttribute(k_wave_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");
-    k_wave_forward<R><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool);
+    k_wave_forward<R><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool, max_ops);
   } else {
     const size_t smem = adj_smem<R>(t, max_ops);
     if (smem > 227 * 1024) return fail(TQ_ERR_ARG, "tq_wave_run: adjoint needs %zu B shared memory", smem);
@@ -361,7 +364,8 @@ extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n
   if (!items || !pool) return fail(TQ_ERR_ARG, "tq_wave_run: NULL pointer");
   if (kind != 1 && (!passes || !stages || !ops || !theta)) return fail(TQ_ERR_ARG, "tq_wave_run: NULL table");
   if (kind == 1 && (!groups || !terms || !partials)) return fail(TQ_ERR_ARG, "tq_wave_run: NULL Pauli table");
-  if (kind == 2 && (!partials || max_pass_ops < 1)) return fail(TQ_ERR_ARG, "tq_wave_run: adjoint partials");
+  if (kind == 2 && !partials) return fail(TQ_ERR_ARG, "tq_wave_run: adjoint partials");
+  if (kind != 1 && max_pass_ops < 1) return fail(TQ_ERR_ARG, "tq_wave_run: max_pass_ops %d < 1", max_pass_ops);
   cudaStream_t s = (cudaStream_t)stream;
   return dtype == TQ_C64 ? wave_launch<float>(kind, items, n_items, t, hbits, passes, stages, ops, groups, terms,
                                               theta, pool, partials, max_pass_ops, s)

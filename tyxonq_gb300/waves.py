@@ -40,6 +40,17 @@ PASS_DTYPE = np.dtype({"names": ["t", "nlow", "op_begin", "op_end", "pos"],
                        "formats": ["<i4", "<i4", "<i4", "<i4", ("<i4", 16)], "itemsize": 80})
 
 
+def _max_pass_ops(enc) -> int:
+    """Largest op count of one pass of an EncodedStaged."""
+    st = enc.stages_host
+    best = 0
+    for p in range(enc.n_passes):
+        ps = enc.passes[p]
+        if ps.op_end > ps.op_begin:
+            best = max(best, int(st[ps.op_end - 1]["op_end"] - st[ps.op_begin]["op_begin"]))
+    return best
+
+
 def _dev(arr: np.ndarray, device) -> torch.Tensor:
     return torch.frombuffer(bytearray(arr.tobytes() or b"\0" * 16), dtype=torch.uint8).to(device)
 
@@ -58,6 +69,7 @@ class WavePlan:
         S = 8 if dtype == torch.complex64 else 16
         self.passes, self.stages, self.ops = [], [], []
         self.adj_max_ops = 1
+        self.fwd_max_ops = 1
         self._np = self._ns = self._no = 0
         cache = {}
         for e in entries:
@@ -186,12 +198,14 @@ class WavePlan:
 
     def _encode(self, n, gates, params) -> dict:
         t = self.t
-        segs = plan_passes(gates, n, t)
+        segs = plan_passes(gates, n, t, max_ops=self.max_ops)
         fwd = []
         for s in segs:
             if s.kind != "tiles":
                 raise NotImplementedError("wave path needs tileable gates")
-            fwd += self._add_staged(encode_staged(n, s.passes, gates, params=params))
+            enc = encode_staged(n, s.passes, gates, params=params)
+            fwd += self._add_staged(enc)
+            self.fwd_max_ops = max(self.fwd_max_ops, _max_pass_ops(enc))
         if not fwd:  # no gates: one empty pass writes |basis>
             qs = list(range(n - 1, n - 1 - t, -1))
             fwd += self._add_staged(encode_staged(n, [PassPlan(qs, [], 5)], gates))
@@ -230,7 +244,7 @@ class WavePlan:
                          self.hbits, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
                          P(self.ops_dev.data_ptr()), P(groups_dev.data_ptr()), P(terms_dev.data_ptr()),
                          P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()),
-                         self.adj_max_ops, stream)
+                         self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
             else:
                 kind, b, c = L
                 out = energies if kind == "reduce_e" else grads
