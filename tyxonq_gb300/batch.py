@@ -57,7 +57,7 @@ class Schedule:
     max_pass_ops: int = 512
     large: str = "waves"  # instances above res1_max: "waves" (L2-resident grid-wide phases) or "cta"
     wave_t: int = 12
-    wave_hbits: int = 10
+    wave_hbits: int = 12
     wave_budget: int = 96 << 20
     wave_max_ops: int = 256
 
@@ -78,6 +78,21 @@ class Schedule:
         if n <= self.res1_max:
             return "res1", 1, 1024
         return "streamed", 1, 1024
+
+
+def sort_terms_by_class(groups: np.ndarray, terms: np.ndarray, hbits: int) -> np.ndarray:
+    """Order each group's terms by their Z/Y bits 8 .. hbits-1 (the bits that
+    tell apart the amplitudes one thread of the wave H psi kernel holds), so
+    the kernel's per-class sums switch class at most 2^(hbits-8) - 1 times per
+    group.  Groups keep their term ranges; only the order inside changes."""
+    if len(terms) == 0 or hbits <= 8:
+        return terms
+    gid = np.repeat(np.arange(len(groups)), groups["n_terms"])
+    first = np.repeat(groups["first_term"], groups["n_terms"])
+    order_in = np.arange(len(terms)) - first  # position inside the group (groups are contiguous, in order)
+    cls = (terms["zy"] >> np.uint64(8)) & np.uint64((1 << (hbits - 8)) - 1)
+    idx = np.lexsort((order_in, cls.astype(np.int64), gid))
+    return terms[idx]
 
 
 def structure_gates(structure) -> tuple[list[Gate], dict]:
@@ -152,6 +167,10 @@ class BatchedVQE:
             H: PauliSum = inst.H
             g, t = H.pack()
             if cname == "streamed" and self.sched.large == "waves":
+                t = sort_terms_by_class(g, t, self.sched.wave_hbits)
+                # groups whose flips share the bits above the H psi tile read the same
+                # partner tile: neighbours in the loop, so it is reused from L1
+                g = g[np.lexsort((g["flip"], g["flip"] >> np.uint64(self.sched.wave_hbits)))]
                 wave_entries.append({"idx": i, "n": n, "gates": gates, "params": params, "key": (n, skey),
                                      "theta_offset": theta_off, "theta_off": theta_off, "grad_offset": theta_off,
                                      "basis": int(getattr(inst, "basis", 0)), "group_begin": n_groups_total,

@@ -7,7 +7,9 @@
 //   kind 0  forward: register-staged tile pass on psi (the instance's first
 //           pass also writes the initial basis state, so no separate init);
 //   kind 1  H psi: one output tile of 2^hbits amplitudes per item, partner
-//           amplitudes psi[i ^ flip] read directly, accumulators in registers;
+//           amplitudes psi[i ^ flip] read from source tiles staged once in
+//           shared memory per distinct high part of the flip, accumulators in
+//           registers;
 //           the item's share of <psi|H psi> goes to partials[part_off];
 //   kind 2  adjoint: register-staged un-apply of psi and lam with the
 //           gradient terms Im <lam|G|psi> reduced per warp in a fixed order,
@@ -52,6 +54,12 @@ __device__ __forceinline__ int64_t w_base(int64_t g, const WPass& P) {
   int64_t x = g << P.nlow;
   for (int k = P.nlow; k < P.t; ++k) x = insert_zero(x, P.pos[k]);
   return x;
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 __device__ __forceinline__ void w_commit_wait() {
@@ -129,12 +137,20 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
 }
 
 // ------------------------------------------------------------------ H psi
+// Item = output tile of HN = 2^hb amplitudes (256 threads x PER).  The partner
+// of output i under a group with flip m is psi[i ^ m]: it lies in source tile
+// (tile ^ (m >> hb)) at offset (i ^ m) mod HN.  Groups are visited in the order
+// of the table (the host sorts them by m >> hb), and each distinct source tile
+// is copied once into shared memory, where every group that shares it reads
+// its partners.
 template <typename R, int PER>
 __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restrict__ items, int n_items, int hbits,
                                                    const tq_pauli_group* __restrict__ groups,
                                                    const tq_pauli_term* __restrict__ terms, void* pool,
                                                    double* partials) {
   typedef typename C2<R>::T T2;
+  extern __shared__ __align__(16) unsigned char smem[];
+  cplx<R>* src = reinterpret_cast<cplx<R>*>(smem);
   __shared__ double red[32];
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
@@ -142,43 +158,106 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
     const int HN = 1 << hb;
     const T2* psi = reinterpret_cast<const T2*>(pool) + I.psi_off;
     T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
-    const int64_t t0 = (int64_t)I.tile << hb;
+    const int64_t tile = I.tile;
+    const int64_t t0 = tile << hb;
     cplx<R> acc[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) acc[k] = cplx<R>(0, 0);
     const bool full = (HN >= PER * (int)blockDim.x);
-    for (int g = I.group_begin; g < I.group_begin + I.group_count; ++g) {
-      const uint64_t m = __ldg(&groups[g].flip);
-      const int first = __ldg(&groups[g].first_term), cnt = __ldg(&groups[g].n_terms);
-      // partner amplitudes first (independent loads in flight), then each term once for all of them
-      cplx<R> pv[PER], f[PER];
-#pragma unroll
-      for (int k = 0; k < PER; ++k) {
-        const int j = threadIdx.x + k * blockDim.x;
-        const T2 v = (full || j < HN) ? psi[(t0 + j) ^ (int64_t)m] : T2();
-        pv[k] = cplx<R>(v.x, v.y);
-        f[k] = cplx<R>(0, 0);
+    const int gend = I.group_begin + I.group_count;
+    // source tiles double-buffered: the next run's tile streams in while this run computes
+    auto issue = [&](cplx<R>* dst, int64_t h) {
+      const T2* sp = psi + ((tile ^ h) << hb);
+      constexpr int A = 16 / sizeof(cplx<R>);
+      if (HN >= A) {
+        for (int c = threadIdx.x; c < HN / A; c += blockDim.x) cp_async16(&dst[c * A], &sp[c * A]);
+      } else {
+        for (int j = threadIdx.x; j < HN; j += blockDim.x) dst[j] = cplx<R>(sp[j].x, sp[j].y);
       }
-      // src_k = (t0 | tid | k << 8) ^ m with disjoint bit fields (t0 is a multiple of
-      // 2^hb = PER * 256), so parity(src_k & zy) = parity((t0 | tid) ^ m) & zy)
-      // XOR parity(k & (zy >> 8)): one popc per term and thread, not one per amplitude.
-      const uint64_t sbase = (uint64_t)((t0 | (int64_t)threadIdx.x) ^ (int64_t)m);
-      for (int tt = 0; tt < cnt; ++tt) {
-        const uint64_t zy = __ldg(&terms[first + tt].zy);
-        const R wr = (R)__ldg(&terms[first + tt].w_re), wi = (R)__ldg(&terms[first + tt].w_im);
-        const int p0 = __popcll(sbase & zy) & 1;
-        const int kz = (int)(zy >> 8);
+      cp_async_commit();
+    };
+    int buf = 0;
+    if (I.group_count > 0) issue(src, (int64_t)(__ldg(&groups[I.group_begin].flip) >> hb));
+    for (int g = I.group_begin; g < gend;) {
+      const int64_t h = (int64_t)(__ldg(&groups[g].flip) >> hb);
+      int ge = g + 1;
+      while (ge < gend && (int64_t)(__ldg(&groups[ge].flip) >> hb) == h) ++ge;
+      cplx<R>* cb = src + (buf ? HN : 0);
+      if (ge < gend) issue(src + (buf ? 0 : HN), (int64_t)(__ldg(&groups[ge].flip) >> hb));
+      else cp_async_commit();
+      cp_async_wait_group<1>();
+      __syncthreads();
+      for (; g < ge; ++g) {
+        const uint64_t m = __ldg(&groups[g].flip);
+        const int first = __ldg(&groups[g].first_term), cnt = __ldg(&groups[g].n_terms);
+        const int ml = (int)(m & (uint64_t)(HN - 1));
+        cplx<R> pv[PER], W[PER];
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
-          const int kp = k & kz;
-          const int par = p0 ^ ((kp ^ (kp >> 1) ^ (kp >> 2) ^ (kp >> 3)) & 1);
-          f[k].x += par ? -wr : wr;
-          f[k].y += par ? -wi : wi;
+          const int j = threadIdx.x + k * blockDim.x;
+          pv[k] = (full || j < HN) ? cb[j ^ ml] : cplx<R>(0, 0);
+          W[k] = cplx<R>(0, 0);
         }
-      }
+        // src_k = (t0 | tid | k << 8) ^ m with disjoint bit fields (t0 is a multiple
+        // of 2^hb = PER * 256), so parity(src_k & zy) = parity(((t0 | tid) ^ m) & zy)
+        // XOR parity(k & c) with c = (zy >> 8) & (PER - 1): one popcount per term
+        // and thread.
+        const uint64_t sbase = (uint64_t)((t0 | (int64_t)threadIdx.x) ^ (int64_t)m);
+        if (cnt <= 2 || PER == 1) {
+          // few terms: signs per amplitude directly
+          for (int tt = 0; tt < cnt; ++tt) {
+            const uint64_t zy = __ldg(&terms[first + tt].zy);
+            const R wr = (R)__ldg(&terms[first + tt].w_re), wi = (R)__ldg(&terms[first + tt].w_im);
+            const int p0 = __popcll(sbase & zy) & 1;
+            const int c = (int)(zy >> 8) & (PER - 1);
 #pragma unroll
-      for (int k = 0; k < PER; ++k) acc[k] = cfma(f[k], pv[k], acc[k]);
+            for (int k = 0; k < PER; ++k) {
+              const bool neg = (p0 ^ __popc(k & c)) & 1;
+              W[k] = cplx<R>(W[k].x + (neg ? -wr : wr), W[k].y + (neg ? -wi : wi));
+            }
+          }
+        } else {
+          // many terms: sum per class c (W_c), then f_k = sum_c W_c (-1)^{popc(k & c)},
+          // a PER-point Walsh-Hadamard transform.  Terms sorted by c make the class
+          // switches rare; the result does not depend on the order.
+          int cur = 0;
+          R sr = 0, si = 0;
+          for (int tt = 0; tt < cnt; ++tt) {
+            const uint64_t zy = __ldg(&terms[first + tt].zy);
+            const R wr = (R)__ldg(&terms[first + tt].w_re), wi = (R)__ldg(&terms[first + tt].w_im);
+            const int c = (int)(zy >> 8) & (PER - 1);
+            if (c != cur) {  // same for every thread: the term is shared
+#pragma unroll
+              for (int q = 0; q < PER; ++q)
+                if (q == cur) W[q] = cplx<R>(W[q].x + sr, W[q].y + si);
+              cur = c;
+              sr = si = 0;
+            }
+            const bool neg = __popcll(sbase & zy) & 1;
+            sr += neg ? -wr : wr;
+            si += neg ? -wi : wi;
+          }
+#pragma unroll
+          for (int q = 0; q < PER; ++q)
+            if (q == cur) W[q] = cplx<R>(W[q].x + sr, W[q].y + si);
+#pragma unroll
+          for (int hh = 1; hh < PER; hh <<= 1) {
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+              if (q & hh) continue;
+              const cplx<R> a = W[q], b = W[q + hh];
+              W[q] = cplx<R>(a.x + b.x, a.y + b.y);
+              W[q + hh] = cplx<R>(a.x - b.x, a.y - b.y);
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < PER; ++k) acc[k] = cfma(W[k], pv[k], acc[k]);
+      }
+      __syncthreads();  // readers of cb are done before it is refilled
+      buf ^= 1;
     }
+    cp_async_wait_group<0>();
     R eloc = 0;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
@@ -319,13 +398,20 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
   if (kind == 1) {
     if (hbits < 8 || hbits > 12) return fail(TQ_ERR_ARG, "tq_wave_run: hbits %d outside [8, 12]", hbits);
     const int grid = n_items;
+    const size_t sm = 2 * (sizeof(cplx<R>) << hbits);  // two source tiles
+    cudaError_t e = cudaSuccess;
+#define TQ_HPSI(PER_)                                                                                          \
+  e = cudaFuncSetAttribute(k_wave_hpsi<R, PER_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);        \
+  if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");                                  \
+  k_wave_hpsi<R, PER_><<<grid, 256, sm, s>>>(items, n_items, hbits, groups, terms, pool, partials);
     switch (hbits) {
-      case 8: k_wave_hpsi<R, 1><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
-      case 9: k_wave_hpsi<R, 2><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
-      case 10: k_wave_hpsi<R, 4><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
-      case 11: k_wave_hpsi<R, 8><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
-      default: k_wave_hpsi<R, 16><<<grid, 256, 0, s>>>(items, n_items, hbits, groups, terms, pool, partials); break;
+      case 8: TQ_HPSI(1) break;
+      case 9: TQ_HPSI(2) break;
+      case 10: TQ_HPSI(4) break;
+      case 11: TQ_HPSI(8) break;
+      default: TQ_HPSI(16) break;
     }
+#undef TQ_HPSI
     TQ_CHECK_LAUNCH("tq_wave_run (H psi)");
     return TQ_OK;
   }
