@@ -121,6 +121,16 @@ TQ_API int tq_sv_expect_z_all(const void* psi, int n, int dtype, double* out_dev
  * engine.py:377-379 / probability() engine.py:1041-1047. */
 TQ_API int tq_sv_probabilities(const void* psi, int n, int dtype, void* probs, void* stream);
 
+/* Reduced density matrix of one qubit (unnormalised): out_dev[0..3] =
+ * sum |a|^2, sum |b|^2, Re sum a conj(b), Im sum a conj(b) over the amplitude
+ * pairs a = psi_i (qubit 0), b = psi_{i'} (qubit 1).  The Born weights of a
+ * one-qubit Kraus channel, ||K_i psi||^2 = Tr(K_i rho K_i^dagger), follow on the
+ * host; replaces the per-operator apply-and-sum loop of apply_kraus_statevector
+ * (tyxonq/libs/quantum_library/kernels/statevector.py:132-218).  FP64 sums. */
+TQ_API size_t tq_sv_qubit_rdm_workspace_bytes(int n);
+TQ_API int tq_sv_qubit_rdm(const void* psi, int n, int dtype, int qubit, double* out_dev, void* ws,
+                           size_t ws_bytes, void* stream);
+
 /* Squared norm sum_i |psi_i|^2 into *out_dev (FP64). */
 TQ_API size_t tq_sv_norm_workspace_bytes(int n);
 TQ_API int tq_sv_norm2(const void* psi, int n, int dtype, double* out_dev, void* ws, size_t ws_bytes,

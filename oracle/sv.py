@@ -166,16 +166,88 @@ def project_z(psi: np.ndarray, q: int, keep: int, n: int) -> np.ndarray:
 
 # ------------------------------------------------------------------ engine dispatch (engine.py)
 RUN_OPS = {"h", "rz", "rx", "ry", "cx", "cry", "cz", "iswap", "swap", "rxx", "ryy", "rzz", "x", "s", "sdg",
-           "measure_z", "barrier", "project_z", "reset", "unitary"}
+           "measure_z", "barrier", "project_z", "reset", "unitary", "kraus"}
 # state() lacks cry/y/z/t/tdg/cy/measure_z/barrier branches (engine.py:914-1039)
 STATE_OPS = {"h", "rz", "rx", "ry", "cx", "cz", "iswap", "swap", "rxx", "ryy", "rzz", "x", "s", "sdg",
-             "project_z", "reset", "unitary"}
+             "project_z", "reset", "unitary", "kraus"}
+
+
+def apply_kraus(psi: np.ndarray, ops: Sequence[np.ndarray], q: int, n: int, status: float) -> np.ndarray:
+    """apply_kraus_statevector (kernels/statevector.py:132-218): Born weights
+    p_i = ||K_i psi||^2, normalised cumulative sums, the first i with
+    status <= cum_i (0 if none), then K_i psi / ||K_i psi||."""
+    outs = [apply_1q(psi, np.asarray(k, dtype=np.complex128), q, n) for k in ops]
+    p = np.array([float(np.real(np.vdot(o, o))) for o in outs])
+    cum = np.cumsum(p / p.sum())
+    sel = 0
+    for i, c in enumerate(cum):
+        if status <= float(c):
+            sel = i
+            break
+    out = outs[sel]
+    return out / np.sqrt(np.real(np.vdot(out, out)))
+
+
+# gates that feed use_noise's Z attenuation (engine.py:56-143)
+ATTENUATED_OPS = {"h", "rz", "rx", "ry", "cx", "cry", "cz", "iswap", "swap", "rxx", "ryy", "rzz", "x", "s", "sdg",
+                  "unitary"}
+
+
+def z_attenuation(n: int, ops: Sequence[Any], noise: dict, unitary_cache: dict | None = None) -> np.ndarray:
+    """_attenuate (engine.py:488-494) over the run() gate loop: depolarizing p
+    multiplies the factor of every wire a gate touches by max(0, 1 - 4p/3)."""
+    att = np.ones(n)
+    if str(noise.get("type", "")).lower() != "depolarizing":
+        return att
+    f = max(0.0, 1.0 - 4.0 * float(noise.get("p", 0.0)) / 3.0)
+    cache = unitary_cache or {}
+    for op in ops:
+        if not isinstance(op, (list, tuple)) or not op or op[0] not in ATTENUATED_OPS:
+            continue
+        if op[0] in ("h", "rz", "rx", "ry", "x", "s", "sdg"):
+            wires = [int(op[1])]
+        elif op[0] == "unitary":
+            if len(op) == 3 and cache.get(str(op[2])) is not None:
+                wires = [int(op[1])]
+            elif len(op) == 4 and cache.get(str(op[3])) is not None:
+                wires = [int(op[1]), int(op[2])]
+            else:
+                continue
+        else:
+            wires = [int(op[1]), int(op[2])]
+        for q in wires:
+            att[q] *= f
+    return att
+
+
+def noisy_probabilities(psi: np.ndarray, n: int, noise: dict) -> np.ndarray:
+    """The sampled distribution of run(use_noise=True) (engine.py:377-414):
+    |psi|^2, then readout (kron of per-qubit calibration matrices, identity
+    where absent) or depolarizing mixing (1 - a) p + a / 2^n, a = min(1, 4p/3);
+    clip to [0, 1], renormalise, uniform if nothing is left."""
+    p = np.abs(psi) ** 2
+    ntype = str(noise.get("type", "")).lower()
+    if ntype == "readout":
+        cals = noise.get("cals", {}) or {}
+        A = None
+        for q in range(n):
+            m = np.asarray(cals.get(q, np.eye(2)), dtype=float)
+            A = m if A is None else np.kron(A, m)
+        p = A @ p
+    elif ntype == "depolarizing":
+        a = max(0.0, min(1.0, 4.0 * float(noise.get("p", 0.0)) / 3.0))
+        p = (1.0 - a) * p + a / p.size
+    p = np.clip(p, 0.0, 1.0)
+    s = float(p.sum())
+    p = p / (s if s > 1e-12 else 1.0)
+    return p / p.sum() if p.sum() > 0 else np.full(p.size, 1.0 / p.size)
 
 
 def run_ops(n: int, ops: Sequence[Any], *, mode: str = "state", unitary_cache: dict | None = None,
-            initial: np.ndarray | None = None) -> tuple[np.ndarray, list[int]]:
+            initial: np.ndarray | None = None, kraus_cache: dict | None = None) -> tuple[np.ndarray, list[int]]:
     """Gate loop of StatevectorEngine.run (engine.py:52-374) / .state
-    (engine.py:914-1039).  Returns (psi, measured qubits)."""
+    (engine.py:914-1039).  Returns (psi, measured qubits).  Kraus ops need an
+    explicit status here (the reference draws a missing one at random)."""
     psi = init_state(n) if initial is None else np.asarray(initial, dtype=np.complex128).reshape(-1).copy()
     allowed = RUN_OPS if mode == "run" else STATE_OPS
     measures: list[int] = []
@@ -199,6 +271,10 @@ def run_ops(n: int, ops: Sequence[Any], *, mode: str = "state", unitary_cache: d
             psi = project_z(psi, int(op[1]), int(op[2]), n)
         elif name == "reset":
             psi = project_z(psi, int(op[1]), 0, n)
+        elif name == "kraus":  # engine.py:145-155
+            kops = (kraus_cache or {}).get(str(op[2]))
+            if kops is not None:
+                psi = apply_kraus(psi, kops, int(op[1]), n, float(op[3]))
         elif name == "unitary":
             cache = unitary_cache or {}
             if len(op) == 3:

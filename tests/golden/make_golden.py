@@ -11,7 +11,9 @@ It imports TyxonQ from the given source tree and records, for seeded inputs:
   * apply_kqubit_unitary outputs for k = 1..5;
   * Pauli-sum energies through pauli_string_sum_dense + dynamics.expectation;
   * the 12-qubit hardware-efficient TFIM energy (numpy and pytorch backends)
-    and its PyTorch-autograd gradient.
+    and its PyTorch-autograd gradient;
+  * circuits with one-qubit Kraus channels (explicit status): final states,
+    <Z_q>, and <Z_q> under use_noise depolarizing attenuation.
 Outputs: tests/golden/golden.npz (arrays) and tests/golden/golden.json
 (circuits and scalars).  The reference is not needed to *use* the fixtures.
 """
@@ -181,6 +183,41 @@ def main(ref_src: str) -> None:
     arrays["hea12_codes"] = np.asarray(codes, dtype=np.int64)
     arrays["hea12_w"] = np.asarray(weights)
     meta["hea12"] = {"n": n, "layers": L, "energy_numpy": e_np, "energy_pytorch": float(e_t.item())}
+
+    # Kraus channels (stochastic unravelling with explicit status) and use_noise
+    meta["noise"] = []
+    g1, g2 = 0.2, 0.3
+    kraus_sets = {
+        "amp_damp": [np.array([[1, 0], [0, math.sqrt(1 - g1)]]), np.array([[0, math.sqrt(g1)], [0, 0]])],
+        "phase_damp": [np.array([[1, 0], [0, math.sqrt(1 - g2)]]), np.array([[0, 0], [0, math.sqrt(g2)]])],
+        "depol": [math.sqrt(1 - 0.75 * 0.1) * np.eye(2), math.sqrt(0.1 / 4) * np.array([[0, 1], [1, 0]]),
+                  math.sqrt(0.1 / 4) * np.array([[0, -1j], [1j, 0]]), math.sqrt(0.1 / 4) * np.array([[1, 0], [0, -1]])],
+    }
+    for ni, n in enumerate([3, 5, 6]):
+        ops = random_ops(n, 12 + 4 * ni)
+        c = Circuit(n, ops=[tuple(o) for o in ops])
+        kr = []
+        for j in range(4):
+            name = ["amp_damp", "phase_damp", "depol", "amp_damp"][j]
+            q = int(rng.integers(n))
+            st = float(rng.uniform(0, 1))
+            c.kraus(q, kraus_sets[name], status=st)
+            kr.append([name, q, st])
+            for o in random_ops(n, 3):
+                c.ops.append(tuple(o))
+        psi = np.asarray(eng.state(c), dtype=np.complex128)
+        c_m = Circuit(n, ops=list(c.ops) + [("measure_z", q) for q in range(n)])
+        c_m._kraus_cache = dict(c._kraus_cache)
+        z = eng.run(c_m, shots=0)["expectations"]
+        zn = eng.run(c_m, shots=0, use_noise=True, noise={"type": "depolarizing", "p": 0.05})["expectations"]
+        arrays[f"nz{ni}_state"] = psi
+        arrays[f"nz{ni}_runz"] = np.asarray([z[f"Z{q}"] for q in range(n)])
+        arrays[f"nz{ni}_runz_depol"] = np.asarray([zn[f"Z{q}"] for q in range(n)])
+        names = {id(v): k for k, v in kraus_sets.items()}
+        meta["noise"].append({"name": f"nz{ni}", "n": n, "ops": [list(o) for o in c.ops],
+                              "kraus": {k: names[id(v)] for k, v in c._kraus_cache.items()}})
+    meta["kraus_sets"] = {k: [[[complex(x).real, complex(x).imag] for x in np.asarray(m).reshape(-1)] for m in v]
+                          for k, v in kraus_sets.items()}
 
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "golden.json").write_text(json.dumps(meta, indent=1))

@@ -24,3 +24,22 @@ def circuit_cases():
         ops = [tuple(o) for o in c["ops"]]
         out.append((c["name"], c["n"], ops, ucache, arrays[f"{c['name']}_state"], arrays[f"{c['name']}_runz"]))
     return out
+
+
+def kraus_sets():
+    _, meta = load()
+    return {k: [np.array([complex(re, im) for re, im in m], dtype=np.complex128).reshape(2, 2) for m in v]
+            for k, v in meta["kraus_sets"].items()}
+
+
+def noise_cases():
+    """(name, n, ops, kraus_cache, state, run <Z>, run <Z> under use_noise depolarizing p=0.05)."""
+    arrays, meta = load()
+    sets = kraus_sets()
+    out = []
+    for c in meta["noise"]:
+        kc = {key: sets[name] for key, name in c["kraus"].items()}
+        ops = [tuple(o) for o in c["ops"]]
+        out.append((c["name"], c["n"], ops, kc, arrays[f"{c['name']}_state"], arrays[f"{c['name']}_runz"],
+                    arrays[f"{c['name']}_runz_depol"]))
+    return out

@@ -397,5 +397,11 @@ def test_lowering_follows_reference_dispatch():
     assert [g.kind for g in g_state] == ["u1", "d1"]  # y/z/t/cry ignored, cx(q,q) no-op
     assert [g.kind for g in g_run] == ["u1", "u2", "d1"]  # run() has cry
     assert m_run == [0] and m_state == []
+    # a Kraus op whose operators are not cached is skipped (engine.py:150-151); pulses are not supported
+    assert lower_ops(_C(1, [("kraus", 0, "k")]), mode="run")[0] == []
+    c = _C(1, [("kraus", 0, "k", 0.3)])
+    c._kraus_cache = {"k": [np.eye(2)]}
+    (g,), _ = lower_ops(c, mode="state")
+    assert g.kind == "kraus" and g.qubits == (0,) and g.status == 0.3 and len(g.kraus) == 1
     with pytest.raises(NotImplementedError):
-        lower_ops(_C(1, [("kraus", 0, "k")]), mode="run")
+        lower_ops(_C(1, [("pulse", 0, "p")]), mode="run")

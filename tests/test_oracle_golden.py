@@ -123,3 +123,32 @@ def test_chi2_sampler_check_is_sensitive():
     # a planted mistake in the oracle side: sample from the wrong distribution
     bad = sv.sample_counts(sv.run_ops(4, [("h", 0), ("ry", 1, 0.5), ("cx", 0, 2), ("rx", 3, 1.1)])[0], 20000, rng)
     assert sv.chi2_pvalue(bad, p) < 1e-6
+
+
+@pytest.mark.parametrize("case", golden_data.noise_cases(), ids=lambda c: c[0])
+def test_kraus_and_noise_against_reference(case):
+    """Kraus channels with explicit status and use_noise Z attenuation, against
+    the reference engine's own outputs."""
+    name, n, ops, kc, state, runz, runz_depol = case
+    psi, _ = sv.run_ops(n, ops, mode="state", kraus_cache=kc)
+    np.testing.assert_allclose(psi, state, atol=1e-12)
+    ops_m = list(ops) + [("measure_z", q) for q in range(n)]
+    psi_r, meas = sv.run_ops(n, ops_m, mode="run", kraus_cache=kc)
+    z = np.array([sv.expect_z(psi_r, q, n) for q in meas])
+    np.testing.assert_allclose(z, runz, atol=1e-12)
+    att = sv.z_attenuation(n, ops_m, {"type": "depolarizing", "p": 0.05})
+    np.testing.assert_allclose(z * att, runz_depol, atol=1e-12)
+
+
+def test_noisy_probabilities_readout_and_depolarizing():
+    rng = np.random.default_rng(3)
+    n = 4
+    psi = rng.normal(size=16) + 1j * rng.normal(size=16)
+    psi /= np.linalg.norm(psi)
+    p = np.abs(psi) ** 2
+    cals = {0: np.array([[0.9, 0.2], [0.1, 0.8]]), 2: np.array([[0.95, 0.05], [0.05, 0.95]])}
+    pr = sv.noisy_probabilities(psi, n, {"type": "readout", "cals": cals})
+    A = np.kron(np.kron(np.kron(cals[0], np.eye(2)), cals[2]), np.eye(2))
+    np.testing.assert_allclose(pr, A @ p / (A @ p).sum(), atol=1e-14)
+    pd = sv.noisy_probabilities(psi, n, {"type": "depolarizing", "p": 0.3})
+    np.testing.assert_allclose(pd, 0.6 * p + 0.4 / 16, atol=1e-14)

@@ -63,6 +63,8 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_expect_z_workspace_bytes": (c_size_t, [c_int]),
     "tq_sv_expect_z_all": (c_int, [_P, c_int, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_probabilities": (c_int, [_P, c_int, c_int, _P, _P]),
+    "tq_sv_qubit_rdm_workspace_bytes": (c_size_t, [c_int]),
+    "tq_sv_qubit_rdm": (c_int, [_P, c_int, c_int, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_norm_workspace_bytes": (c_size_t, [c_int]),
     "tq_sv_norm2": (c_int, [_P, c_int, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_sample_workspace_bytes": (c_size_t, [c_int, c_int64]),

@@ -56,6 +56,30 @@ __global__ void k_finalize(const double* partials, int nblk, int nout, double* o
   if (threadIdx.x == 0) out[o] = acc;
 }
 
+// ----------------------------------------------------------------- one-qubit reduced density matrix
+// Over the pairs (a, b) = (psi_i, psi_{i | bit}) with the bit clear:
+// partials[blk * 4 + {0,1,2,3}] = sum |a|^2, sum |b|^2, Re sum a conj(b), Im sum a conj(b).
+template <typename R>
+__global__ void k_qubit_rdm(const typename C2<R>::T* psi, int64_t half, int bit, double* partials) {
+  __shared__ double sh[32];
+  R s00 = 0, s11 = 0, sre = 0, sim = 0;
+  const int64_t lo = (int64_t(1) << bit) - 1;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < half; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = ((p >> bit) << (bit + 1)) | (p & lo);
+    const cplx<R> a = ldc<R>(psi, i), b = ldc<R>(psi, i | (int64_t(1) << bit));
+    s00 += a.x * a.x + a.y * a.y;
+    s11 += b.x * b.x + b.y * b.y;
+    sre += a.x * b.x + a.y * b.y;
+    sim += a.y * b.x - a.x * b.y;
+  }
+  const R v[4] = {s00, s11, sre, sim};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double t = block_sum((double)v[k], sh);
+    if (threadIdx.x == 0) partials[(int64_t)blockIdx.x * 4 + k] = t;
+  }
+}
+
 // ----------------------------------------------------------------- norm / inner
 template <typename R>
 __global__ void k_inner_re(const typename C2<R>::T* a, const typename C2<R>::T* b, int64_t N,
@@ -480,6 +504,33 @@ extern "C" int tq_sv_expect_z_all(const void* psi, int n, int dtype, double* out
     k_expect_z<double><<<(unsigned)nb, 256, 0, s>>>((const double2*)psi, n, lch, (double*)ws);
   k_finalize<<<n, 1024, 0, s>>>((const double*)ws, (int)nb, n, out_dev);
   TQ_CHECK_LAUNCH("tq_sv_expect_z_all");
+  return TQ_OK;
+}
+
+extern "C" size_t tq_sv_qubit_rdm_workspace_bytes(int n) {
+  if (n < 1 || n > TQ_MAX_QUBITS) return 0;
+  return sizeof(double) * 4 * (size_t)red_blocks(n - 1);
+}
+
+extern "C" int tq_sv_qubit_rdm(const void* psi, int n, int dtype, int qubit, double* out_dev, void* ws,
+                               size_t ws_bytes, void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if ((rc = check_qubit(n, qubit))) return rc;
+  if (!psi || !out_dev) return fail(TQ_ERR_ARG, "tq_sv_qubit_rdm: NULL pointer");
+  const size_t need = tq_sv_qubit_rdm_workspace_bytes(n);
+  if (!ws || ws_bytes < need)
+    return fail(TQ_ERR_WORKSPACE, "tq_sv_qubit_rdm: workspace of %zu bytes < %zu", ws_bytes, need);
+  const int nb = red_blocks(n - 1);
+  const int64_t half = int64_t(1) << (n - 1);
+  const int bit = tq_bit(n, qubit);
+  cudaStream_t s = STREAM(stream);
+  if (dtype == TQ_C64)
+    k_qubit_rdm<float><<<nb, 256, 0, s>>>((const float2*)psi, half, bit, (double*)ws);
+  else
+    k_qubit_rdm<double><<<nb, 256, 0, s>>>((const double2*)psi, half, bit, (double*)ws);
+  k_finalize<<<4, 1024, 0, s>>>((const double*)ws, nb, 4, out_dev);
+  TQ_CHECK_LAUNCH("tq_sv_qubit_rdm");
   return TQ_OK;
 }
 

@@ -18,8 +18,14 @@ Differences from the reference, kept deliberately and documented:
   * states are complex64 by default (complex128 with dtype="complex128");
   * the shot RNG is a seeded counter-based generator (``seed=`` option or
     engine ``seed``), the reference draws from an unseeded numpy RNG;
-  * noise / Kraus / pulse ops raise NotImplementedError instead of running
-    the reference's host-side approximations.
+  * Kraus channels run as the reference's stochastic unravelling
+    (apply_kraus_statevector) with the Born weights from one device reduction
+    (the qubit's 2x2 reduced density matrix); an op without `status` draws it
+    from the engine's seeded generator instead of Python's `random`;
+  * use_noise (readout calibration matrices / depolarizing mixing of the
+    sampled distribution, Z attenuation of expectations; engine.py:386-410,
+    466-470, 488-494) is applied on the device;
+  * pulse ops raise NotImplementedError.
 """
 from __future__ import annotations
 
@@ -30,7 +36,7 @@ import numpy as np
 import torch
 
 from . import kernels as K
-from .ir import Gate, lower_ops
+from .ir import ATTENUATED, Gate, lower_ops
 
 _DTYPES = {"complex64": torch.complex64, "complex128": torch.complex128, torch.complex64: torch.complex64,
            torch.complex128: torch.complex128}
@@ -109,12 +115,26 @@ class GpuStatevectorEngine:
             return t
         return K.init_statevector(n, dtype=self.dtype, device=self.device)
 
-    def _execute(self, psi: torch.Tensor, gates: list[Gate]) -> torch.Tensor:
+    def _execute_unitary(self, psi: torch.Tensor, gates: list[Gate]) -> torch.Tensor:
         if self.fusion == "plain" or not gates:
             return execute_plain(psi, gates)
         from . import program
 
         return program.execute_fused(psi, gates)
+
+    def _execute(self, psi: torch.Tensor, gates: list[Gate]) -> torch.Tensor:
+        """Gate segments between Kraus channels run fused (or plain); each
+        channel is one stochastic step on the device state."""
+        seg: list[Gate] = []
+        for g in gates:
+            if g.kind != "kraus":
+                seg.append(g)
+                continue
+            psi = self._execute_unitary(psi, seg)
+            seg = []
+            status = g.status if g.status is not None else float(self._seed_rng.random())
+            K.apply_kraus(psi, g.kraus, g.qubits[0], status)
+        return self._execute_unitary(psi, seg)
 
     def simulate(self, circuit, mode: str = "state") -> tuple[torch.Tensor, list[int]]:
         """Final device state and measured qubits."""
@@ -130,23 +150,25 @@ class GpuStatevectorEngine:
     # ------------------------------------------------------------ engine API
     def run(self, circuit, shots: int | None = None, **kwargs: Any) -> Dict[str, Any]:
         shots = int(shots or 0)
-        if bool(kwargs.get("use_noise", False)):
-            raise NotImplementedError("use_noise (approximate noise) is not part of the GPU statevector engine")
+        use_noise = bool(kwargs.get("use_noise", False))
+        noise = (kwargs.get("noise") or {}) if use_noise else None
         n = int(getattr(circuit, "num_qubits", 0))
         psi, measures = self.simulate(circuit, mode="run")
         if shots > 0 and measures:
             seed = kwargs.get("seed")
             if seed is None:
                 seed = int(self._seed_rng.integers(0, 2**63 - 1))
-            idx = K.sample(psi, shots, int(seed)).cpu().numpy()
+            src = _noisy_amplitudes(psi, n, noise) if use_noise else psi
+            idx = K.sample(src, shots, int(seed)).cpu().numpy()
             return {"result": K.counts_from_indices(idx, n),
                     "metadata": {"shots": shots, "backend": getattr(self.backend, "name", "pytorch"),
                                  "three_level": bool(kwargs.get("three_level", False))}}
         expectations: Dict[str, float] = {}
         if measures:
             z = K.expect_z_all(psi).cpu().numpy()
+            att = _z_attenuation(circuit, noise, n) if use_noise else None
             for q in measures:
-                expectations[f"Z{q}"] = float(z[q])
+                expectations[f"Z{q}"] = float(z[q]) * (att[q] if att is not None else 1.0)
         return {"expectations": expectations,
                 "metadata": {"shots": shots, "backend": getattr(self.backend, "name", "pytorch")}}
 
@@ -193,6 +215,64 @@ class GpuStatevectorEngine:
     def energy(self, circuit, hamiltonian) -> float:
         """Re <psi|H|psi> for a Pauli-sum H, FP64 accumulation."""
         return self.expval(circuit, hamiltonian)
+
+
+def _z_attenuation(circuit, noise: dict, n: int) -> list[float]:
+    """Per-qubit <Z> factor of use_noise (engine.py:50, 56-143, _attenuate
+    :488-494): each gate multiplies the factor of every wire it touches by
+    max(0, 1 - 4p/3) for depolarizing noise; other noise types leave 1."""
+    att = [1.0] * n
+    if str((noise or {}).get("type", "")).lower() != "depolarizing":
+        return att
+    f = max(0.0, 1.0 - 4.0 * float(noise.get("p", 0.0)) / 3.0)
+    ucache = getattr(circuit, "_unitary_cache", {}) or {}
+    for op in getattr(circuit, "ops", []):
+        if not isinstance(op, (list, tuple)) or not op or op[0] not in ATTENUATED:
+            continue
+        name = op[0]
+        if name in ("h", "rz", "rx", "ry", "x", "s", "sdg"):
+            wires = [int(op[1])]
+        elif name == "unitary":
+            if len(op) == 3 and ucache.get(str(op[2])) is not None:
+                wires = [int(op[1])]
+            elif len(op) == 4 and ucache.get(str(op[3])) is not None:
+                wires = [int(op[1]), int(op[2])]
+            else:
+                continue
+        else:
+            wires = [int(op[1]), int(op[2])]
+        for q in wires:
+            att[q] *= f
+    return att
+
+
+def _noisy_amplitudes(psi: torch.Tensor, n: int, noise: dict) -> torch.Tensor:
+    """Amplitudes whose squared moduli are the use_noise sampling distribution
+    (engine.py:386-410): |psi|^2, then the readout calibration kron(A_0, ...,
+    A_{n-1}) applied qubit by qubit as 2x2 maps on the device, or depolarizing
+    mixing (1 - a) p + a / 2^n with a = min(1, 4p/3); clamped to [0, 1] and
+    renormalised (uniform if everything vanished)."""
+    probs = K.probabilities(psi).to(torch.float64)
+    ntype = str(noise.get("type", "")).lower()
+    if ntype == "readout":
+        cals = noise.get("cals", {}) or {}
+        pc = torch.complex(probs, torch.zeros_like(probs))
+        for q in range(n):
+            m = cals.get(q)
+            if m is None:
+                continue
+            K.apply_1q(pc, np.asarray(m.detach().cpu().numpy() if hasattr(m, "detach") else m,
+                                      dtype=np.complex128).reshape(2, 2), q)
+        probs = pc.real.contiguous()
+    elif ntype == "depolarizing":
+        a = max(0.0, min(1.0, 4.0 * float(noise.get("p", 0.0)) / 3.0))
+        probs = (1.0 - a) * probs + a / float(1 << n)
+    probs = probs.clamp(0.0, 1.0)
+    tot = float(probs.sum().item())
+    probs = probs / (tot if tot > 1e-12 else 1.0)
+    tot = float(probs.sum().item())
+    probs = probs / tot if tot > 0 else torch.full_like(probs, 1.0 / float(1 << n))
+    return torch.complex(probs.sqrt(), torch.zeros_like(probs)).to(psi.dtype)
 
 
 def _differentiable_angles(circuit) -> bool:

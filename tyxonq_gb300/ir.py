@@ -19,10 +19,13 @@ import numpy as np
 from . import gates as G
 
 RUN_GATES = {"h", "rz", "rx", "ry", "cx", "cry", "cz", "iswap", "swap", "rxx", "ryy", "rzz", "x", "s", "sdg",
-             "measure_z", "barrier", "project_z", "reset", "unitary"}
+             "measure_z", "barrier", "project_z", "reset", "unitary", "kraus"}
 STATE_GATES = RUN_GATES - {"cry", "measure_z", "barrier"}
 EXTENDED_GATES = {"y", "z", "t", "tdg", "cy", "phase", "cnot"}
-UNSUPPORTED = {"kraus", "pulse", "pulse_inline"}
+UNSUPPORTED = {"pulse", "pulse_inline"}
+# ops that feed the reference's use_noise Z attenuation (engine.py:56-140, _attenuate :488-494)
+ATTENUATED = {"h", "rz", "rx", "ry", "cx", "cry", "cz", "iswap", "swap", "rxx", "ryy", "rzz", "x", "s", "sdg",
+              "unitary"}
 
 # Pauli generator of each rotation: U(a) = exp(-i a/2 P)
 ROTATION_GENERATORS = {"rx": "X", "ry": "Y", "rz": "Z", "rxx": "XX", "ryy": "YY", "rzz": "ZZ"}
@@ -33,7 +36,8 @@ class Gate:
     """One device gate.
 
     kind: 'u1' dense 2x2 | 'd1' diagonal 2x2 | 'u2' dense 4x4 | 'cx' | 'cz' |
-          'swap' | 'uk' dense 2^k | 'prot' Pauli rotation | 'proj' Z projection
+          'swap' | 'uk' dense 2^k | 'prot' Pauli rotation | 'proj' Z projection |
+          'kraus' one-qubit channel (kraus: operator list, status: float or None)
     qubits: target qubits, first = most significant matrix index bit.
     mat: complex128 matrix (u1/d1/u2/uk; d1 stores the 2x2 diagonal matrix).
     rot: (name, angle, source) for parametrised rotations, else None; `source`
@@ -46,6 +50,8 @@ class Gate:
     rot: tuple | None = None
     keep: int = 0
     pauli: tuple | None = None  # ((q, 'X'|'Y'|'Z'), ...) for kind 'prot'
+    kraus: tuple | None = None  # 2x2 operators of kind 'kraus'
+    status: float | None = None
 
 
 def _angle(x: Any) -> float:
@@ -115,6 +121,15 @@ def lower_ops(circuit: Any, mode: str = "state", extended: bool = False) -> tupl
             a, b = int(op[1]), int(op[2])
             if a != b:
                 out.append(Gate("u2", (a, b), G.gate_iswap_4x4() if name == "iswap" else G.gate_cy_4x4()))
+        elif name == "kraus":
+            # ("kraus", qubit, key[, status]) with operators in circuit._kraus_cache
+            # (engine.py:145-155); an unknown key is skipped as there
+            ops_k = (getattr(circuit, "_kraus_cache", {}) or {}).get(str(op[2]))
+            if ops_k is None:
+                continue
+            mats = tuple(np.asarray(k.detach().cpu().numpy() if hasattr(k, "detach") else k,
+                                    dtype=np.complex128).reshape(2, 2) for k in ops_k)
+            out.append(Gate("kraus", (int(op[1]),), kraus=mats, status=float(op[3]) if len(op) > 3 else None))
         elif name == "measure_z":
             measures.append(int(op[1]))
         elif name == "barrier":

@@ -10,6 +10,7 @@ complex128 CUDA tensors of length 2^n.
 from __future__ import annotations
 
 import ctypes
+import math
 import threading
 from typing import Sequence
 
@@ -230,6 +231,37 @@ def norm2(psi: torch.Tensor) -> torch.Tensor:
     p, cap = _ws(lib.tq_sv_norm_workspace_bytes(n), psi.device)
     nat.call("tq_sv_norm2", _ptr(psi), n, dtype_tag(psi), _ptr(out), p, cap, stream_ptr(psi.device))
     return out
+
+
+def qubit_rdm(psi: torch.Tensor, qubit: int) -> np.ndarray:
+    """Unnormalised 2x2 reduced density matrix of `qubit` (host complex128)."""
+    n = _check_state(psi)
+    out = torch.empty(4, dtype=torch.float64, device=psi.device)
+    lib = nat.load()
+    p, cap = _ws(lib.tq_sv_qubit_rdm_workspace_bytes(n), psi.device)
+    nat.call("tq_sv_qubit_rdm", _ptr(psi), n, dtype_tag(psi), int(qubit), _ptr(out), p, cap, stream_ptr(psi.device))
+    r = out.cpu().numpy()
+    return np.array([[r[0], r[2] + 1j * r[3]], [r[2] - 1j * r[3], r[1]]], dtype=np.complex128)
+
+
+def apply_kraus(psi: torch.Tensor, ops, qubit: int, status: float) -> int:
+    """One stochastic Kraus step (apply_kraus_statevector,
+    tyxonq/libs/quantum_library/kernels/statevector.py:132-218): Born weights
+    p_i = ||K_i psi||^2 from the qubit's reduced density matrix, the first i
+    whose cumulative normalised weight reaches `status` (0 if none does), then
+    psi <- K_i psi / sqrt(p_i).  Returns the chosen index."""
+    rho = qubit_rdm(psi, qubit)
+    mats = [np.asarray(k.detach().cpu().numpy() if hasattr(k, "detach") else k, dtype=np.complex128).reshape(2, 2)
+            for k in ops]
+    p = np.array([float(np.real(np.trace(m @ rho @ m.conj().T))) for m in mats])
+    cum = np.cumsum(p / p.sum())
+    sel = 0
+    for i, c in enumerate(cum):
+        if status <= float(c) and p[i] > 0:  # a zero-weight operator would leave a zero state
+            sel = i
+            break
+    apply_1q(psi, mats[sel] / math.sqrt(p[sel]), qubit)
+    return sel
 
 
 def inner_re(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:

@@ -681,6 +681,8 @@ def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int
     """Plan and encode a forward program.  params: gate index -> (pidx, pscale)
     for gates whose angle is read from device theta at run time.  staged:
     register-staged passes (default when the tile has >= 9 bits)."""
+    if any(g.kind == "kraus" for g in gates):
+        raise NotImplementedError("Kraus channels are stochastic steps between programs (GpuStatevectorEngine)")
     gates = [_canon(g) for g in gates]
     if t is None:
         t = default_tile_bits(n, dtype)
