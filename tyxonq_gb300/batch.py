@@ -58,7 +58,8 @@ class Schedule:
     large: str = "waves"  # instances above res1_max: "waves" (L2-resident grid-wide phases) or "cta"
     wave_t: int = 12
     wave_hbits: int = 12
-    wave_budget: int = 96 << 20
+    wave_budget: int = 64 << 20  # per lane
+    wave_lanes: int = 2  # waves in flight at once, each lane on its own stream
     wave_max_ops: int = 256
 
     @classmethod
@@ -245,6 +246,7 @@ class BatchedVQE:
 
             sc = self.sched
             self.waves = WavePlan(wave_entries, dtype, dev, t=sc.wave_t, hbits=sc.wave_hbits, budget=sc.wave_budget,
+                                  lanes=sc.wave_lanes,
                                   max_ops=sc.wave_max_ops)
             self.n_structures += self.waves.n_structures
         lib = nat.load()
@@ -340,8 +342,17 @@ class BatchedVQE:
                      P(self.energies.data_ptr()), P(self.grads.data_ptr()),
                      P(self.counters.data_ptr() + 4 * k), s)
         if self.waves is not None:
+            lanes = [main]
+            if self.waves.lanes > 1:
+                if getattr(self, "_lane_streams", None) is None:
+                    self._lane_streams = [torch.cuda.Stream(self.device) for _ in range(self.waves.lanes - 1)]
+                for ls in self._lane_streams:
+                    ls.wait_stream(main)
+                lanes += self._lane_streams
             self.waves.launch(self.groups_dev, self.terms_dev, self.theta, self.energies, self.grads,
-                              ctypes.c_void_p(main.cuda_stream))
+                              ctypes.c_void_p(main.cuda_stream), [ctypes.c_void_p(x.cuda_stream) for x in lanes])
+            for ls in lanes[1:]:
+                main.wait_stream(ls)
         if side is not main:
             main.wait_stream(side)
 

@@ -415,7 +415,7 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
     TQ_CHECK_LAUNCH("tq_wave_run (H psi)");
     return TQ_OK;
   }
-  if (t < 9 || t > (sizeof(R) == 4 ? 13 : 12)) return fail(TQ_ERR_ARG, "tq_wave_run: t=%d", t);
+  if (t < 9 || t > (sizeof(R) == 4 && kind == 0 ? 13 : 12)) return fail(TQ_ERR_ARG, "tq_wave_run: t=%d", t);
   const int threads = 1 << (t - kRB);
   const int grid = n_items;
   if (kind == 0) {

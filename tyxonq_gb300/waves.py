@@ -57,10 +57,13 @@ def _dev(arr: np.ndarray, device) -> torch.Tensor:
 
 class WavePlan:
     def __init__(self, entries, dtype, device, t: int = 12, hbits: int = 12, budget: int = 48 << 20,
-                 max_ops: int = 256):
+                 max_ops: int = 256, lanes: int = 1):
         """entries: list of dicts with keys idx (instance index), n, gates,
         params, key (structure key), theta_off, grad_offset, basis,
-        group_begin, group_count."""
+        group_begin, group_count.  Waves are dealt round-robin to `lanes`
+        independent launch sequences with disjoint pool and partial ranges,
+        which may run on separate streams (each lane's wave fits `budget`)."""
+        self.lanes = max(1, int(lanes))
         self.dtype = dtype
         self.dt = 0 if dtype == torch.complex64 else 1
         self.t = t
@@ -91,13 +94,17 @@ class WavePlan:
             waves.append(cur)
         self.waves = waves
         items, launches, rows = [], [], []
-        pool_need = part_need = 0
-        for wv in waves:
+        item_lane, row_lane, self.launch_lanes = [], [], []
+        lane_pool = [0] * self.lanes
+        lane_part = [0] * self.lanes
+        for wi, wv in enumerate(waves):
+            lane = wi % self.lanes
+            n_items0, n_rows0, n_launch0 = len(items), len(rows), len(launches)
             off = 0
             for e in wv:
                 e["psi_off"], e["lam_off"] = off, off + (1 << e["n"])
                 off += 2 << e["n"]
-            pool_need = max(pool_need, off)
+            lane_pool[lane] = max(lane_pool[lane], off)
             part = 0
             # energy partial slots first, then gradient partials
             for e in wv:
@@ -139,7 +146,7 @@ class WavePlan:
                     for kk, slot, coef in pslots:
                         grad_rows.append((base + kk, ntile, nops, coef, e["grad_offset"] + slot))
                 launches.append(("run", 2, b, len(items) - b))
-            part_need = max(part_need, part)
+            lane_part[lane] = max(lane_part[lane], part)
             erow = [(e["epart"], 1 << (e["n"] - min(hbits, e["n"])), 1, 1.0, e["idx"]) for e in wv]
             rb = len(rows)
             rows += erow
@@ -154,13 +161,24 @@ class WavePlan:
                 rb = len(rows)
                 rows += layers[lay]
                 launches.append(("reduce_g", rb, len(layers[lay])))
+            item_lane += [lane] * (len(items) - n_items0)
+            row_lane += [lane] * (len(rows) - n_rows0)
+            self.launch_lanes += [lane] * (len(launches) - n_launch0)
         self.launches = launches
         self.n_items = len(items)
+        pool_base = np.concatenate([[0], np.cumsum(lane_pool)]).astype(np.int64)
+        part_base = np.concatenate([[0], np.cumsum(lane_part)]).astype(np.int64)
+        pool_need, part_need = int(pool_base[-1]), int(part_base[-1])
         it = np.zeros(len(items), dtype=WAVE_ITEM_DTYPE)
         if items:
             cols = list(zip(*items))
             for name, col in zip(WAVE_ITEM_DTYPE.names, cols):
                 it[name] = col
+            il = np.asarray(item_lane)
+            it["psi_off"] += pool_base[il]
+            it["lam_off"] += pool_base[il]
+            it["part_off"] += part_base[il].astype(np.int32)
+        rows = [(r[0] + int(part_base[l]),) + tuple(r[1:]) for r, l in zip(rows, row_lane)]
         self.items_dev = _dev(it, device)
         r = np.array(rows, dtype=object) if rows else np.zeros((0, 5))
         self.r_first = torch.tensor([x[0] for x in rows] or [0], dtype=torch.int32, device=device)
@@ -232,10 +250,13 @@ class WavePlan:
         return {"fwd": fwd, "adj": adj}
 
     # ------------------------------------------------------------ execution
-    def launch(self, groups_dev, terms_dev, theta, energies, grads, stream) -> None:
+    def launch(self, groups_dev, terms_dev, theta, energies, grads, stream, lane_streams=None) -> None:
+        """Enqueue every launch; lane l's on lane_streams[l] when given, else all on `stream`."""
         P = ctypes.c_void_p
         isz = WAVE_ITEM_DTYPE.itemsize
-        for L in self.launches:
+        for L, lane in zip(self.launches, self.launch_lanes):
+            if lane_streams is not None:
+                stream = lane_streams[lane]
             if L[0] == "run":
                 _, kind, b, c = L
                 if c == 0:
