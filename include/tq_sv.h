@@ -346,11 +346,14 @@ typedef struct {
  * lam, gradient partials per item and parameter op).  Every pass keeps at
  * least 4 contiguous low bits (nlow >= 4); a forward (kind 0) or adjoint
  * (kind 2) pass holds at most max_pass_ops ops, which sizes the shared memory
- * of the launch.  Items whose pass breaks either rule are skipped. */
+ * of the launch.  Items whose pass breaks either rule are skipped.
+ * stage_bits: register bits per stage of the passes (forward 4; adjoint 3 or
+ * 4 -- a CTA has 2^(t - stage_bits) threads holding 2^stage_bits amplitudes
+ * of psi and of lam each; bits[stage_bits..3] of a tq_tile_stage are unused). */
 TQ_API int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
-                       const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
-                       const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,
-                       double* partials, int max_pass_ops, void* stream);
+                       int stage_bits, const tq_tile_pass* passes, const tq_tile_stage* stages,
+                       const tq_tile_op* ops, const tq_pauli_group* groups, const tq_pauli_term* terms,
+                       const double* theta, void* pool, double* partials, int max_pass_ops, void* stream);
 
 /* Fixed-order reductions of wave partials: out[k] (+)= scale[k] * sum of
  * partials[first[k] + j * stride[k]] for j < count[k]; accumulate != 0 adds. */

@@ -110,3 +110,22 @@ def test_new_theta_changes_results_consistently():
             e_ref, g_ref = _oracle(inst)
             assert abs(e[k] - e_ref) < 1e-10
             np.testing.assert_allclose(grads[k], g_ref, atol=1e-10)
+
+
+def test_three_bit_adjoint_stages_match_oracle():
+    """Wave adjoint with 3-bit register stages (8 amplitudes of psi and lam per thread)."""
+    from tyxonq_gb300.batch import BatchedVQE, Schedule
+
+    insts = _instances(6, 33, (14, 15))
+    sc = Schedule.default(torch.complex64)
+    sc.wave_adj_stage_bits = 3
+    bv = BatchedVQE(insts, dtype=torch.complex64, schedule=sc)
+    assert bv.waves is not None and bv.waves.adj_rb == 3
+    e, g = bv.run(np.concatenate([i.theta for i in insts]))
+    e = e.cpu().numpy()
+    grads = bv.split_grads(g.cpu().numpy())
+    for k, inst in enumerate(insts):
+        e_ref, g_ref = _oracle(inst)
+        norm = inst.H.one_norm()
+        assert abs(e[k] - e_ref) < 1e-5 * norm
+        np.testing.assert_allclose(grads[k], g_ref, atol=1e-4 * norm)

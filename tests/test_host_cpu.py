@@ -238,8 +238,10 @@ def _op_matrix_local(o, theta, t):
     return M
 
 
-def test_staged_adjoint_encoding_emulated_matches_oracle_gradient():
-    """Reverse sweep over register stages as the wave adjoint kernel runs it."""
+@pytest.mark.parametrize("rb", [3, 4])
+def test_staged_adjoint_encoding_emulated_matches_oracle_gradient(rb):
+    """Reverse sweep over register stages (rb bits, 2^rb amplitudes per thread)
+    as the wave adjoint kernel runs it."""
     from tyxonq_gb300.batch import structure_gates
     from tyxonq_gb300.workloads import batched_vqe
 
@@ -257,7 +259,7 @@ def test_staged_adjoint_encoding_emulated_matches_oracle_gradient():
     grad = np.zeros(inst.n_params)
     for s in P.plan_passes(rg, n, 9, max_ops=64):
         for pp in s.passes:
-            enc = P.encode_staged(n, [pp], rg, params=rparams, slots=slots)
+            enc = P.encode_staged(n, [pp], rg, params=rparams, slots=slots, rb=rb)
             pa = enc.passes[0]
             t = pa.t
             pos = [pa.pos[j] for j in range(t)]
@@ -267,17 +269,18 @@ def test_staged_adjoint_encoding_emulated_matches_oracle_gradient():
                 idx = np.array([base + sum(((j >> k) & 1) << pos[k] for k in range(t)) for j in range(1 << t)])
                 sp, sl = psi[idx], lam[idx]
                 for st in enc.stages_host[pa.op_begin:pa.op_end]:
-                    bits = [int(b) for b in st["bits"]]
+                    bits = [int(b) for b in st["bits"]][:rb]
+                    assert all(b >= 0 for b in bits) and all(int(b) == -1 for b in st["bits"][rb:])
                     rest = [b for b in range(t) if b not in bits]
                     ops = enc.ops_host[st["op_begin"]:st["op_end"]]
-                    mats = [_op_matrix_local(o, inst.theta, 4) for o in ops]
-                    for tid in range(1 << (t - 4)):
+                    mats = [_op_matrix_local(o, inst.theta, rb) for o in ops]
+                    for tid in range(1 << (t - rb)):
                         b0 = sum(((tid >> k) & 1) << b for k, b in enumerate(rest))
-                        ridx = np.array([b0 + sum(((i >> k) & 1) << bits[k] for k in range(4)) for i in range(16)])
+                        ridx = np.array([b0 + sum(((i >> k) & 1) << bits[k] for k in range(rb)) for i in range(1 << rb)])
                         x, y = sp[ridx], sl[ridx]
                         for o, M in zip(ops, mats):
                             if o["slot"] >= 0:
-                                i = np.arange(16)
+                                i = np.arange(1 << rb)
                                 on = (i & int(o["gcm"])) == int(o["gcm"])
                                 sg = np.array([-1 if bin(k & int(o["gzm"])).count("1") % 2 else 1 for k in i])
                                 v = (1j ** int(o["gny"])) * sg * x

@@ -82,7 +82,7 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_inner_workspace_bytes": (c_size_t, [c_int]),
     "tq_sv_inner_re": (c_int, [_P, _P, c_int, c_int, _P, _P, c_size_t, _P]),
     "tq_batch_smem_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
-    "tq_wave_run": (c_int, [c_int, c_int, _P, c_int, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, _P, c_int, _P]),
+    "tq_wave_run": (c_int, [c_int, c_int, _P, c_int, c_int, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, _P, c_int, _P]),
     "tq_wave_reduce": (c_int, [_P, _P, _P, _P, _P, _P, c_int, _P, c_int, _P]),
     "tq_batch_run": (c_int, [c_int, _P, _P, c_int, c_int, c_int, c_int, c_int, c_size_t, _P, _P, _P, _P, _P, _P,
                              _P, _P, _P, _P]),

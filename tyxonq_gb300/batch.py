@@ -61,6 +61,7 @@ class Schedule:
     wave_budget: int = 64 << 20  # per lane
     wave_lanes: int = 2  # waves in flight at once, each lane on its own stream
     wave_max_ops: int = 256
+    wave_adj_stage_bits: int = 4  # register bits per adjoint stage (3: 8 amplitudes of psi and of lam per thread)
 
     @classmethod
     def default(cls, dtype) -> "Schedule":
@@ -246,7 +247,7 @@ class BatchedVQE:
 
             sc = self.sched
             self.waves = WavePlan(wave_entries, dtype, dev, t=sc.wave_t, hbits=sc.wave_hbits, budget=sc.wave_budget,
-                                  lanes=sc.wave_lanes,
+                                  lanes=sc.wave_lanes, adj_stage_bits=sc.wave_adj_stage_bits,
                                   max_ops=sc.wave_max_ops)
             self.n_structures += self.waves.n_structures
         lib = nat.load()

@@ -31,61 +31,84 @@ __device__ __forceinline__ int pphys(int j) { return j + ((j >> 4) << 1); }
 __host__ __device__ __forceinline__ int padded_len(int t) { return (1 << t) + ((1 << t) >> 3); }
 
 // ------------------------------------------------------------------ register routines
-template <typename R, int K>
+template <typename R, int NR, int K>
 __device__ __forceinline__ void r_u1(cplx<R>* x, cplx<R> u0, cplx<R> u1, cplx<R> u2, cplx<R> u3) {
+  if constexpr (!((1 << K) < NR)) {
+    return;
+  } else {
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
     const int j = i | (1 << K);
     const cplx<R> a = x[i], b = x[j];
     x[i] = cfma(u1, b, cmul(u0, a));
     x[j] = cfma(u3, b, cmul(u2, a));
   }
+  }
 }
 
 // [[c, a01], [a10, c]] with real entries
-template <typename R, int K>
+template <typename R, int NR, int K>
 __device__ __forceinline__ void r_rr(cplx<R>* x, R c, R a01, R a10) {
+  if constexpr (!((1 << K) < NR)) {
+    return;
+  } else {
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
     const int j = i | (1 << K);
     const cplx<R> u = x[i], v = x[j];
     x[i] = cplx<R>(fma(a01, v.x, c * u.x), fma(a01, v.y, c * u.y));
     x[j] = cplx<R>(fma(a10, u.x, c * v.x), fma(a10, u.y, c * v.y));
   }
+  }
 }
 
 // [[c, i b01], [i b10, c]] with c, b01, b10 real
-template <typename R, int K>
+template <typename R, int NR, int K>
 __device__ __forceinline__ void r_ri(cplx<R>* x, R c, R b01, R b10) {
+  if constexpr (!((1 << K) < NR)) {
+    return;
+  } else {
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
     const int j = i | (1 << K);
     const cplx<R> u = x[i], v = x[j];
     x[i] = cplx<R>(fma(-b01, v.y, c * u.x), fma(b01, v.x, c * u.y));
     x[j] = cplx<R>(fma(-b10, u.y, c * v.x), fma(b10, u.x, c * v.y));
   }
+  }
 }
 
-template <typename R, int K>
+template <typename R, int NR, int K>
 __device__ __forceinline__ void r_d1(cplx<R>* x, cplx<R> d0, cplx<R> d1) {
+  if constexpr (!((1 << K) < NR)) {
+    return;
+  } else {
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) x[i] = cmul(((i >> K) & 1) ? d1 : d0, x[i]);
+  for (int i = 0; i < NR; ++i) x[i] = cmul(((i >> K) & 1) ? d1 : d0, x[i]);
+  }
 }
 
-template <typename R, int K>
+template <typename R, int NR, int K>
 __device__ __forceinline__ void r_dh(cplx<R>* x, cplx<R> d1) {
+  if constexpr (!((1 << K) < NR)) {
+    return;
+  } else {
 #pragma unroll
-  for (int i = 0; i < kNR; ++i)
+  for (int i = 0; i < NR; ++i)
     if ((i >> K) & 1) x[i] = cmul(d1, x[i]);
+  }
 }
 
-template <typename R, int A, int B>
+template <typename R, int NR, int A, int B>
 __device__ __forceinline__ void r_u2(cplx<R>* x, const tq_tile_op& o, bool adj) {
+  if constexpr (!((1 << A) < NR && (1 << B) < NR)) {
+    return;
+  } else {
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if (((i >> A) & 1) || ((i >> B) & 1)) continue;
     const int id[4] = {i, i | (1 << B), i | (1 << A), i | (1 << A) | (1 << B)};
     const cplx<R> v0 = x[id[0]], v1 = x[id[1]], v2 = x[id[2]], v3 = x[id[3]];
@@ -104,13 +127,17 @@ __device__ __forceinline__ void r_u2(cplx<R>* x, const tq_tile_op& o, bool adj) 
       x[id[r]] = acc;
     }
   }
+  }
 }
 
 // MODE 0 CX (control A, target B), 1 SWAP, 2 CZ
-template <typename R, int MODE, int A, int B>
+template <typename R, int NR, int MODE, int A, int B>
 __device__ __forceinline__ void r_perm(cplx<R>* x) {
+  if constexpr (!((1 << A) < NR && (1 << B) < NR)) {
+    return;
+  } else {
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if (((i >> A) & 1) || ((i >> B) & 1)) continue;
     if (MODE == 0) {
       const int p = i | (1 << A), q = p | (1 << B);
@@ -127,15 +154,19 @@ __device__ __forceinline__ void r_perm(cplx<R>* x) {
       x[q] = cplx<R>(-x[q].x, -x[q].y);
     }
   }
+  }
 }
 
 // exp(-i a/2 P) on register bits: flip mask XM (compile time), sign mask zm and
 // control mask cm (runtime), coefficients c (real part used) and w.
-template <typename R, int XM>
+template <typename R, int NR, int XM>
 __device__ __forceinline__ void r_prot(cplx<R>* x, uint32_t zm, uint32_t cm, cplx<R> c, cplx<R> w) {
+  if constexpr (!(XM < NR)) {
+    return;
+  } else {
   if (XM == 0) {
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) {
+    for (int i = 0; i < NR; ++i) {
       if ((i & cm) != cm) continue;
       const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
       x[i] = cmul(cplx<R>(c.x + sg * w.x, sg * w.y), x[i]);
@@ -143,7 +174,7 @@ __device__ __forceinline__ void r_prot(cplx<R>* x, uint32_t zm, uint32_t cm, cpl
   } else {
     constexpr int H = (XM & 8) ? 3 : (XM & 4) ? 2 : (XM & 2) ? 1 : 0;
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) {
+    for (int i = 0; i < NR; ++i) {
       if ((i >> H) & 1) continue;
       const int j = i ^ XM;
       if ((i & cm) != cm) continue;
@@ -154,58 +185,62 @@ __device__ __forceinline__ void r_prot(cplx<R>* x, uint32_t zm, uint32_t cm, cpl
       x[j] = cfma(cplx<R>(w.x * si, w.y * si), a, cplx<R>(c.x * b.x, c.x * b.y));
     }
   }
+  }
 }
 
-template <typename R>
+template <typename R, int NR>
 __device__ __forceinline__ void r_u2_dispatch(cplx<R>* x, const tq_tile_op& o, bool adj) {
   switch (o.a * 4 + o.b) {
-    case 1: r_u2<R, 0, 1>(x, o, adj); break;
-    case 2: r_u2<R, 0, 2>(x, o, adj); break;
-    case 3: r_u2<R, 0, 3>(x, o, adj); break;
-    case 4: r_u2<R, 1, 0>(x, o, adj); break;
-    case 6: r_u2<R, 1, 2>(x, o, adj); break;
-    case 7: r_u2<R, 1, 3>(x, o, adj); break;
-    case 8: r_u2<R, 2, 0>(x, o, adj); break;
-    case 9: r_u2<R, 2, 1>(x, o, adj); break;
-    case 11: r_u2<R, 2, 3>(x, o, adj); break;
-    case 12: r_u2<R, 3, 0>(x, o, adj); break;
-    case 13: r_u2<R, 3, 1>(x, o, adj); break;
-    case 14: r_u2<R, 3, 2>(x, o, adj); break;
+    case 1: r_u2<R, NR, 0, 1>(x, o, adj); break;
+    case 2: r_u2<R, NR, 0, 2>(x, o, adj); break;
+    case 3: r_u2<R, NR, 0, 3>(x, o, adj); break;
+    case 4: r_u2<R, NR, 1, 0>(x, o, adj); break;
+    case 6: r_u2<R, NR, 1, 2>(x, o, adj); break;
+    case 7: r_u2<R, NR, 1, 3>(x, o, adj); break;
+    case 8: r_u2<R, NR, 2, 0>(x, o, adj); break;
+    case 9: r_u2<R, NR, 2, 1>(x, o, adj); break;
+    case 11: r_u2<R, NR, 2, 3>(x, o, adj); break;
+    case 12: r_u2<R, NR, 3, 0>(x, o, adj); break;
+    case 13: r_u2<R, NR, 3, 1>(x, o, adj); break;
+    case 14: r_u2<R, NR, 3, 2>(x, o, adj); break;
     default: break;
   }
 }
 
-template <typename R>
+template <typename R, int NR>
 __device__ __forceinline__ void r_prot_dispatch(cplx<R>* x, uint32_t xm, uint32_t zm, uint32_t cm, cplx<R> c,
                                                 cplx<R> w) {
-  switch (xm & 15) {
-    case 0: r_prot<R, 0>(x, zm, cm, c, w); break;
-    case 1: r_prot<R, 1>(x, zm, cm, c, w); break;
-    case 2: r_prot<R, 2>(x, zm, cm, c, w); break;
-    case 3: r_prot<R, 3>(x, zm, cm, c, w); break;
-    case 4: r_prot<R, 4>(x, zm, cm, c, w); break;
-    case 5: r_prot<R, 5>(x, zm, cm, c, w); break;
-    case 6: r_prot<R, 6>(x, zm, cm, c, w); break;
-    case 7: r_prot<R, 7>(x, zm, cm, c, w); break;
-    case 8: r_prot<R, 8>(x, zm, cm, c, w); break;
-    case 9: r_prot<R, 9>(x, zm, cm, c, w); break;
-    case 10: r_prot<R, 10>(x, zm, cm, c, w); break;
-    case 11: r_prot<R, 11>(x, zm, cm, c, w); break;
-    case 12: r_prot<R, 12>(x, zm, cm, c, w); break;
-    case 13: r_prot<R, 13>(x, zm, cm, c, w); break;
-    case 14: r_prot<R, 14>(x, zm, cm, c, w); break;
-    default: r_prot<R, 15>(x, zm, cm, c, w); break;
+  switch (xm & (NR - 1)) {
+    case 0: r_prot<R, NR, 0>(x, zm, cm, c, w); break;
+    case 1: r_prot<R, NR, 1>(x, zm, cm, c, w); break;
+    case 2: r_prot<R, NR, 2>(x, zm, cm, c, w); break;
+    case 3: r_prot<R, NR, 3>(x, zm, cm, c, w); break;
+    case 4: r_prot<R, NR, 4>(x, zm, cm, c, w); break;
+    case 5: r_prot<R, NR, 5>(x, zm, cm, c, w); break;
+    case 6: r_prot<R, NR, 6>(x, zm, cm, c, w); break;
+    case 7: r_prot<R, NR, 7>(x, zm, cm, c, w); break;
+    case 8: r_prot<R, NR, 8>(x, zm, cm, c, w); break;
+    case 9: r_prot<R, NR, 9>(x, zm, cm, c, w); break;
+    case 10: r_prot<R, NR, 10>(x, zm, cm, c, w); break;
+    case 11: r_prot<R, NR, 11>(x, zm, cm, c, w); break;
+    case 12: r_prot<R, NR, 12>(x, zm, cm, c, w); break;
+    case 13: r_prot<R, NR, 13>(x, zm, cm, c, w); break;
+    case 14: r_prot<R, NR, 14>(x, zm, cm, c, w); break;
+    default: r_prot<R, NR, 15>(x, zm, cm, c, w); break;
   }
 }
 
 // ------------------------------------------------------------------ gradient routines
 // Im <lam|G|psi> over the 16 register amplitudes (x = psi, y = lam):
 // G|i> = [i & cm == cm] ph (-1)^{popc(i & zm)} |i ^ XM>  (register-bit masks).
-template <typename R, int XM>
+template <typename R, int NR, int XM>
 __device__ __forceinline__ R r_grad(const cplx<R>* x, const cplx<R>* y, uint32_t zm, uint32_t cm, cplx<R> ph) {
+  if constexpr (!(XM < NR)) {
+    return R(0);
+  } else {
   R acc = 0;
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if ((i & cm) != cm) continue;
     const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
     const cplx<R> v = cmul(ph, x[i]);
@@ -213,40 +248,44 @@ __device__ __forceinline__ R r_grad(const cplx<R>* x, const cplx<R>* y, uint32_t
     acc += sg * (l.x * v.y - l.y * v.x);
   }
   return acc;
+  }
 }
 
-template <typename R>
+template <typename R, int NR>
 __device__ __forceinline__ R r_grad_dispatch(const cplx<R>* x, const cplx<R>* y, const tq_tile_op& o) {
   const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
   const cplx<R> ph(re[o.gny & 3], im[o.gny & 3]);
   const uint32_t zm = o.gzm, cm = o.gcm;
-  switch (o.gxm & 15) {
-    case 0: return r_grad<R, 0>(x, y, zm, cm, ph);
-    case 1: return r_grad<R, 1>(x, y, zm, cm, ph);
-    case 2: return r_grad<R, 2>(x, y, zm, cm, ph);
-    case 3: return r_grad<R, 3>(x, y, zm, cm, ph);
-    case 4: return r_grad<R, 4>(x, y, zm, cm, ph);
-    case 5: return r_grad<R, 5>(x, y, zm, cm, ph);
-    case 6: return r_grad<R, 6>(x, y, zm, cm, ph);
-    case 7: return r_grad<R, 7>(x, y, zm, cm, ph);
-    case 8: return r_grad<R, 8>(x, y, zm, cm, ph);
-    case 9: return r_grad<R, 9>(x, y, zm, cm, ph);
-    case 10: return r_grad<R, 10>(x, y, zm, cm, ph);
-    case 11: return r_grad<R, 11>(x, y, zm, cm, ph);
-    case 12: return r_grad<R, 12>(x, y, zm, cm, ph);
-    case 13: return r_grad<R, 13>(x, y, zm, cm, ph);
-    case 14: return r_grad<R, 14>(x, y, zm, cm, ph);
-    default: return r_grad<R, 15>(x, y, zm, cm, ph);
+  switch (o.gxm & (NR - 1)) {
+    case 0: return r_grad<R, NR, 0>(x, y, zm, cm, ph);
+    case 1: return r_grad<R, NR, 1>(x, y, zm, cm, ph);
+    case 2: return r_grad<R, NR, 2>(x, y, zm, cm, ph);
+    case 3: return r_grad<R, NR, 3>(x, y, zm, cm, ph);
+    case 4: return r_grad<R, NR, 4>(x, y, zm, cm, ph);
+    case 5: return r_grad<R, NR, 5>(x, y, zm, cm, ph);
+    case 6: return r_grad<R, NR, 6>(x, y, zm, cm, ph);
+    case 7: return r_grad<R, NR, 7>(x, y, zm, cm, ph);
+    case 8: return r_grad<R, NR, 8>(x, y, zm, cm, ph);
+    case 9: return r_grad<R, NR, 9>(x, y, zm, cm, ph);
+    case 10: return r_grad<R, NR, 10>(x, y, zm, cm, ph);
+    case 11: return r_grad<R, NR, 11>(x, y, zm, cm, ph);
+    case 12: return r_grad<R, NR, 12>(x, y, zm, cm, ph);
+    case 13: return r_grad<R, NR, 13>(x, y, zm, cm, ph);
+    case 14: return r_grad<R, NR, 14>(x, y, zm, cm, ph);
+    default: return r_grad<R, NR, 15>(x, y, zm, cm, ph);
   }
 }
 
 // G flips bit K, Z factors only on K (sign w1 on the bit-K-set half):
 // Im(ph (sum conj(y_j) x_i + w1 sum conj(y_i) x_j)), i = j ^ (1 << K), bit K of i clear.
-template <typename R, int K>
+template <typename R, int NR, int K>
 __device__ __forceinline__ R g_pair(const cplx<R>* x, const cplx<R>* y, cplx<R> ph, R w1) {
+  if constexpr (!((1 << K) < NR)) {
+    return R(0);
+  } else {
   R ax = 0, ay = 0, bx = 0, by = 0;
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
     const int j = i | (1 << K);
     ax = fma(y[j].x, x[i].x, fma(y[j].y, x[i].y, ax));
@@ -256,14 +295,18 @@ __device__ __forceinline__ R g_pair(const cplx<R>* x, const cplx<R>* y, cplx<R> 
   }
   const R zx = fma(w1, bx, ax), zy = fma(w1, by, ay);
   return ph.x * zy + ph.y * zx;
+  }
 }
 
 // Diagonal G: weight w0 where bit K is clear, w1 where it is set.
-template <typename R, int K>
+template <typename R, int NR, int K>
 __device__ __forceinline__ R g_diag(const cplx<R>* x, const cplx<R>* y, cplx<R> ph, R w0, R w1) {
+  if constexpr (!((1 << K) < NR)) {
+    return R(0);
+  } else {
   R s0x = 0, s0y = 0, s1x = 0, s1y = 0;
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) {
       s1x = fma(y[i].x, x[i].x, fma(y[i].y, x[i].y, s1x));
       s1y = fma(y[i].x, x[i].y, fma(-y[i].y, x[i].x, s1y));
@@ -274,6 +317,7 @@ __device__ __forceinline__ R g_diag(const cplx<R>* x, const cplx<R>* y, cplx<R> 
   }
   const R zx = fma(w1, s1x, w0 * s0x), zy = fma(w1, s1y, w0 * s0y);
   return ph.x * zy + ph.y * zx;
+  }
 }
 
 // ------------------------------------------------------------------ compiled ops
@@ -284,11 +328,11 @@ enum RCode : int32_t {
   RC_RI = 9,     // + K: [[c, i b01], [i b10, c]]: m0.x, m1.y, m2.y
   RC_D = 13,     // + K: diag(m0, m1); a negative sign swaps the two
   RC_DH = 17,    // + K: diag(1, m1)
-  RC_CX = 21,    // + pair index (12 ordered pairs)
-  RC_SWAP = 33,
-  RC_CZ = 45,
-  RC_U2 = 57,    // dense 4x4 read from the op table
-  RC_PROT = 58,  // general Pauli rotation: c = m0, w = m1, masks from the op table
+  RC_CX = 21,    // + pair index 4 a + b (a != b)
+  RC_SWAP = 37,
+  RC_CZ = 53,
+  RC_U2 = 69,    // dense 4x4 read from the op table
+  RC_PROT = 70,  // general Pauli rotation: c = m0, w = m1, masks from the op table
 };
 enum RGCode : int32_t { RG_NONE = -1, RG_GEN = 0, RG_PAIR = 1, RG_DIAG = 5 };
 
@@ -306,8 +350,8 @@ struct __align__(16) ROp {
   R gw0, gw1;
 };
 
-// ordered pair (a, b), a != b, of register bits -> 0..11
-__device__ __forceinline__ int pair_index(int a, int b) { return a * 3 + (b < a ? b : b - 1); }
+// ordered pair (a, b), a != b, of register bits -> 4 a + b
+__device__ __forceinline__ int pair_index(int a, int b) { return 4 * a + b; }
 
 __device__ __forceinline__ bool one_bit(uint32_t m) { return m != 0 && (m & (m - 1)) == 0; }
 
@@ -513,22 +557,24 @@ __device__ __forceinline__ R rop_sign(const ROp<R>& r, uint64_t gbase, int tbase
   return par ? R(-1) : R(1);
 }
 
-#define TQ_RK_CASES(BASE, FN, ...)                          \
-  case BASE + 0: FN<R, 0>(x, __VA_ARGS__); if (NA == 2) FN<R, 0>(y, __VA_ARGS__); break; \
-  case BASE + 1: FN<R, 1>(x, __VA_ARGS__); if (NA == 2) FN<R, 1>(y, __VA_ARGS__); break; \
-  case BASE + 2: FN<R, 2>(x, __VA_ARGS__); if (NA == 2) FN<R, 2>(y, __VA_ARGS__); break; \
-  case BASE + 3: FN<R, 3>(x, __VA_ARGS__); if (NA == 2) FN<R, 3>(y, __VA_ARGS__); break;
+#define TQ_RK_CASES(BASE, FN, ...)                                                               \
+  case BASE + 0: FN<R, NR, 0>(x, __VA_ARGS__); if (NA == 2) FN<R, NR, 0>(y, __VA_ARGS__); break; \
+  case BASE + 1: FN<R, NR, 1>(x, __VA_ARGS__); if (NA == 2) FN<R, NR, 1>(y, __VA_ARGS__); break; \
+  case BASE + 2: FN<R, NR, 2>(x, __VA_ARGS__); if (NA == 2) FN<R, NR, 2>(y, __VA_ARGS__); break; \
+  case BASE + 3: FN<R, NR, 3>(x, __VA_ARGS__); if (NA == 2) FN<R, NR, 3>(y, __VA_ARGS__); break;
 
-#define TQ_PAIR_CASE(BASE, I, MODE, A, B) \
-  case BASE + I: r_perm<R, MODE, A, B>(x); if (NA == 2) r_perm<R, MODE, A, B>(y); break;
+#define TQ_PAIR_CASE(BASE, MODE, A, B) \
+  case BASE + 4 * A + B: r_perm<R, NR, MODE, A, B>(x); if (NA == 2) r_perm<R, NR, MODE, A, B>(y); break;
 #define TQ_PAIR_CASES(BASE, MODE)                                                                      \
-  TQ_PAIR_CASE(BASE, 0, MODE, 0, 1) TQ_PAIR_CASE(BASE, 1, MODE, 0, 2) TQ_PAIR_CASE(BASE, 2, MODE, 0, 3)  \
-  TQ_PAIR_CASE(BASE, 3, MODE, 1, 0) TQ_PAIR_CASE(BASE, 4, MODE, 1, 2) TQ_PAIR_CASE(BASE, 5, MODE, 1, 3)  \
-  TQ_PAIR_CASE(BASE, 6, MODE, 2, 0) TQ_PAIR_CASE(BASE, 7, MODE, 2, 1) TQ_PAIR_CASE(BASE, 8, MODE, 2, 3)  \
-  TQ_PAIR_CASE(BASE, 9, MODE, 3, 0) TQ_PAIR_CASE(BASE, 10, MODE, 3, 1) TQ_PAIR_CASE(BASE, 11, MODE, 3, 2)
+  TQ_PAIR_CASE(BASE, MODE, 0, 1) TQ_PAIR_CASE(BASE, MODE, 0, 2) TQ_PAIR_CASE(BASE, MODE, 0, 3)           \
+  TQ_PAIR_CASE(BASE, MODE, 1, 0) TQ_PAIR_CASE(BASE, MODE, 1, 2) TQ_PAIR_CASE(BASE, MODE, 1, 3)           \
+  TQ_PAIR_CASE(BASE, MODE, 2, 0) TQ_PAIR_CASE(BASE, MODE, 2, 1) TQ_PAIR_CASE(BASE, MODE, 2, 3)           \
+  TQ_PAIR_CASE(BASE, MODE, 3, 0) TQ_PAIR_CASE(BASE, MODE, 3, 1) TQ_PAIR_CASE(BASE, MODE, 3, 2)
 
-// Apply compiled op r to x (and to y when NA == 2) with sign s.
-template <typename R, int NA>
+// Apply compiled op r to x (and to y when NA == 2) with sign s; NR
+// amplitudes per array (2^stage bits).  Codes for register bits >= log2(NR)
+// never occur and compile to nothing.
+template <typename R, int NA, int NR>
 __device__ __forceinline__ void rop_apply(cplx<R>* x, cplx<R>* y, const ROp<R>& r,
                                           const tq_tile_op* __restrict__ ops, bool adj, R s) {
   switch (r.code) {
@@ -541,60 +587,139 @@ __device__ __forceinline__ void rop_apply(cplx<R>* x, cplx<R>* y, const ROp<R>& 
     TQ_PAIR_CASES(RC_CX, 0)
     TQ_PAIR_CASES(RC_SWAP, 1)
     TQ_PAIR_CASES(RC_CZ, 2)
-    case RC_U2: {
-      const tq_tile_op& o = ops[r.op];
-      r_u2_dispatch<R>(x, o, adj);
-      if (NA == 2) r_u2_dispatch<R>(y, o, adj);
-      break;
-    }
-    case RC_PROT: {
-      const tq_tile_op& o = ops[r.op];
-      const cplx<R> w(s * r.m[1].x, s * r.m[1].y);
-      r_prot_dispatch<R>(x, o.xm, o.zm, o.cm, r.m[0], w);
-      if (NA == 2) r_prot_dispatch<R>(y, o.xm, o.zm, o.cm, r.m[0], w);
-      break;
-    }
-    default: break;
+    default: break;  // RC_U2 / RC_PROT: cold path (s_cold_apply)
   }
 }
 
 // Gradient partial Im <y|G|x> of compiled op r (unsigned; the caller applies the op's sign).
-template <typename R>
+template <typename R, int NR>
 __device__ __forceinline__ R rop_grad(const cplx<R>* x, const cplx<R>* y, const ROp<R>& r,
                                       const tq_tile_op* __restrict__ ops) {
   switch (r.gcode) {
-    case RG_PAIR + 0: return g_pair<R, 0>(x, y, r.gph, r.gw0);
-    case RG_PAIR + 1: return g_pair<R, 1>(x, y, r.gph, r.gw0);
-    case RG_PAIR + 2: return g_pair<R, 2>(x, y, r.gph, r.gw0);
-    case RG_PAIR + 3: return g_pair<R, 3>(x, y, r.gph, r.gw0);
-    case RG_DIAG + 0: return g_diag<R, 0>(x, y, r.gph, r.gw0, r.gw1);
-    case RG_DIAG + 1: return g_diag<R, 1>(x, y, r.gph, r.gw0, r.gw1);
-    case RG_DIAG + 2: return g_diag<R, 2>(x, y, r.gph, r.gw0, r.gw1);
-    case RG_DIAG + 3: return g_diag<R, 3>(x, y, r.gph, r.gw0, r.gw1);
-    default: return r_grad_dispatch<R>(x, y, ops[r.op]);
+    case RG_PAIR + 0: return g_pair<R, NR, 0>(x, y, r.gph, r.gw0);
+    case RG_PAIR + 1: return g_pair<R, NR, 1>(x, y, r.gph, r.gw0);
+    case RG_PAIR + 2: return g_pair<R, NR, 2>(x, y, r.gph, r.gw0);
+    case RG_PAIR + 3: return g_pair<R, NR, 3>(x, y, r.gph, r.gw0);
+    case RG_DIAG + 0: return g_diag<R, NR, 0>(x, y, r.gph, r.gw0, r.gw1);
+    case RG_DIAG + 1: return g_diag<R, NR, 1>(x, y, r.gph, r.gw0, r.gw1);
+    case RG_DIAG + 2: return g_diag<R, NR, 2>(x, y, r.gph, r.gw0, r.gw1);
+    case RG_DIAG + 3: return g_diag<R, NR, 3>(x, y, r.gph, r.gw0, r.gw1);
+    default: return R(0);  // RG_GEN: cold path (s_cold_grad)
   }
 }
 
 // ------------------------------------------------------------------ stage mapping
 // Per-thread register <-> padded shared-memory index of register i for a stage
-// with register bits b[0..3] (ascending local positions).
+// with RB register bits b[0..RB) (ascending local positions).
+template <int RB>
 struct StageMap {
   int base;       // local index with all register bits zero
-  int m[kRB];     // 1 << bits[k]
+  int m[RB];      // 1 << bits[k]
   __device__ __forceinline__ int idx(int i) const {  // i is a compile-time constant at every call
-    return base | ((i & 1) ? m[0] : 0) | ((i & 2) ? m[1] : 0) | ((i & 4) ? m[2] : 0) | ((i & 8) ? m[3] : 0);
+    int v = base;
+#pragma unroll
+    for (int k = 0; k < RB; ++k) v |= ((i >> k) & 1) ? m[k] : 0;
+    return v;
   }
 };
 
-__device__ __forceinline__ StageMap stage_map(const tq_tile_stage& st, int tid) {
-  StageMap m;
+template <int RB>
+__device__ __forceinline__ StageMap<RB> stage_map(const tq_tile_stage& st, int tid) {
+  StageMap<RB> m;
   int b = tid;
 #pragma unroll
-  for (int k = 0; k < kRB; ++k) b = insz(b, st.bits[k]);
+  for (int k = 0; k < RB; ++k) b = insz(b, st.bits[k]);
   m.base = b;
 #pragma unroll
-  for (int k = 0; k < kRB; ++k) m.m[k] = 1 << st.bits[k];
+  for (int k = 0; k < RB; ++k) m.m[k] = 1 << st.bits[k];
   return m;
+}
+
+// Ops without a register routine: general dense 4x4 (RC_U2), Pauli rotations
+// with several flip bits or a control (RC_PROT), and general gradient
+// generators (RG_GEN).  The thread moves its registers to its own slots of the
+// shared-memory tile (no other thread touches them, so no barrier is needed),
+// applies the op there with runtime register-bit indices and reloads.
+template <typename R>
+__device__ __forceinline__ bool rop_is_cold(const ROp<R>& r) {
+  return r.code == RC_U2 || r.code == RC_PROT || r.gcode == RG_GEN;
+}
+
+template <int RB>
+__device__ __forceinline__ int slot_of(const StageMap<RB>& mp, int i) {
+  int v = mp.base;
+#pragma unroll
+  for (int k = 0; k < RB; ++k)
+    if ((i >> k) & 1) v |= mp.m[k];
+  return pphys(v);
+}
+
+template <typename R, int RB>
+__device__ void s_cold_apply(cplx<R>* s, const StageMap<RB>& mp, const tq_tile_op& o, const ROp<R>& r, bool adj,
+                             R sgn) {
+  constexpr int NR = 1 << RB;
+  if (r.code == RC_U2) {
+    const int A = o.a, B = o.b, plo = A < B ? A : B, phi = A < B ? B : A;
+    for (int q = 0; q < NR / 4; ++q) {
+      const int i = insz(insz(q, plo), phi);
+      const int id[4] = {slot_of<RB>(mp, i), slot_of<RB>(mp, i | (1 << B)), slot_of<RB>(mp, i | (1 << A)),
+                         slot_of<RB>(mp, i | (1 << A) | (1 << B))};
+      const cplx<R> v[4] = {s[id[0]], s[id[1]], s[id[2]], s[id[3]]};
+      for (int rr = 0; rr < 4; ++rr) {
+        cplx<R> acc(R(0), R(0));
+        for (int c = 0; c < 4; ++c) {
+          cplx<R> u = adj ? op_m<R>(o, 4 * c + rr) : op_m<R>(o, 4 * rr + c);
+          if (adj) u.y = -u.y;
+          acc = cfma(u, v[c], acc);
+        }
+        s[id[rr]] = acc;
+      }
+    }
+  } else if (r.code == RC_PROT) {
+    const cplx<R> c = r.m[0], w(sgn * r.m[1].x, sgn * r.m[1].y);
+    const uint32_t xm = o.xm & (NR - 1), zm = o.zm, cm = o.cm;
+    if (xm == 0) {
+      for (int i = 0; i < NR; ++i) {
+        if ((i & cm) != cm) continue;
+        const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
+        const int a = slot_of<RB>(mp, i);
+        s[a] = cmul(cplx<R>(c.x + sg * w.x, sg * w.y), s[a]);
+      }
+    } else {
+      const int h = 31 - __clz(xm);
+      for (int i = 0; i < NR; ++i) {
+        if ((i >> h) & 1) continue;
+        const int j = i ^ (int)xm;
+        if ((i & cm) != cm) continue;
+        const int ai = slot_of<RB>(mp, i), aj = slot_of<RB>(mp, j);
+        const cplx<R> a = s[ai], b = s[aj];
+        const R si = (__popc(i & zm) & 1) ? R(-1) : R(1);
+        const R sj = (__popc(j & zm) & 1) ? R(-1) : R(1);
+        s[ai] = cfma(cplx<R>(w.x * sj, w.y * sj), b, cplx<R>(c.x * a.x, c.x * a.y));
+        s[aj] = cfma(cplx<R>(w.x * si, w.y * si), a, cplx<R>(c.x * b.x, c.x * b.y));
+      }
+    }
+  }
+  // any other code of a cold record (a hot op with a general generator) is applied by the caller
+}
+
+// Im <lam|G|psi> over the thread's slots (sp = psi, sl = lam), G from the op's
+// generator masks: G|i> = [i & gcm == gcm] i^gny (-1)^{popc(i & gzm)} |i ^ gxm>.
+template <typename R, int RB>
+__device__ R s_cold_grad(const cplx<R>* sp, const cplx<R>* sl, const StageMap<RB>& mp, const tq_tile_op& o) {
+  constexpr int NR = 1 << RB;
+  const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
+  const cplx<R> ph(re[o.gny & 3], im[o.gny & 3]);
+  const uint32_t xm = o.gxm & (NR - 1), zm = o.gzm, cm = o.gcm;
+  R acc = 0;
+  for (int i = 0; i < NR; ++i) {
+    if ((i & cm) != cm) continue;
+    const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
+    const cplx<R> v = cmul(ph, sp[slot_of<RB>(mp, i)]);
+    const cplx<R> l = sl[slot_of<RB>(mp, i ^ (int)xm)];
+    acc += sg * (l.x * v.y - l.y * v.x);
+  }
+  return acc;
 }
 
 // ------------------------------------------------------------------ out-of-place forms
@@ -711,12 +836,12 @@ __device__ __forceinline__ void t_prot(const cplx<R>* a, cplx<R>* b, uint32_t zm
   case BASE + 1: FN<R, 1>(a, b, __VA_ARGS__); break;     \
   case BASE + 2: FN<R, 2>(a, b, __VA_ARGS__); break;     \
   case BASE + 3: FN<R, 3>(a, b, __VA_ARGS__); break;
-#define TQ_TPAIR_CASE(BASE, I, MODE, A, B) case BASE + I: t_perm<R, MODE, A, B>(a, b); break;
-#define TQ_TPAIR_CASES(BASE, MODE)                                                                         \
-  TQ_TPAIR_CASE(BASE, 0, MODE, 0, 1) TQ_TPAIR_CASE(BASE, 1, MODE, 0, 2) TQ_TPAIR_CASE(BASE, 2, MODE, 0, 3)  \
-  TQ_TPAIR_CASE(BASE, 3, MODE, 1, 0) TQ_TPAIR_CASE(BASE, 4, MODE, 1, 2) TQ_TPAIR_CASE(BASE, 5, MODE, 1, 3)  \
-  TQ_TPAIR_CASE(BASE, 6, MODE, 2, 0) TQ_TPAIR_CASE(BASE, 7, MODE, 2, 1) TQ_TPAIR_CASE(BASE, 8, MODE, 2, 3)  \
-  TQ_TPAIR_CASE(BASE, 9, MODE, 3, 0) TQ_TPAIR_CASE(BASE, 10, MODE, 3, 1) TQ_TPAIR_CASE(BASE, 11, MODE, 3, 2)
+#define TQ_TPAIR_CASE(BASE, MODE, A, B) case BASE + 4 * A + B: t_perm<R, MODE, A, B>(a, b); break;
+#define TQ_TPAIR_CASES(BASE, MODE)                                                                          \
+  TQ_TPAIR_CASE(BASE, MODE, 0, 1) TQ_TPAIR_CASE(BASE, MODE, 0, 2) TQ_TPAIR_CASE(BASE, MODE, 0, 3)            \
+  TQ_TPAIR_CASE(BASE, MODE, 1, 0) TQ_TPAIR_CASE(BASE, MODE, 1, 2) TQ_TPAIR_CASE(BASE, MODE, 1, 3)            \
+  TQ_TPAIR_CASE(BASE, MODE, 2, 0) TQ_TPAIR_CASE(BASE, MODE, 2, 1) TQ_TPAIR_CASE(BASE, MODE, 2, 3)            \
+  TQ_TPAIR_CASE(BASE, MODE, 3, 0) TQ_TPAIR_CASE(BASE, MODE, 3, 1) TQ_TPAIR_CASE(BASE, MODE, 3, 2)
 
 // b = (compiled forward op r) a, with sign s.
 template <typename R>
@@ -796,7 +921,7 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, ROp<R>* rops, bool reside
                                            uint64_t gbase) {
   for (int si = s0; si < s1; ++si) {
     const tq_tile_stage st = stages[si];
-    const StageMap m = stage_map(st, threadIdx.x);
+    const StageMap<kRB> m = stage_map<kRB>(st, threadIdx.x);
     cplx<R> x[kNR], x2[kNR];
 #pragma unroll
     for (int i = 0; i < kNR; ++i) x[i] = s[pphys(m.idx(i))];

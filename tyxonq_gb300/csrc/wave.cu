@@ -288,14 +288,15 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
 // ------------------------------------------------------------------ adjoint
 // Shared memory: psi tile | lam tile | offset table | the pass's compiled ops
 // (max_ops records, built at item start) | per-warp gradient partials
-// (max_ops x warps doubles).
-template <typename R>
-__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
+// (max_ops x warps, in R; summed over warps in FP64 in a fixed order).
+template <typename R, int RB>
+__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, RB == 3 ? 2 : 1)
     k_wave_adjoint(const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes,
                    const tq_tile_stage* __restrict__ stages, const tq_tile_op* __restrict__ ops,
                    const double* __restrict__ theta, void* pool, double* partials, int max_ops) {
   extern __shared__ __align__(16) unsigned char smem[];
   typedef typename C2<R>::T T2;
+  constexpr int NR = 1 << RB;  // amplitudes of psi (and of lam) per thread
   const int nwarps = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
@@ -311,13 +312,13 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
     unsigned char* tail = smem + 2 * PT * sizeof(cplx<R>);
     int64_t* hoff = reinterpret_cast<int64_t*>(tail);
     ROp<R>* rops = reinterpret_cast<ROp<R>*>(tail + w_hoff_bytes(P.t));
-    double* wpart = reinterpret_cast<double*>(tail + w_hoff_bytes(P.t) + (size_t)max_ops * sizeof(ROp<R>));
+    R* wpart = reinterpret_cast<R*>(tail + w_hoff_bytes(P.t) + (size_t)max_ops * sizeof(ROp<R>));
     T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
     T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
     const double* th = theta + I.theta_off;
     __syncthreads();
     w_hoff(hoff, P);
-    for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = 0.0;
+    for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = R(0);
     rops_build<R>(rops, ops, op0, op0 + nops, th, true, true);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
@@ -327,10 +328,10 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
     __syncthreads();
     for (int si = P.op_begin; si < P.op_end; ++si) {
       const tq_tile_stage st = stages[si];
-      const StageMap mp = stage_map(st, threadIdx.x);
-      cplx<R> x[kNR], y[kNR];
+      const StageMap<RB> mp = stage_map<RB>(st, threadIdx.x);
+      cplx<R> x[NR], y[NR];
 #pragma unroll
-      for (int i = 0; i < kNR; ++i) {
+      for (int i = 0; i < NR; ++i) {
         const int j = pphys(mp.idx(i));
         x[i] = sp[j];
         y[i] = sl[j];
@@ -338,16 +339,37 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
       for (int k = st.op_begin; k < st.op_end; ++k) {
         const ROp<R>& r = rops[k - op0];
         const R zs = rop_sign<R>(r, (uint64_t)base, mp.base);
+        R part = 0;
+        if (rop_is_cold(r)) {  // same for every thread: the record is shared
+#pragma unroll
+          for (int i = 0; i < NR; ++i) {
+            const int j = pphys(mp.idx(i));
+            sp[j] = x[i];
+            sl[j] = y[i];
+          }
+          const tq_tile_op& o = ops[r.op];
+          if (r.gcode != RG_NONE) part = zs * s_cold_grad<R, RB>(sp, sl, mp, o);
+          s_cold_apply<R, RB>(sp, mp, o, r, true, zs);
+          s_cold_apply<R, RB>(sl, mp, o, r, true, zs);
+#pragma unroll
+          for (int i = 0; i < NR; ++i) {
+            const int j = pphys(mp.idx(i));
+            x[i] = sp[j];
+            y[i] = sl[j];
+          }
+          if (r.code != RC_U2 && r.code != RC_PROT) rop_apply<R, 2, NR>(x, y, r, ops, true, zs);
+        } else {
+          if (r.gcode != RG_NONE) part = zs * rop_grad<R, NR>(x, y, r, ops);
+          rop_apply<R, 2, NR>(x, y, r, ops, true, zs);
+        }
         if (r.gcode != RG_NONE) {
-          R part = zs * rop_grad<R>(x, y, r, ops);
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
-          if (lane == 0) wpart[(k - op0) * nwarps + warp] = (double)part;
+          if (lane == 0) wpart[(k - op0) * nwarps + warp] = part;
         }
-        rop_apply<R, 2>(x, y, r, ops, true, zs);
       }
 #pragma unroll
-      for (int i = 0; i < kNR; ++i) {
+      for (int i = 0; i < NR; ++i) {
         const int j = pphys(mp.idx(i));
         sp[j] = x[i];
         sl[j] = y[i];
@@ -358,7 +380,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
     w_store<R>(sl, lam, base, hoff, P);
     for (int k = threadIdx.x; k < nops; k += blockDim.x) {
       double s = 0;
-      for (int w = 0; w < nwarps; ++w) s += wpart[k * nwarps + w];
+      for (int w = 0; w < nwarps; ++w) s += (double)wpart[k * nwarps + w];
       partials[I.part_off + k] = s;
     }
   }
@@ -385,13 +407,13 @@ static size_t fwd_smem(int t, int max_ops) {
   return padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + (size_t)max_ops * sizeof(ROp<R>);
 }
 template <typename R>
-static size_t adj_smem(int t, int max_ops) {
+static size_t adj_smem(int t, int rb, int max_ops) {
   return 2 * padded_len(t) * sizeof(cplx<R>) + w_hoff_bytes(t) + (size_t)max_ops * sizeof(ROp<R>) +
-         sizeof(double) * (size_t)max_ops * ((1 << (t - kRB)) / 32);
+         sizeof(R) * (size_t)max_ops * ((1 << (t - rb)) / 32);
 }
 
 template <typename R>
-static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, int hbits,
+static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, int hbits, int rb,
                        const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
                        const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,
                        double* partials, int max_ops, cudaStream_t s) {
@@ -415,8 +437,12 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
     TQ_CHECK_LAUNCH("tq_wave_run (H psi)");
     return TQ_OK;
   }
-  if (t < 9 || t > (sizeof(R) == 4 && kind == 0 ? 13 : 12)) return fail(TQ_ERR_ARG, "tq_wave_run: t=%d", t);
-  const int threads = 1 << (t - kRB);
+  if (t < 9 || t > (sizeof(R) == 4 ? 13 : 12)) return fail(TQ_ERR_ARG, "tq_wave_run: t=%d", t);
+  if (kind == 0 ? rb != kRB : (rb != 3 && rb != 4))
+    return fail(TQ_ERR_ARG, "tq_wave_run: %d register bits per stage (forward 4, adjoint 3 or 4)", rb);
+  const int threads = 1 << (t - rb);
+  if (threads > (sizeof(R) == 4 ? 512 : 256))
+    return fail(TQ_ERR_ARG, "tq_wave_run: t=%d with %d-bit stages needs %d threads per CTA", t, rb, threads);
   const int grid = n_items;
   if (kind == 0) {
     const size_t smem = fwd_smem<R>(t, max_ops);
@@ -425,11 +451,19 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
     if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");
     k_wave_forward<R><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool, max_ops);
   } else {
-    const size_t smem = adj_smem<R>(t, max_ops);
+    const size_t smem = adj_smem<R>(t, rb, max_ops);
     if (smem > 227 * 1024) return fail(TQ_ERR_ARG, "tq_wave_run: adjoint needs %zu B shared memory", smem);
-    cudaError_t e = cudaFuncSetAttribute(k_wave_adjoint<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = rb == 3 ? cudaFuncSetAttribute(k_wave_adjoint<R, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem)
+                            : cudaFuncSetAttribute(k_wave_adjoint<R, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");
-    k_wave_adjoint<R><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool, partials, max_ops);
+    if (rb == 3)
+      k_wave_adjoint<R, 3><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool, partials,
+                                                        max_ops);
+    else
+      k_wave_adjoint<R, 4><<<grid, threads, smem, s>>>(items, n_items, passes, stages, ops, theta, pool, partials,
+                                                        max_ops);
   }
   TQ_CHECK_LAUNCH("tq_wave_run");
   return TQ_OK;
@@ -440,9 +474,9 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
 using namespace tq;
 
 extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
-                           const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
-                           const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,
-                           double* partials, int max_pass_ops, void* stream) {
+                           int stage_bits, const tq_tile_pass* passes, const tq_tile_stage* stages,
+                           const tq_tile_op* ops, const tq_pauli_group* groups, const tq_pauli_term* terms,
+                           const double* theta, void* pool, double* partials, int max_pass_ops, void* stream) {
   if (dtype != TQ_C64 && dtype != TQ_C128) return fail(TQ_ERR_ARG, "tq_wave_run: bad dtype %d", dtype);
   if (kind < 0 || kind > 2) return fail(TQ_ERR_ARG, "tq_wave_run: bad kind %d", kind);
   if (n_items < 0) return fail(TQ_ERR_ARG, "tq_wave_run: negative item count");
@@ -453,10 +487,10 @@ extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n
   if (kind == 2 && !partials) return fail(TQ_ERR_ARG, "tq_wave_run: adjoint partials");
   if (kind != 1 && max_pass_ops < 1) return fail(TQ_ERR_ARG, "tq_wave_run: max_pass_ops %d < 1", max_pass_ops);
   cudaStream_t s = (cudaStream_t)stream;
-  return dtype == TQ_C64 ? wave_launch<float>(kind, items, n_items, t, hbits, passes, stages, ops, groups, terms,
-                                              theta, pool, partials, max_pass_ops, s)
-                         : wave_launch<double>(kind, items, n_items, t, hbits, passes, stages, ops, groups, terms,
-                                               theta, pool, partials, max_pass_ops, s);
+  return dtype == TQ_C64 ? wave_launch<float>(kind, items, n_items, t, hbits, stage_bits, passes, stages, ops, groups,
+                                              terms, theta, pool, partials, max_pass_ops, s)
+                         : wave_launch<double>(kind, items, n_items, t, hbits, stage_bits, passes, stages, ops,
+                                               groups, terms, theta, pool, partials, max_pass_ops, s);
 }
 
 extern "C" int tq_wave_reduce(const double* partials, const int32_t* first, const int32_t* count,

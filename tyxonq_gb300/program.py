@@ -612,7 +612,7 @@ class EncodedStaged:
 
 
 def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], params: dict | None = None,
-                  slots: dict | None = None) -> EncodedStaged:
+                  slots: dict | None = None, rb: int = STAGE_BITS) -> EncodedStaged:
     """Encode passes as register stages.  Forward (slots None): single-qubit
     runs merged, two-qubit gates kept as permutations / dense 4x4,
     parametrised gates as device-side rotations.  Adjoint (slots given, gates
@@ -644,7 +644,7 @@ def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], para
         op_bits = [tuple(loc[q] for q in active_qubits(g)) for g, _, _, _ in items]
         dep_bits = [tuple(loc[q] for q in g.qubits if q in loc) for g, _, _, _ in items]
         st_begin = len(stage_rows)
-        for bits, order in plan_stages(op_bits, t, dep_bits=dep_bits):
+        for bits, order in plan_stages(op_bits, t, rb=rb, dep_bits=dep_bits):
             reg = {b: k for k, b in enumerate(bits)}
             qreg = {q: reg[loc[q]] for q in qs if loc[q] in reg}
             ob = len(fields)
@@ -670,7 +670,7 @@ def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], para
         passes.append(p)
     st = np.zeros(len(stage_rows), dtype=STAGE_DTYPE)
     for i, (bits, b, e) in enumerate(stage_rows):
-        st[i] = (bits, b, e)
+        st[i] = (list(bits) + [-1] * (STAGE_BITS - len(bits)), b, e)
     arr = (TilePass * max(len(passes), 1))(*passes)
     return EncodedStaged(arr, len(passes), st, pack_ops(fields))
 

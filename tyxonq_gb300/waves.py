@@ -57,13 +57,14 @@ def _dev(arr: np.ndarray, device) -> torch.Tensor:
 
 class WavePlan:
     def __init__(self, entries, dtype, device, t: int = 12, hbits: int = 12, budget: int = 48 << 20,
-                 max_ops: int = 256, lanes: int = 1):
+                 max_ops: int = 256, lanes: int = 1, adj_stage_bits: int = 4):
         """entries: list of dicts with keys idx (instance index), n, gates,
         params, key (structure key), theta_off, grad_offset, basis,
         group_begin, group_count.  Waves are dealt round-robin to `lanes`
         independent launch sequences with disjoint pool and partial ranges,
         which may run on separate streams (each lane's wave fits `budget`)."""
         self.lanes = max(1, int(lanes))
+        self.adj_rb = int(adj_stage_bits)
         self.dtype = dtype
         self.dt = 0 if dtype == torch.complex64 else 1
         self.t = t
@@ -236,7 +237,7 @@ class WavePlan:
             if s.kind != "tiles":
                 raise NotImplementedError("wave path needs tileable gates")
             for pp in s.passes:
-                enc = encode_staged(n, [pp], rg, params=rparams, slots=slots)
+                enc = encode_staged(n, [pp], rg, params=rparams, slots=slots, rb=self.adj_rb)
                 pid = self._add_staged(enc)[0]
                 ops = enc.ops_host
                 pslots = [(k, int(ops[k]["slot"]), float(ops[k]["gcoef"])) for k in range(len(ops))
@@ -262,7 +263,8 @@ class WavePlan:
                 if c == 0:
                     continue
                 nat.call("tq_wave_run", kind, self.dt, P(self.items_dev.data_ptr() + isz * b), c, self.t,
-                         self.hbits, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
+                         self.hbits, self.adj_rb if kind == 2 else 4, P(self.passes_dev.data_ptr()),
+                         P(self.stages_dev.data_ptr()),
                          P(self.ops_dev.data_ptr()), P(groups_dev.data_ptr()), P(terms_dev.data_ptr()),
                          P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()),
                          self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
