@@ -102,34 +102,6 @@ __device__ __forceinline__ void r_dh(cplx<R>* x, cplx<R> d1) {
   }
 }
 
-template <typename R, int NR, int A, int B>
-__device__ __forceinline__ void r_u2(cplx<R>* x, const tq_tile_op& o, bool adj) {
-  if constexpr (!((1 << A) < NR && (1 << B) < NR)) {
-    return;
-  } else {
-#pragma unroll
-  for (int i = 0; i < NR; ++i) {
-    if (((i >> A) & 1) || ((i >> B) & 1)) continue;
-    const int id[4] = {i, i | (1 << B), i | (1 << A), i | (1 << A) | (1 << B)};
-    const cplx<R> v0 = x[id[0]], v1 = x[id[1]], v2 = x[id[2]], v3 = x[id[3]];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      cplx<R> u[4];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        u[c] = adj ? op_m<R>(o, 4 * c + r) : op_m<R>(o, 4 * r + c);
-        if (adj) u[c].y = -u[c].y;
-      }
-      cplx<R> acc = cmul(u[0], v0);
-      acc = cfma(u[1], v1, acc);
-      acc = cfma(u[2], v2, acc);
-      acc = cfma(u[3], v3, acc);
-      x[id[r]] = acc;
-    }
-  }
-  }
-}
-
 // MODE 0 CX (control A, target B), 1 SWAP, 2 CZ
 template <typename R, int NR, int MODE, int A, int B>
 __device__ __forceinline__ void r_perm(cplx<R>* x) {
@@ -154,125 +126,6 @@ __device__ __forceinline__ void r_perm(cplx<R>* x) {
       x[q] = cplx<R>(-x[q].x, -x[q].y);
     }
   }
-  }
-}
-
-// exp(-i a/2 P) on register bits: flip mask XM (compile time), sign mask zm and
-// control mask cm (runtime), coefficients c (real part used) and w.
-template <typename R, int NR, int XM>
-__device__ __forceinline__ void r_prot(cplx<R>* x, uint32_t zm, uint32_t cm, cplx<R> c, cplx<R> w) {
-  if constexpr (!(XM < NR)) {
-    return;
-  } else {
-  if (XM == 0) {
-#pragma unroll
-    for (int i = 0; i < NR; ++i) {
-      if ((i & cm) != cm) continue;
-      const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
-      x[i] = cmul(cplx<R>(c.x + sg * w.x, sg * w.y), x[i]);
-    }
-  } else {
-    constexpr int H = (XM & 8) ? 3 : (XM & 4) ? 2 : (XM & 2) ? 1 : 0;
-#pragma unroll
-    for (int i = 0; i < NR; ++i) {
-      if ((i >> H) & 1) continue;
-      const int j = i ^ XM;
-      if ((i & cm) != cm) continue;
-      const cplx<R> a = x[i], b = x[j];
-      const R si = (__popc(i & zm) & 1) ? R(-1) : R(1);
-      const R sj = (__popc(j & zm) & 1) ? R(-1) : R(1);
-      x[i] = cfma(cplx<R>(w.x * sj, w.y * sj), b, cplx<R>(c.x * a.x, c.x * a.y));
-      x[j] = cfma(cplx<R>(w.x * si, w.y * si), a, cplx<R>(c.x * b.x, c.x * b.y));
-    }
-  }
-  }
-}
-
-template <typename R, int NR>
-__device__ __forceinline__ void r_u2_dispatch(cplx<R>* x, const tq_tile_op& o, bool adj) {
-  switch (o.a * 4 + o.b) {
-    case 1: r_u2<R, NR, 0, 1>(x, o, adj); break;
-    case 2: r_u2<R, NR, 0, 2>(x, o, adj); break;
-    case 3: r_u2<R, NR, 0, 3>(x, o, adj); break;
-    case 4: r_u2<R, NR, 1, 0>(x, o, adj); break;
-    case 6: r_u2<R, NR, 1, 2>(x, o, adj); break;
-    case 7: r_u2<R, NR, 1, 3>(x, o, adj); break;
-    case 8: r_u2<R, NR, 2, 0>(x, o, adj); break;
-    case 9: r_u2<R, NR, 2, 1>(x, o, adj); break;
-    case 11: r_u2<R, NR, 2, 3>(x, o, adj); break;
-    case 12: r_u2<R, NR, 3, 0>(x, o, adj); break;
-    case 13: r_u2<R, NR, 3, 1>(x, o, adj); break;
-    case 14: r_u2<R, NR, 3, 2>(x, o, adj); break;
-    default: break;
-  }
-}
-
-template <typename R, int NR>
-__device__ __forceinline__ void r_prot_dispatch(cplx<R>* x, uint32_t xm, uint32_t zm, uint32_t cm, cplx<R> c,
-                                                cplx<R> w) {
-  switch (xm & (NR - 1)) {
-    case 0: r_prot<R, NR, 0>(x, zm, cm, c, w); break;
-    case 1: r_prot<R, NR, 1>(x, zm, cm, c, w); break;
-    case 2: r_prot<R, NR, 2>(x, zm, cm, c, w); break;
-    case 3: r_prot<R, NR, 3>(x, zm, cm, c, w); break;
-    case 4: r_prot<R, NR, 4>(x, zm, cm, c, w); break;
-    case 5: r_prot<R, NR, 5>(x, zm, cm, c, w); break;
-    case 6: r_prot<R, NR, 6>(x, zm, cm, c, w); break;
-    case 7: r_prot<R, NR, 7>(x, zm, cm, c, w); break;
-    case 8: r_prot<R, NR, 8>(x, zm, cm, c, w); break;
-    case 9: r_prot<R, NR, 9>(x, zm, cm, c, w); break;
-    case 10: r_prot<R, NR, 10>(x, zm, cm, c, w); break;
-    case 11: r_prot<R, NR, 11>(x, zm, cm, c, w); break;
-    case 12: r_prot<R, NR, 12>(x, zm, cm, c, w); break;
-    case 13: r_prot<R, NR, 13>(x, zm, cm, c, w); break;
-    case 14: r_prot<R, NR, 14>(x, zm, cm, c, w); break;
-    default: r_prot<R, NR, 15>(x, zm, cm, c, w); break;
-  }
-}
-
-// ------------------------------------------------------------------ gradient routines
-// Im <lam|G|psi> over the 16 register amplitudes (x = psi, y = lam):
-// G|i> = [i & cm == cm] ph (-1)^{popc(i & zm)} |i ^ XM>  (register-bit masks).
-template <typename R, int NR, int XM>
-__device__ __forceinline__ R r_grad(const cplx<R>* x, const cplx<R>* y, uint32_t zm, uint32_t cm, cplx<R> ph) {
-  if constexpr (!(XM < NR)) {
-    return R(0);
-  } else {
-  R acc = 0;
-#pragma unroll
-  for (int i = 0; i < NR; ++i) {
-    if ((i & cm) != cm) continue;
-    const R sg = (__popc(i & zm) & 1) ? R(-1) : R(1);
-    const cplx<R> v = cmul(ph, x[i]);
-    const cplx<R> l = y[i ^ XM];
-    acc += sg * (l.x * v.y - l.y * v.x);
-  }
-  return acc;
-  }
-}
-
-template <typename R, int NR>
-__device__ __forceinline__ R r_grad_dispatch(const cplx<R>* x, const cplx<R>* y, const tq_tile_op& o) {
-  const R re[4] = {R(1), R(0), R(-1), R(0)}, im[4] = {R(0), R(1), R(0), R(-1)};
-  const cplx<R> ph(re[o.gny & 3], im[o.gny & 3]);
-  const uint32_t zm = o.gzm, cm = o.gcm;
-  switch (o.gxm & (NR - 1)) {
-    case 0: return r_grad<R, NR, 0>(x, y, zm, cm, ph);
-    case 1: return r_grad<R, NR, 1>(x, y, zm, cm, ph);
-    case 2: return r_grad<R, NR, 2>(x, y, zm, cm, ph);
-    case 3: return r_grad<R, NR, 3>(x, y, zm, cm, ph);
-    case 4: return r_grad<R, NR, 4>(x, y, zm, cm, ph);
-    case 5: return r_grad<R, NR, 5>(x, y, zm, cm, ph);
-    case 6: return r_grad<R, NR, 6>(x, y, zm, cm, ph);
-    case 7: return r_grad<R, NR, 7>(x, y, zm, cm, ph);
-    case 8: return r_grad<R, NR, 8>(x, y, zm, cm, ph);
-    case 9: return r_grad<R, NR, 9>(x, y, zm, cm, ph);
-    case 10: return r_grad<R, NR, 10>(x, y, zm, cm, ph);
-    case 11: return r_grad<R, NR, 11>(x, y, zm, cm, ph);
-    case 12: return r_grad<R, NR, 12>(x, y, zm, cm, ph);
-    case 13: return r_grad<R, NR, 13>(x, y, zm, cm, ph);
-    case 14: return r_grad<R, NR, 14>(x, y, zm, cm, ph);
-    default: return r_grad<R, NR, 15>(x, y, zm, cm, ph);
   }
 }
 
