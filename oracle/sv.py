@@ -418,6 +418,41 @@ def grad_adjoint(n, gates, theta, codes, coeffs) -> tuple[float, np.ndarray]:
     return e, g
 
 
+# ------------------------------------------------------------------ shot estimates
+def group_by_basis(codes: np.ndarray, coeffs: np.ndarray) -> tuple[float, dict]:
+    """group_hamiltonian_pauli_terms (hamiltonian_grouping.py:120-138): terms
+    with identical product bases share a group; identity terms add to a constant."""
+    inv = "IXYZ"
+    const, groups = 0.0, {}
+    for row, c in zip(np.asarray(codes), np.asarray(coeffs)):
+        term = tuple((q, inv[int(x)]) for q, x in enumerate(row) if x)
+        if not term:
+            const += float(c)
+            continue
+        groups.setdefault(tuple(inv[int(x)] for x in row), []).append((term, float(c)))
+    return const, groups
+
+
+def term_expectation_from_counts(counts: dict, idxs) -> float:
+    """counts_expval.py:7-20: mean of prod_q (+1 if bit q is 0 else -1)."""
+    total = sum(counts.values()) or 1
+    acc = 0.0
+    for b, cnt in counts.items():
+        s = 1.0
+        for q in idxs:
+            s *= 1.0 if b[q] == "0" else -1.0
+        acc += s * cnt
+    return acc / total
+
+
+def expval_pauli_sum(counts: dict, items, identity_const: float = 0.0) -> float:
+    """counts_expval.py:96-130 (counts path): identity + sum coeff * <Z...Z>."""
+    e = float(identity_const)
+    for term, c in items:
+        e += c * term_expectation_from_counts(counts, [q for q, _ in term])
+    return e
+
+
 # ------------------------------------------------------------------ sampling
 def probabilities(psi: np.ndarray) -> np.ndarray:
     """engine.py:377-414: |psi|^2 renormalised."""

@@ -13,7 +13,8 @@ It imports TyxonQ from the given source tree and records, for seeded inputs:
   * the 12-qubit hardware-efficient TFIM energy (numpy and pytorch backends)
     and its PyTorch-autograd gradient;
   * circuits with one-qubit Kraus channels (explicit status): final states,
-    <Z_q>, and <Z_q> under use_noise depolarizing attenuation.
+    <Z_q>, and <Z_q> under use_noise depolarizing attenuation;
+  * expval_pauli_sum energies and per-term expectations from counts.
 Outputs: tests/golden/golden.npz (arrays) and tests/golden/golden.json
 (circuits and scalars).  The reference is not needed to *use* the fixtures.
 """
@@ -218,6 +219,22 @@ def main(ref_src: str) -> None:
                               "kraus": {k: names[id(v)] for k, v in c._kraus_cache.items()}})
     meta["kraus_sets"] = {k: [[[complex(x).real, complex(x).imag] for x in np.asarray(m).reshape(-1)] for m in v]
                           for k, v in kraus_sets.items()}
+
+    # shot-count postprocessing: expval_pauli_sum over a random counts histogram
+    from tyxonq.postprocessing.counts_expval import expval_pauli_sum
+
+    meta["counts"] = []
+    for ci, n in enumerate([3, 6]):
+        keys = rng.integers(0, 1 << n, size=40)
+        counts = {format(int(k), f"0{n}b"): int(rng.integers(1, 50)) for k in keys}
+        items = []
+        for _ in range(8):
+            w = int(rng.integers(1, min(4, n) + 1))
+            qs = sorted(int(x) for x in rng.choice(n, w, replace=False))
+            items.append((tuple((q, "Z") for q in qs), float(rng.normal())))
+        res = expval_pauli_sum(counts, items, identity_const=0.25)
+        meta["counts"].append({"n": n, "counts": counts, "items": [[list(map(list, t)), c] for t, c in items],
+                               "energy": res["energy"], "expvals": res["expvals"]})
 
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "golden.json").write_text(json.dumps(meta, indent=1))

@@ -43,3 +43,10 @@ def noise_cases():
         out.append((c["name"], c["n"], ops, kc, arrays[f"{c['name']}_state"], arrays[f"{c['name']}_runz"],
                     arrays[f"{c['name']}_runz_depol"]))
     return out
+
+
+def counts_cases():
+    """(n, counts, items [(term, coeff)], energy, expvals) from the reference's expval_pauli_sum."""
+    _, meta = load()
+    return [(c["n"], c["counts"], [(tuple((int(q), p) for q, p in t), float(w)) for t, w in c["items"]],
+             c["energy"], c["expvals"]) for c in meta["counts"]]

@@ -152,3 +152,39 @@ def test_noisy_probabilities_readout_and_depolarizing():
     np.testing.assert_allclose(pr, A @ p / (A @ p).sum(), atol=1e-14)
     pd = sv.noisy_probabilities(psi, n, {"type": "depolarizing", "p": 0.3})
     np.testing.assert_allclose(pd, 0.6 * p + 0.4 / 16, atol=1e-14)
+
+
+@pytest.mark.parametrize("case", golden_data.counts_cases(), ids=lambda c: f"n{c[0]}")
+def test_counts_expectation_against_reference(case):
+    n, counts, items, energy, expvals = case
+    ev = [sv.term_expectation_from_counts(counts, [q for q, _ in t]) for t, _ in items]
+    np.testing.assert_allclose(ev, expvals, atol=1e-14)
+    assert abs(sv.expval_pauli_sum(counts, items, 0.25) - energy) < 1e-12
+
+
+def test_parity_expectations_match_counts_rule():
+    """The device path reduces parities from sampled indices; same numbers as
+    the counts rule on the histogram of those indices."""
+    from tyxonq_gb300.shots import parity_expectations
+
+    rng = np.random.default_rng(8)
+    n = 7
+    idx = np.sort(rng.integers(0, 1 << n, size=3000))
+    counts = {}
+    for i in idx:
+        b = format(int(i), f"0{n}b")
+        counts[b] = counts.get(b, 0) + 1
+    terms = [((0, "Z"), (3, "X")), ((6, "Y"),), ((1, "Z"), (2, "Z"), (5, "Z"))]
+    ev = parity_expectations(idx, terms, n)
+    ref = [sv.term_expectation_from_counts(counts, [q for q, _ in t]) for t in terms]
+    np.testing.assert_allclose(ev, ref, atol=1e-12)
+
+
+def test_group_by_basis_matches_oracle():
+    from tyxonq_gb300.hamiltonian import random_pauli_sum
+    from tyxonq_gb300.shots import group_by_basis
+
+    H = random_pauli_sum(6, 40, np.random.default_rng(2))
+    c1, g1 = group_by_basis(H, 6)
+    c0, g0 = sv.group_by_basis(H.codes, H.coeffs)
+    assert c1 == c0 and g1 == g0

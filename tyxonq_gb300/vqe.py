@@ -49,12 +49,32 @@ class HEA:
         self._est = ParametricEstimator(self.n_qubits, hwe_ry_param_gates(self.n_qubits, self.layers), self.n_params,
                                         self.hamiltonian, dtype=dtype, device=device)
 
-    def energy(self, params: Sequence[float] | None = None) -> float:
+    def _shots(self, runtime, shots):
+        rt = runtime or self.runtime
+        return int(shots or 0) if rt == "device" or shots else 0
+
+    def energy(self, params: Sequence[float] | None = None, *, runtime: str | None = None, shots: int = 0,
+               seed: int = 0) -> float:
+        """Exact energy (numeric runtime), or a shot estimate from basis-group
+        sampling when shots > 0 (device runtime, tyxonq_gb300.shots)."""
         p = self.init_guess if params is None else np.asarray(params, dtype=np.float64)
+        nshots = self._shots(runtime, shots)
+        if nshots:
+            from .shots import ShotEstimator
+
+            return ShotEstimator(self._est, self.hamiltonian, nshots, seed).energy(p)
         return self._est.energy(p)
 
-    def energy_and_grad(self, params: Sequence[float] | None = None) -> tuple[float, np.ndarray]:
+    def energy_and_grad(self, params: Sequence[float] | None = None, *, runtime: str | None = None,
+                        shots: int = 0, seed: int = 0) -> tuple[float, np.ndarray]:
+        """Exact energy and adjoint gradient, or with shots > 0 the shot
+        estimate and parameter-shift gradient of the device runtime."""
         p = self.init_guess if params is None else np.asarray(params, dtype=np.float64)
+        nshots = self._shots(runtime, shots)
+        if nshots:
+            from .shots import ShotEstimator
+
+            return ShotEstimator(self._est, self.hamiltonian, nshots, seed).energy_and_grad(p)
         return self._est.energy_and_grad(p)
 
     def kernel(self, method: str = "L-BFGS-B", maxiter: int = 200) -> float:
