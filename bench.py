@@ -25,7 +25,7 @@ METRIC = "VQE energy+grad evals/s batched vs plain GPU; p50/p99 latency; gate HB
 
 # DRAM bytes read + written by one k_staged_forward launch of the 28-qubit pass,
 # from the ncu capture summarised in profiles/k_staged_forward_28q_c64.txt
-STAGED_PASS_DRAM_BYTES = 4.2455e9
+STAGED_PASS_DRAM_BYTES = 4.2654e9
 
 
 def _peaks():
