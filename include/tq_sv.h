@@ -366,6 +366,45 @@ TQ_API size_t tq_sv_inner_workspace_bytes(int n);
 TQ_API int tq_sv_inner_re(const void* a, const void* b, int n, int dtype, double* out_dev, void* ws,
                    size_t ws_bytes, void* stream);
 
+/* ------------------------------------------------------------ CI-space UCC */
+
+/* CI vector c (D real amplitudes, device) of the determinants with fixed
+ * alpha / beta electron counts.  Excitation j maps determinant i to
+ * fperm[j*D + i] with sign fphase[j*D + i] (0 where it annihilates i), and
+ * f2phase[j*D + i] is the sign of its square; evolution
+ *   c <- c + omc_t[j] * f2phase_j * c + sin_t[j] * fphase_j * c[fperm_j]
+ * replaces evolve_civector_by_tensor
+ * (chem_libs/quantum_chem_library/civector_ops.py:334-350).  Applies
+ * excitations 0..n_ex-1 in order, or n_ex-1..0 with -sin_t (their inverses)
+ * when reverse != 0.  sin_t / omc_t are HOST arrays; tmp is a D-double device
+ * buffer; fperm entries must lie in [0, D). */
+TQ_API int tq_ci_apply_excitations(double* civ, double* tmp, int64_t D, const int32_t* fperm, const int8_t* fphase,
+                                   const int8_t* f2phase, const double* sin_t, const double* omc_t, int n_ex,
+                                   int reverse, void* stream);
+
+/* Reverse sweep of energy_and_grad_civector (civector_ops.py:141-200): from
+ * the evolved ket and bra = H ket, un-apply excitations n_ex-1..0 to both and
+ * write grads[j] = sum_i bra_i fphase_j[i] ket[fperm_j[i]] (device, FP64,
+ * fixed-order sums); dE/dtheta_j = 2 grads[j].  sin_t / omc_t are HOST arrays. */
+TQ_API size_t tq_ci_adjoint_workspace_bytes(int64_t D, int n_ex);
+TQ_API int tq_ci_adjoint(const double* ket, const double* bra, int64_t D, const int32_t* fperm, const int8_t* fphase,
+                         const int8_t* f2phase, const double* sin_t, const double* omc_t, int n_ex, double* grads,
+                         void* ws, size_t ws_bytes, void* stream);
+
+/* sum_i a_i b_i into *out_dev (FP64, fixed order). */
+TQ_API size_t tq_ci_dot_workspace_bytes(int64_t D);
+TQ_API int tq_ci_dot(const double* a, const double* b, int64_t D, double* out_dev, void* ws, size_t ws_bytes,
+                     void* stream);
+
+/* Scatter a CI vector into an n-qubit state (psi zeroed first; determinant
+ * bitstring = basis index, fermion mode m = basis bit m) and read the CI
+ * components of a state back (real parts).  H conserves the particle
+ * numbers, so H applied in the full state and gathered equals H in CI space
+ * (the reference forms the CI-space operator, hamiltonian_builders.py:283-318). */
+TQ_API int tq_ci_embed(const double* civ, const uint64_t* strings, int64_t D, void* psi, int n, int dtype,
+                       void* stream);
+TQ_API int tq_ci_gather(const void* psi, const uint64_t* strings, int64_t D, int dtype, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -81,6 +81,13 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_generator_im": (c_int, [_P, _P, c_int, c_int, c_uint64, c_uint64, c_uint64, _P, _P, c_size_t, _P]),
     "tq_sv_inner_workspace_bytes": (c_size_t, [c_int]),
     "tq_sv_inner_re": (c_int, [_P, _P, c_int, c_int, _P, _P, c_size_t, _P]),
+    "tq_ci_apply_excitations": (c_int, [_P, _P, c_int64, _P, _P, _P, _P, _P, c_int, c_int, _P]),
+    "tq_ci_adjoint_workspace_bytes": (c_size_t, [c_int64, c_int]),
+    "tq_ci_adjoint": (c_int, [_P, _P, c_int64, _P, _P, _P, _P, _P, c_int, _P, _P, c_size_t, _P]),
+    "tq_ci_dot_workspace_bytes": (c_size_t, [c_int64]),
+    "tq_ci_dot": (c_int, [_P, _P, c_int64, _P, _P, c_size_t, _P]),
+    "tq_ci_embed": (c_int, [_P, _P, c_int64, _P, c_int, c_int, _P]),
+    "tq_ci_gather": (c_int, [_P, _P, c_int64, c_int, _P, _P]),
     "tq_batch_smem_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
     "tq_wave_run": (c_int, [c_int, c_int, _P, c_int, c_int, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, _P, c_int, _P]),
     "tq_wave_reduce": (c_int, [_P, _P, _P, _P, _P, _P, c_int, _P, c_int, _P]),

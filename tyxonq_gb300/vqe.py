@@ -89,8 +89,13 @@ class HEA:
 
 
 class UCCSD:
+    """engine="statevector" (default): trotterised Pauli rotations on the
+    n-qubit state with adjoint gradients; engine="civector": the CI-space
+    evolution of civector_ops.py on the determinants with n_elec / 2 electrons
+    per spin (tyxonq_gb300.ci), FP64."""
+
     def __init__(self, int1e: np.ndarray, int2e: np.ndarray, n_elec: int, e_core: float = 0.0,
-                 dtype=torch.complex64, device="cuda"):
+                 dtype=torch.complex64, device="cuda", engine: str = "statevector"):
         from .chem import hf_basis, molecular_hamiltonian, uccsd_param_gates
 
         self.int1e, self.int2e = np.asarray(int1e), np.asarray(int2e)
@@ -102,8 +107,19 @@ class UCCSD:
         pg, self.n_params, self.ex_ops = uccsd_param_gates(self.n_orb, self.n_elec)
         self.param_gates = pg
         self.init_guess = np.zeros(self.n_params)
-        self._est = ParametricEstimator(self.n_qubits, pg, self.n_params, self.hamiltonian, dtype=dtype,
-                                        device=device, init_basis=hf_basis(self.n_qubits, self.n_elec // 2))
+        self.engine = engine
+        if engine == "civector":
+            from .ci import CIVectorUCC
+
+            no = self.n_elec // 2
+            # same parametrisation as the statevector engine: one angle per excitation
+            self._est = CIVectorUCC(self.n_qubits, (no, no), self.ex_ops, list(range(len(self.ex_ops))),
+                                    self.hamiltonian, device=device)
+        elif engine == "statevector":
+            self._est = ParametricEstimator(self.n_qubits, pg, self.n_params, self.hamiltonian, dtype=dtype,
+                                            device=device, init_basis=hf_basis(self.n_qubits, self.n_elec // 2))
+        else:
+            raise ValueError(f"unknown UCC engine {engine!r} (statevector | civector)")
 
     def energy(self, params: Sequence[float] | None = None) -> float:
         p = self.init_guess if params is None else np.asarray(params, dtype=np.float64)
