@@ -463,16 +463,29 @@ __device__ __forceinline__ R rop_grad(const cplx<R>* x, const cplx<R>* y, const 
 
 // ------------------------------------------------------------------ stage mapping
 // Per-thread register <-> padded shared-memory index of register i for a stage
-// with RB register bits b[0..RB) (ascending local positions).
+// with RB register bits b[0..RB) (ascending local positions).  pphys is
+// additive over disjoint bit sets (j + 2 (j >> 4) has no carries between them),
+// so the padded address of register i is p0 + sum of pm[k] over i's bits.
 template <int RB>
 struct StageMap {
   int base;       // local index with all register bits zero
-  int m[RB];      // 1 << bits[k]
-  __device__ __forceinline__ int idx(int i) const {  // i is a compile-time constant at every call
-    int v = base;
+  int p0;         // pphys(base)
+  int pm[RB];     // pphys(1 << bits[k])
+  __device__ __forceinline__ int phys(int i) const {  // i is a compile-time constant at most calls
+    int v = p0;
 #pragma unroll
-    for (int k = 0; k < RB; ++k) v |= ((i >> k) & 1) ? m[k] : 0;
+    for (int k = 0; k < RB; ++k) v += ((i >> k) & 1) ? pm[k] : 0;
     return v;
+  }
+  // addr[i] = phys(i) for every register: one add each
+  __device__ __forceinline__ void addrs(int* addr) const {
+    addr[0] = p0;
+#pragma unroll
+    for (int i = 1; i < (1 << RB); ++i) {
+      const int low = i & -i;
+      const int k = low == 1 ? 0 : low == 2 ? 1 : low == 4 ? 2 : 3;
+      addr[i] = addr[i ^ low] + pm[k];
+    }
   }
 };
 
@@ -483,8 +496,9 @@ __device__ __forceinline__ StageMap<RB> stage_map(const tq_tile_stage& st, int t
 #pragma unroll
   for (int k = 0; k < RB; ++k) b = insz(b, st.bits[k]);
   m.base = b;
+  m.p0 = pphys(b);
 #pragma unroll
-  for (int k = 0; k < RB; ++k) m.m[k] = 1 << st.bits[k];
+  for (int k = 0; k < RB; ++k) m.pm[k] = pphys(1 << st.bits[k]);
   return m;
 }
 
@@ -500,11 +514,7 @@ __device__ __forceinline__ bool rop_is_cold(const ROp<R>& r) {
 
 template <int RB>
 __device__ __forceinline__ int slot_of(const StageMap<RB>& mp, int i) {
-  int v = mp.base;
-#pragma unroll
-  for (int k = 0; k < RB; ++k)
-    if ((i >> k) & 1) v |= mp.m[k];
-  return pphys(v);
+  return mp.phys(i);
 }
 
 template <typename R, int RB>
@@ -776,8 +786,12 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, ROp<R>* rops, bool reside
     const tq_tile_stage st = stages[si];
     const StageMap<kRB> m = stage_map<kRB>(st, threadIdx.x);
     cplx<R> x[kNR], x2[kNR];
+    {
+      int ad[kNR];
+      m.addrs(ad);
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) x[i] = s[pphys(m.idx(i))];
+      for (int i = 0; i < kNR; ++i) x[i] = s[ad[i]];
+    }
     for (int k0 = st.op_begin; k0 < st.op_end;) {
       const int k1 = resident ? st.op_end : min(k0 + kRopCap, st.op_end);
       const ROp<R>* rr = rops - (resident ? op0 : k0);
@@ -803,8 +817,12 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, ROp<R>* rops, bool reside
       }
       k0 = k;
     }
+    {
+      int ad[kNR];
+      m.addrs(ad);
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) s[pphys(m.idx(i))] = x[i];
+      for (int i = 0; i < kNR; ++i) s[ad[i]] = x[i];
+    }
     __syncthreads();
   }
 }

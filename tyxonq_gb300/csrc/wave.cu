@@ -330,11 +330,14 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, RB == 3 ? 2 : 1)
       const tq_tile_stage st = stages[si];
       const StageMap<RB> mp = stage_map<RB>(st, threadIdx.x);
       cplx<R> x[NR], y[NR];
+      {
+        int ad[NR];
+        mp.addrs(ad);
 #pragma unroll
-      for (int i = 0; i < NR; ++i) {
-        const int j = pphys(mp.idx(i));
-        x[i] = sp[j];
-        y[i] = sl[j];
+        for (int i = 0; i < NR; ++i) {
+          x[i] = sp[ad[i]];
+          y[i] = sl[ad[i]];
+        }
       }
       for (int k = st.op_begin; k < st.op_end; ++k) {
         const ROp<R>& r = rops[k - op0];
@@ -343,7 +346,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, RB == 3 ? 2 : 1)
         if (rop_is_cold(r)) {  // same for every thread: the record is shared
 #pragma unroll
           for (int i = 0; i < NR; ++i) {
-            const int j = pphys(mp.idx(i));
+            const int j = mp.phys(i);
             sp[j] = x[i];
             sl[j] = y[i];
           }
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, RB == 3 ? 2 : 1)
           s_cold_apply<R, RB>(sl, mp, o, r, true, zs);
 #pragma unroll
           for (int i = 0; i < NR; ++i) {
-            const int j = pphys(mp.idx(i));
+            const int j = mp.phys(i);
             x[i] = sp[j];
             y[i] = sl[j];
           }
@@ -368,11 +371,14 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, RB == 3 ? 2 : 1)
           if (lane == 0) wpart[(k - op0) * nwarps + warp] = part;
         }
       }
+      {
+        int ad[NR];
+        mp.addrs(ad);
 #pragma unroll
-      for (int i = 0; i < NR; ++i) {
-        const int j = pphys(mp.idx(i));
-        sp[j] = x[i];
-        sl[j] = y[i];
+        for (int i = 0; i < NR; ++i) {
+          sp[ad[i]] = x[i];
+          sl[ad[i]] = y[i];
+        }
       }
       __syncthreads();
     }
