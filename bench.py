@@ -6,8 +6,10 @@ Prints ONE JSON line (rank 0): batched energy + adjoint-gradient evaluations
 per second of 4096 seeded VQE instances (graph replay, L2 flushed between
 steps), the same end to end from host parameters to host results, the plain
 one-launch-per-gate engine on a sample, serving latency percentiles, the
-28-qubit fused circuit and single-gate HBM bandwidths, the roofline of the
-fused pass kernel, a CPU baseline and SM clocks sampled during the timed steps.
+28-qubit fused circuit and single-gate HBM bandwidths, per-call times of the
+12-qubit HEA (energy, gradient, 4096 shots) and the 16-qubit UCCSD, the
+roofline of the fused pass kernel, a CPU baseline and SM clocks sampled during
+the timed steps.
 """
 from __future__ import annotations
 
@@ -249,10 +251,71 @@ def bench_gate_kernels(args, dev):
             "pass_gbs": 2 * N * S / (avg_launch * 1e-3) / 1e9, "single_gate": bench_single_gates(n2)}
 
 
+def bench_small_configs(reps: int = 10) -> dict:
+    """Per-call times, host parameters in and host results out, of
+    * the 12-qubit HEA (4 layers of [RY on every qubit; CX ladder]) with the
+      open-chain TFIM (23 terms): complex128 energy + adjoint gradient, and
+      4096 Z-basis shots (forward, sampling, counts dictionary);
+    * the 16-qubit UCCSD from the Hartree-Fock bitstring (8 orbitals, 4
+      electrons, 198 excitations as 1440 Pauli rotations, Jordan-Wigner H of
+      seeded random integrals): adjoint energy + gradient in complex128 and
+      complex64, and the FP64 CI-space engine."""
+    import numpy as np
+    import torch
+
+    from tyxonq_gb300 import chem
+    from tyxonq_gb300 import kernels as K
+    from tyxonq_gb300.adjoint import ParamGate, ParametricEstimator
+    from tyxonq_gb300.ir import Gate, _rot_gate
+    from tyxonq_gb300.vqe import UCCSD
+    from tyxonq_gb300.workloads import hea_tfim
+
+    def per_call_ms(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / reps
+
+    _, H12, th12 = hea_tfim(12, 4, seed=0)
+    pg = []
+    for l in range(4):
+        pg += [ParamGate(_rot_gate("ry", (q,), 0.0), l * 12 + q) for q in range(12)]
+        pg += [ParamGate(Gate("cx", (q, q + 1))) for q in range(11)]
+    est = ParametricEstimator(12, pg, 48, H12, dtype=torch.complex128)
+    theta = th12.reshape(-1)
+
+    def shots():
+        psi = est._forward(theta)
+        return K.counts_from_indices(K.sample(psi, 4096, seed=11).cpu().numpy(), 12)
+
+    out = {"hea12_tfim": {"energy": est.energy(theta),
+                          "energy_grad_ms": per_call_ms(lambda: est.energy_and_grad(theta)),
+                          "energy_ms": per_call_ms(lambda: est.energy(theta)),
+                          "shots4096_ms": per_call_ms(shots), "dtype": "c128"}}
+    h, g = chem.random_integrals(8, seed=7)
+    ucc = {}
+    for name, kw in (("c128", {"dtype": torch.complex128}), ("c64", {"dtype": torch.complex64}),
+                     ("civector_f64", {"engine": "civector"})):
+        m = UCCSD(h, g, n_elec=4, **kw)
+        p = np.random.default_rng(2).uniform(-0.3, 0.3, m.n_params)
+        ucc[name] = {"energy_grad_ms": per_call_ms(lambda: m.energy_and_grad(p)), "energy": m.energy(p)}
+        ucc["terms"], ucc["params"], ucc["rotations"] = len(m.hamiltonian.coeffs), m.n_params, len(m.param_gates)
+        del m
+    out["uccsd16"] = ucc
+    torch.cuda.empty_cache()
+    return out
+
+
 def bench_single_gates(n: int, reps: int = 4) -> dict:
     """One launch per gate on an n-qubit complex64 state (2 GiB at 28 qubits, far
     above L2): device time per launch and GB/s over the algorithmic bytes of the
-    gate (amplitudes it can change, read and written once)."""
+    gate (amplitudes it can change, read and written once), and over the bytes
+    of the 32-byte DRAM sectors that hold such amplitudes (the least traffic a
+    gate on the lowest index bits can cause)."""
     import ctypes
 
     import numpy as np
@@ -271,21 +334,31 @@ def bench_single_gates(n: int, reps: int = 4) -> dict:
     d_rz = (ctypes.c_double * 4)(np.cos(0.3), -np.sin(0.3), np.cos(0.3), np.sin(0.3))
     d_ph = (ctypes.c_double * 4)(1.0, 0.0, np.cos(0.7), np.sin(0.7))
     mh, m2 = K._mat(h, 2), K._mat(u2, 4)
+    def sector_frac(*bits):
+        # share of 32-byte sectors (4 complex64 amplitudes: index bits 0-1) that hold an
+        # amplitude the gate changes, when the changed amplitudes are those with all `bits` set
+        f = 1.0
+        for b in bits:
+            f *= 1.0 if b < 2 else 0.5
+        return f
+
     kinds = {
-        "dense_1q": (2 * N * S, lambda q, r: nat.call("tq_sv_apply_1q", P, n, 0, q, mh, st)),
-        "diag_1q": (2 * N * S, lambda q, r: nat.call("tq_sv_apply_diag1", P, n, 0, q, d_rz, st)),
-        "phase_1q": (N * S, lambda q, r: nat.call("tq_sv_apply_diag1", P, n, 0, q, d_ph, st)),
-        "cx": (N * S, lambda q, r: nat.call("tq_sv_apply_cx", P, n, 0, q, r, st)),
-        "cz": (N * S // 2, lambda q, r: nat.call("tq_sv_apply_cz", P, n, 0, q, r, st)),
-        "dense_2q": (2 * N * S, lambda q, r: nat.call("tq_sv_apply_2q", P, n, 0, q, r, m2, st)),
+        "dense_1q": (2 * N * S, lambda q, r: 1.0, lambda q, r: nat.call("tq_sv_apply_1q", P, n, 0, q, mh, st)),
+        "diag_1q": (2 * N * S, lambda q, r: 1.0, lambda q, r: nat.call("tq_sv_apply_diag1", P, n, 0, q, d_rz, st)),
+        "phase_1q": (N * S, lambda q, r: sector_frac(n - 1 - q),
+                     lambda q, r: nat.call("tq_sv_apply_diag1", P, n, 0, q, d_ph, st)),
+        "cx": (N * S, lambda q, r: sector_frac(n - 1 - q), lambda q, r: nat.call("tq_sv_apply_cx", P, n, 0, q, r, st)),
+        "cz": (N * S // 2, lambda q, r: sector_frac(n - 1 - q, n - 1 - r),
+               lambda q, r: nat.call("tq_sv_apply_cz", P, n, 0, q, r, st)),
+        "dense_2q": (2 * N * S, lambda q, r: 1.0, lambda q, r: nat.call("tq_sv_apply_2q", P, n, 0, q, r, m2, st)),
     }
     out = {}
-    for name, (alg, fn) in kinds.items():
+    for name, (alg, frac, fn) in kinds.items():
         pairs = [(q, qs[(i + 2) % len(qs)]) for i, q in enumerate(qs)]
         for q, r in pairs:  # warm-up
             fn(q, r)
         torch.cuda.synchronize()
-        times = []
+        times, sector_bytes = [], []
         for _ in range(reps):
             for q, r in pairs:
                 a, b = _events()
@@ -294,8 +367,12 @@ def bench_single_gates(n: int, reps: int = 4) -> dict:
                 b.record()
                 torch.cuda.synchronize()
                 times.append(a.elapsed_time(b))
+                sector_bytes.append(2 * N * S * frac(q, r))
         ms = sum(times) / len(times)
-        out[name] = {"ms": ms, "alg_bytes": alg, "gbs": alg / (ms * 1e-3) / 1e9, "launches": len(times)}
+        out[name] = {"ms": ms, "alg_bytes": alg, "gbs": alg / (ms * 1e-3) / 1e9, "launches": len(times),
+                     "sector_bytes": sum(sector_bytes) / len(sector_bytes),
+                     "sector_gbs": sum(sector_bytes) / (sum(times) * 1e-3) / 1e9,
+                     "qubit_pairs": pairs}
     del psi
     torch.cuda.empty_cache()
     return out
@@ -312,6 +389,9 @@ def run_case(args):
     torch.cuda.set_device(0)
     if args.case == "gates":
         print(json.dumps({"case": "gates", **bench_gate_kernels(args, 0)}))
+        return
+    if args.case == "small":
+        print(json.dumps({"case": "small", **bench_small_configs()}))
         return
     from tyxonq_gb300.batch import BatchedVQE
     from tyxonq_gb300.workloads import batched_vqe
@@ -340,7 +420,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--count", type=int, default=4096)
-    ap.add_argument("--case", default="full", choices=["full", "gates", "batched"],
+    ap.add_argument("--case", default="full", choices=["full", "gates", "batched", "small"],
                     help="gates / batched: run only that part (profiling captures); full: the benchmark line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -435,6 +515,7 @@ def main():
     # ---------------- 28q gate kernels (memory-bound case) + roofline
     gk = bench_gate_kernels(args, dev)
     peak, peak_kind = _peaks()
+    small = bench_small_configs()
 
     # ---------------- serving: Poisson arrivals, 70% energy / 30% energy+gradient, 10-26 qubits
     from tyxonq_gb300.serving import VqeServer, make_trace, replay
@@ -491,6 +572,7 @@ def main():
                     "workload": "Poisson arrivals, 24 sessions x 2 optimizer steps, HEA n~U{10..26} depth~U{2..10}, "
                                 "20-1000 Pauli terms, 30% energy+gradient, complex64"},
         "gate_kernels_28q": gk,
+        "small_configs": small,
         "roofline": {"kernel": "k_staged_forward (28-qubit complex64 fused pass of the depth-40 random circuit, "
                                "2*N*8 B per launch)", "bound": "hbm",
                      "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,

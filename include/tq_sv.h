@@ -405,6 +405,41 @@ TQ_API int tq_ci_embed(const double* civ, const uint64_t* strings, int64_t D, vo
                        void* stream);
 TQ_API int tq_ci_gather(const void* psi, const uint64_t* strings, int64_t D, int dtype, double* out, void* stream);
 
+/* y = H x with H restricted to the CI space as CSR (row_ptr[D + 1] int64,
+ * col int32, val FP64; device), one warp per row, fixed-order sums: the
+ * apply_op(hamiltonian, ket) of energy_and_grad_civector (civector_ops.py:178,
+ * hamiltonian_builders.py:283-318) with the CI-space operator that
+ * hamiltonian_builders.py:165-178 contracts through pyscf. */
+TQ_API int tq_ci_spmv(const int64_t* row_ptr, const int32_t* col, const double* val, int64_t D, const double* x,
+                      double* y, void* stream);
+
+/* Whole energy_and_grad_civector (civector_ops.py:141-200) for
+ * D <= tq_ci_pairs_max_dim(n_ex): ket = unit vector init_index evolved by
+ * excitations 0..n_ex-1 (one CTA, vector in shared memory), bra = H ket (CSR
+ * as in tq_ci_spmv, many CTAs), out[0] = <bra, ket> and, when grad != 0, the
+ * reverse sweep of tq_ci_adjoint with out[1 + j] = grads[j]
+ * (dE/dtheta_j = 2 grads[j]), fixed-order sums.  Each excitation is given by
+ * its PAIRS, the determinants it changes: int32 pairs [total][2] =
+ * {i, (p << 1) | (fphase_j[i] < 0)} with p = fperm_j[i] > i, fphase_j[p] =
+ * -fphase_j[i] and f2phase_j = -1 on both (every other determinant has
+ * fphase_j = f2phase_j = 0); excitation j owns pairs pair_start[j] ..
+ * pair_start[j + 1] (int64 [n_ex + 1], device), at most max_pairs <= 2048
+ * of them (TQ_ERR_RANGE above).
+ * part_start (int64 [n_ex + 2], device) places the partial sums:
+ * part_start[0] = 0, part_start[1] = min(D, 1024), part_start[2 + j] =
+ * part_start[1 + j] + min(pairs of j, 1024); n_partials = part_start[n_ex + 1].
+ * sin_omc: DEVICE FP64 [n_ex][2] = {sin t_j, 1 - cos t_j}.  ket_out (D
+ * doubles, device) receives the evolved ket unless NULL; ws holds
+ * tq_ci_energy_grad_workspace_bytes(D, n_partials) bytes.  Pairs outside
+ * [0, D) are skipped.  TQ_ERR_RANGE when D is above the limit. */
+TQ_API int64_t tq_ci_pairs_max_dim(int n_ex);
+TQ_API size_t tq_ci_energy_grad_workspace_bytes(int64_t D, int64_t n_partials);
+TQ_API int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const int32_t* pairs,
+                             const int64_t* pair_start, int64_t max_pairs, const int64_t* part_start,
+                             int64_t n_partials, const double* sin_omc, const int64_t* row_ptr, const int32_t* col,
+                             const double* val, int grad, double* ket_out, double* out, void* ws, size_t ws_bytes,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -96,6 +96,187 @@ __global__ void k_ci_gather(const typename C2<R>::T* __restrict__ psi, const uin
     out[i] = (double)psi[strings[i]].x;
 }
 
+// ---------------------------------------------------------------------------
+// H in the CI space as CSR (row_ptr[D + 1], col, val): one warp per row, lanes
+// stride over the row's entries, fixed shuffle tree (deterministic).
+__device__ __forceinline__ double ci_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void k_ci_spmv(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                          const double* __restrict__ val, int64_t D, const double* __restrict__ x,
+                          double* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w0; r < D; r += nw) {
+    double acc = 0.0;
+    for (int64_t q = rp[r] + lane; q < rp[r + 1]; q += 32) acc += val[q] * x[col[q]];
+    acc = ci_warp_sum(acc);
+    if (lane == 0) y[r] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One-CTA sweeps over excitation PAIRS.  Excitation j changes only the
+// determinants i with fphase_j[i] != 0; they come in pairs (i, p = perm_j[i])
+// with fphase_j[p] = -fphase_j[i] and f2phase = -1 on both, and every other
+// amplitude is left as it is.  One thread updates both members of a pair in
+// place:
+//   c_i <- c_i - omc c_i + sin phi c_p,   c_p <- c_p - omc c_p - sin phi c_i
+// (phi = fphase_j[i]), so the work per excitation is the pair count, not D.
+// Pair entry (int2): x = i, y = (p << 1) | (phi < 0).  pair_start[j] ..
+// pair_start[j + 1] index excitation j's pairs; a barrier separates
+// excitations.  The entries of the next two excitations are prefetched into
+// registers while the current one is applied.
+//
+// FP64 issues at a small fraction of the FP32 rate on this GPU (and a CTA
+// runs on one SM), so signs are applied by flipping the sign bit with integer
+// operations and cross-thread sums are left to k_ci_segsum on many SMs: each
+// thread stores its in-thread partial of grad_j (and of the energy) to
+// part[part_start[...] + tid].
+constexpr int kCiThreads = 1024;
+
+__device__ __forceinline__ double ci_neg_if(double x, unsigned neg) {
+  return __longlong_as_double(__double_as_longlong(x) ^ ((long long)neg << 63));
+}
+
+template <int IT>
+__device__ __forceinline__ void ci_load_pairs(int2 (&r)[IT], const int2* __restrict__ pairs,
+                                              const int64_t* ps, int j, int n_ex) {
+  if (j < 0 || j >= n_ex) return;
+  const int64_t a = ps[j], np = ps[j + 1] - a;
+#pragma unroll
+  for (int m = 0; m < IT; ++m) {
+    const int64_t k = threadIdx.x + (int64_t)m * kCiThreads;
+    r[m] = k < np ? __ldg(pairs + a + k) : make_int2(-1, 0);
+  }
+}
+
+template <int IT>
+__device__ __forceinline__ void ci_rotate(int2 (&a)[IT], int2 (&b)[IT], int2 (&c)[IT]) {
+#pragma unroll
+  for (int m = 0; m < IT; ++m) {
+    a[m] = b[m];
+    b[m] = c[m];
+  }
+}
+
+// c <- U_j c for one pair (sign = +1 forward, -1 to un-apply).
+__device__ __forceinline__ void ci_pair_update(double* c, int i, int p, double t, double mo) {
+  const double ci = c[i], cp = c[p];
+  c[i] = fma(t, cp, fma(mo, ci, ci));
+  c[p] = fma(ci_neg_if(t, 1u), ci, fma(mo, cp, cp));
+}
+
+__device__ __forceinline__ bool ci_pair_ok(int2 e, int D) {
+  return e.x >= 0 && e.x < D && (e.y >> 1) >= 0 && (e.y >> 1) < D;
+}
+
+// Shared memory layout of both sweeps: [vectors][sin, omc per excitation][pair_start][part_start].
+template <int IT>
+__global__ void __launch_bounds__(kCiThreads, 1)
+    k_ci_forward(int D, int init, int n_ex, const int2* __restrict__ pairs, const int64_t* __restrict__ pair_start,
+                 const double* __restrict__ sin_omc, double* __restrict__ ket) {
+  extern __shared__ double sm[];
+  double* c = sm;
+  double* so = sm + D;
+  int64_t* ps = (int64_t*)(so + 2 * n_ex);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 2 * n_ex; i += kCiThreads) so[i] = sin_omc[i];
+  for (int i = tid; i <= n_ex; i += kCiThreads) ps[i] = pair_start[i];
+  for (int i = tid; i < D; i += kCiThreads) c[i] = (i == init) ? 1.0 : 0.0;
+  __syncthreads();
+  int2 cur[IT], nx1[IT], nx2[IT];
+  ci_load_pairs<IT>(cur, pairs, ps, 0, n_ex);
+  ci_load_pairs<IT>(nx1, pairs, ps, 1, n_ex);
+  for (int j = 0; j < n_ex; ++j) {
+    ci_load_pairs<IT>(nx2, pairs, ps, j + 2, n_ex);
+    const double s = so[2 * j], mo = ci_neg_if(so[2 * j + 1], 1u);
+#pragma unroll
+    for (int m = 0; m < IT; ++m)
+      if (ci_pair_ok(cur[m], D)) ci_pair_update(c, cur[m].x, cur[m].y >> 1, ci_neg_if(s, cur[m].y & 1), mo);
+    __syncthreads();
+    ci_rotate<IT>(cur, nx1, nx2);
+  }
+  for (int i = tid; i < D; i += kCiThreads) ket[i] = c[i];
+}
+
+// Energy partials <ket, bra> and, when grad != 0, the reverse sweep: un-apply
+// excitation j to ket and bra, then grad_j partial = sum over j's pairs of
+// b_i phi k_p - b_p phi k_i (= sum_i bra_i fphase_j[i] ket[fperm_j[i]]).
+template <int IT>
+__global__ void __launch_bounds__(kCiThreads, 1)
+    k_ci_reverse(int D, int n_ex, int grad, const int2* __restrict__ pairs, const int64_t* __restrict__ pair_start,
+                 const int64_t* __restrict__ part_start, const double* __restrict__ sin_omc,
+                 const double* __restrict__ ket, const double* __restrict__ bra, double* __restrict__ part) {
+  extern __shared__ double sm[];
+  double* k = sm;
+  double* b = sm + D;
+  double* so = sm + 2 * D;
+  int64_t* ps = (int64_t*)(so + 2 * n_ex);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 2 * n_ex; i += kCiThreads) so[i] = sin_omc[i];
+  for (int i = tid; i <= n_ex; i += kCiThreads) ps[i] = pair_start[i];
+  double e = 0.0;
+  for (int i = tid; i < D; i += kCiThreads) {
+    const double kv = ket[i], bv = bra[i];
+    k[i] = kv;
+    b[i] = bv;
+    e = fma(kv, bv, e);
+  }
+  if (tid < (D < kCiThreads ? D : kCiThreads)) part[part_start[0] + tid] = e;
+  if (!grad) return;
+  __syncthreads();
+  int2 cur[IT], nx1[IT], nx2[IT];
+  ci_load_pairs<IT>(cur, pairs, ps, n_ex - 1, n_ex);
+  ci_load_pairs<IT>(nx1, pairs, ps, n_ex - 2, n_ex);
+  for (int j = n_ex - 1; j >= 0; --j) {
+    ci_load_pairs<IT>(nx2, pairs, ps, j - 2, n_ex);
+    const double s = ci_neg_if(so[2 * j], 1u), mo = ci_neg_if(so[2 * j + 1], 1u);
+    double acc = 0.0;
+#pragma unroll
+    for (int m = 0; m < IT; ++m) {
+      if (!ci_pair_ok(cur[m], D)) continue;
+      const int i = cur[m].x, p = cur[m].y >> 1;
+      const unsigned neg = cur[m].y & 1;
+      const double t = ci_neg_if(s, neg);
+      ci_pair_update(k, i, p, t, mo);
+      ci_pair_update(b, i, p, t, mo);
+      // pairs of one excitation are disjoint: this thread's own updates are the values it reads
+      acc = fma(ci_neg_if(b[i], neg), k[p], acc);
+      acc = fma(ci_neg_if(b[p], neg ^ 1u), k[i], acc);
+    }
+    const int64_t np = ps[j + 1] - ps[j];
+    if (tid < np) part[part_start[1 + j] + tid] = acc;
+    __syncthreads();
+    ci_rotate<IT>(cur, nx1, nx2);
+  }
+}
+
+// out[o] = sum of part[seg[o] .. seg[o + 1]) in index order (one block per output).
+__global__ void k_ci_segsum(const double* __restrict__ part, const int64_t* __restrict__ seg, double* out) {
+  __shared__ double sh[32];
+  const int64_t a = seg[blockIdx.x], z = seg[blockIdx.x + 1];
+  double acc = 0.0;
+  for (int64_t q = a + threadIdx.x; q < z; q += blockDim.x) acc += part[q];
+  acc = ci_block_sum(acc, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = acc;
+}
+
+static size_t ci_sweep_smem(int64_t vectors, int64_t D, int n_ex) {
+  return sizeof(double) * ((size_t)vectors * D + (size_t)2 * n_ex) + sizeof(int64_t) * (size_t)(n_ex + 1);
+}
+
+static int ci_smem_optin() {
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  return v;
+}
+
 static int ci_blocks(int64_t D) {
   int64_t b = (D + 255) / 256;
   if (b > 1216) b = 1216;
@@ -217,5 +398,77 @@ extern "C" int tq_ci_gather(const void* psi, const uint64_t* strings, int64_t D,
   else
     k_ci_gather<double><<<ci_blocks(D), 256, 0, s>>>((const double2*)psi, strings, D, out);
   TQ_CHECK_LAUNCH("tq_ci_gather");
+  return TQ_OK;
+}
+
+extern "C" int tq_ci_spmv(const int64_t* row_ptr, const int32_t* col, const double* val, int64_t D, const double* x,
+                          double* y, void* stream) {
+  if (D < 1 || !row_ptr || !col || !val || !x || !y) return fail(TQ_ERR_ARG, "tq_ci_spmv: bad argument");
+  int64_t nb = (D + 7) / 8;
+  if (nb > 152 * 16) nb = 152 * 16;
+  k_ci_spmv<<<(int)nb, 256, 0, (cudaStream_t)stream>>>(row_ptr, col, val, D, x, y);
+  TQ_CHECK_LAUNCH("tq_ci_spmv");
+  return TQ_OK;
+}
+
+extern "C" int64_t tq_ci_pairs_max_dim(int n_ex) {
+  if (n_ex < 0) return 0;
+  const int64_t optin = ci_smem_optin();
+  const int64_t fixed = (int64_t)ci_sweep_smem(0, 0, n_ex);
+  const int64_t d = (optin - fixed) / (2 * (int64_t)sizeof(double));
+  return d > 0 ? d : 0;
+}
+
+extern "C" size_t tq_ci_energy_grad_workspace_bytes(int64_t D, int64_t n_partials) {
+  if (D < 1 || n_partials < 0) return 0;
+  return sizeof(double) * ((size_t)2 * D + (size_t)n_partials);
+}
+
+extern "C" int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const int32_t* pairs,
+                                 const int64_t* pair_start, int64_t max_pairs, const int64_t* part_start,
+                                 int64_t n_partials, const double* sin_omc, const int64_t* row_ptr, const int32_t* col,
+                                 const double* val, int grad, double* ket_out, double* out, void* ws, size_t ws_bytes,
+                                 void* stream) {
+  if (D < 1 || n_ex < 0 || init_index < 0 || init_index >= D || max_pairs < 0 || n_partials < 1)
+    return fail(TQ_ERR_ARG, "tq_ci_energy_grad: D=%lld, n_ex=%d, init=%lld, max_pairs=%lld, n_partials=%lld",
+                (long long)D, n_ex, (long long)init_index, (long long)max_pairs, (long long)n_partials);
+  if (D > tq_ci_pairs_max_dim(n_ex))
+    return fail(TQ_ERR_RANGE, "tq_ci_energy_grad: D=%lld above the one-CTA limit %lld for %d excitations",
+                (long long)D, (long long)tq_ci_pairs_max_dim(n_ex), n_ex);
+  if (max_pairs > 2 * (int64_t)kCiThreads)
+    return fail(TQ_ERR_RANGE, "tq_ci_energy_grad: %lld pairs in one excitation (at most %d)", (long long)max_pairs,
+                2 * kCiThreads);
+  if (!pair_start || !part_start || !row_ptr || !col || !val || !out || (n_ex > 0 && (!pairs || !sin_omc)))
+    return fail(TQ_ERR_ARG, "tq_ci_energy_grad: NULL pointer");
+  const size_t need = tq_ci_energy_grad_workspace_bytes(D, n_partials);
+  if (!ws || ws_bytes < need)
+    return fail(TQ_ERR_WORKSPACE, "tq_ci_energy_grad: workspace of %zu bytes < %zu", ws_bytes, need);
+  cudaStream_t s = (cudaStream_t)stream;
+  double* ket = ket_out ? ket_out : (double*)ws;
+  double* bra = (double*)ws + D;
+  double* part = bra + D;
+  const int2* pr = (const int2*)pairs;
+  const size_t smem_f = ci_sweep_smem(1, D, n_ex), smem_r = ci_sweep_smem(2, D, n_ex);
+#define TQ_CI_SWEEPS(IT)                                                                                         \
+  do {                                                                                                           \
+    cudaError_t e = cudaFuncSetAttribute(k_ci_forward<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize,         \
+                                         (int)smem_f);                                                           \
+    if (e == cudaSuccess)                                                                                        \
+      e = cudaFuncSetAttribute(k_ci_reverse<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r);     \
+    if (e != cudaSuccess) return cuda_status(e, "tq_ci_energy_grad: shared memory");                             \
+    k_ci_forward<IT><<<1, kCiThreads, smem_f, s>>>((int)D, (int)init_index, n_ex, pr, pair_start, sin_omc, ket); \
+    k_ci_spmv<<<spmv_blocks, 256, 0, s>>>(row_ptr, col, val, D, ket, bra);                                      \
+    k_ci_reverse<IT><<<1, kCiThreads, smem_r, s>>>((int)D, n_ex, grad, pr, pair_start, part_start, sin_omc, ket, \
+                                                   bra, part);                                                   \
+  } while (0)
+  int64_t spmv_blocks = (D + 7) / 8;
+  if (spmv_blocks > 152 * 16) spmv_blocks = 152 * 16;
+  if (max_pairs <= kCiThreads)
+    TQ_CI_SWEEPS(1);
+  else
+    TQ_CI_SWEEPS(2);
+#undef TQ_CI_SWEEPS
+  k_ci_segsum<<<grad ? 1 + n_ex : 1, 256, 0, s>>>(part, part_start, out);
+  TQ_CHECK_LAUNCH("tq_ci_energy_grad");
   return TQ_OK;
 }
