@@ -257,9 +257,10 @@ def bench_small_configs(reps: int = 10) -> dict:
       open-chain TFIM (23 terms): complex128 energy + adjoint gradient, and
       4096 Z-basis shots (forward, sampling, counts dictionary);
     * the 16-qubit UCCSD from the Hartree-Fock bitstring (8 orbitals, 4
-      electrons, 198 excitations as 1440 Pauli rotations, Jordan-Wigner H of
-      seeded random integrals): adjoint energy + gradient in complex128 and
-      complex64, and the FP64 CI-space engine."""
+      electrons, 198 excitations, Jordan-Wigner H of seeded random integrals):
+      adjoint energy + gradient with the excitations as 1440 Pauli-string
+      exponentials (fused-pass engine) and as exact pair rotations, each in
+      complex128 and complex64, and the FP64 CI-space engine."""
     import numpy as np
     import torch
 
@@ -298,7 +299,10 @@ def bench_small_configs(reps: int = 10) -> dict:
                           "shots4096_ms": per_call_ms(shots), "dtype": "c128"}}
     h, g = chem.random_integrals(8, seed=7)
     ucc = {}
-    for name, kw in (("c128", {"dtype": torch.complex128}), ("c64", {"dtype": torch.complex64}),
+    for name, kw in (("c128_rotations", {"dtype": torch.complex128, "trotter": True}),
+                     ("c64_rotations", {"dtype": torch.complex64, "trotter": True}),
+                     ("c128_excitations", {"dtype": torch.complex128}),
+                     ("c64_excitations", {"dtype": torch.complex64}),
                      ("civector_f64", {"engine": "civector"})):
         m = UCCSD(h, g, n_elec=4, **kw)
         p = np.random.default_rng(2).uniform(-0.3, 0.3, m.n_params)

@@ -440,6 +440,43 @@ TQ_API int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const int3
                              const double* val, int grad, double* ket_out, double* out, void* ws, size_t ws_bytes,
                              void* stream);
 
+/* One fermionic excitation on the n-qubit statevector (fermion mode m =
+ * basis bit m, i.e. qubit n-1-m).  F = T - T^dagger changes only the basis
+ * states whose excitation bits (m_neg | m_pos, k = 2 or 4 of them, ascending
+ * in bits[0..k)) equal m_neg or m_pos; they pair up as s_neg = base | m_neg,
+ * s_pos = base | m_pos with F s_pos = phi s_neg, F s_neg = -phi s_pos,
+ * phi = sign * (popcount(s_neg & zmask) odd ? 1 : -1) (the Jordan-Wigner
+ * Z string; zmask holds no excitation bit), and F^2 = -1 on them.  So
+ * exp(theta F) = psi + (1 - cos) F^2 psi + sin F psi
+ * (statevector_ops.py:140-168 evolve_excitation) is a 2x2 rotation on each
+ * pair and leaves every other amplitude as it is. */
+typedef struct {
+  uint64_t m_neg;
+  uint64_t m_pos;
+  uint64_t zmask;
+  int32_t sign; /* +1 or -1 */
+  int32_t k;    /* 2 (single) or 4 (double) */
+  int32_t bits[4];
+} tq_excitation;
+
+/* Apply excitations 0..n_ex-1 in order (reverse = 0) or their inverses
+ * n_ex-1..0 (reverse != 0) to psi: get_statevector's loop over
+ * evolve_excitation (statevector_ops.py:66-114).  exc: DEVICE array of n_ex
+ * records; sincos: DEVICE FP64 [n_ex][2] = {sin t_j, cos t_j}.  Records with
+ * k not 2 / 4, bits out of range or masks that do not split the excitation
+ * bits are skipped. */
+TQ_API int tq_sv_apply_excitations(void* psi, int n, int dtype, const tq_excitation* exc, int n_ex,
+                                   const double* sincos, int reverse, void* stream);
+
+/* Reverse sweep for the energy gradient (the reference differentiates
+ * get_statevector with torch autograd, pytorch_backend.py:446-564): from the
+ * evolved psi and lam = H psi, un-apply excitations n_ex-1..0 to both and
+ * write grads[j] = Re sum_s conj(lam_s) (F_j psi)_s (device FP64,
+ * fixed-order sums); dE/dtheta_j = 2 grads[j].  psi and lam are overwritten. */
+TQ_API size_t tq_sv_excitation_adjoint_workspace_bytes(int n, int n_ex);
+TQ_API int tq_sv_excitation_adjoint(void* psi, void* lam, int n, int dtype, const tq_excitation* exc, int n_ex,
+                                    const double* sincos, double* grads, void* ws, size_t ws_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

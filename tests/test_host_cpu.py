@@ -408,3 +408,24 @@ def test_lowering_follows_reference_dispatch():
     assert g.kind == "kraus" and g.qubits == (0,) and g.status == 0.3 and len(g.kraus) == 1
     with pytest.raises(NotImplementedError):
         lower_ops(_C(1, [("pulse", 0, "p")]), mode="run")
+
+
+def test_excitation_records_layout_and_masks():
+    """tq_excitation records: the C struct's 48-byte layout, masks splitting
+    the excitation bits, ascending bit list, Z mask disjoint from them."""
+    from tyxonq_gb300 import chem
+    from tyxonq_gb300.excitation import EXCITATION_DTYPE, excitation_records
+
+    assert EXCITATION_DTYPE.itemsize == 48
+    n = 12
+    ex, _ = chem.uccsd_excitations(2, 4)
+    rec = excitation_records(n, ex)
+    for r, f in zip(rec, ex):
+        allbits = sum(1 << x for x in f)
+        assert int(r["m_neg"]) | int(r["m_pos"]) == allbits and int(r["m_neg"]) & int(r["m_pos"]) == 0
+        assert int(r["zmask"]) & allbits == 0 and r["sign"] in (-1, 1) and r["k"] == len(f)
+        assert list(r["bits"][:len(f)]) == sorted(f)
+    with pytest.raises(ValueError):
+        excitation_records(n, [(0, 0)])
+    with pytest.raises(ValueError):
+        excitation_records(n, [(0, 1, 2)])

@@ -1,4 +1,6 @@
-// CI-space UCC: the state restricted to determinants with fixed alpha / beta
+// UCC excitations.  Statevector form (k_exc_*): each excitation rotates the
+// pairs of basis states it changes (tq_excitation in tq_sv.h).
+// CI-space form: the state restricted to determinants with fixed alpha / beta
 // electron counts (real amplitudes).  Each excitation j maps determinant i to
 // perm_j[i] with a sign, and evolves
 //   c <- c + (1 - cos t_j) f2_j * c + sin t_j * f_j * c[perm_j]
@@ -277,6 +279,107 @@ static int ci_smem_optin() {
   return v;
 }
 
+// ---------------------------------------------------------------------------
+// Statevector excitations.  Thread t of the pair range [0, 2^(n-k)) spreads t
+// over the non-excitation bits (a zero inserted at each excitation bit,
+// ascending), forms s_neg / s_pos and rotates the pair; every other amplitude
+// is untouched.
+__device__ __forceinline__ bool exc_ok(const tq_excitation& e, int n) {
+  if (e.k != 2 && e.k != 4) return false;
+  uint64_t all = 0;
+  int prev = -1;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    if (b < e.k) {
+      if (e.bits[b] <= prev || e.bits[b] >= n) return false;
+      prev = e.bits[b];
+      all |= 1ull << e.bits[b];
+    }
+  }
+  return (e.m_neg | e.m_pos) == all && (e.m_neg & e.m_pos) == 0 && (e.zmask & all) == 0;
+}
+
+__device__ __forceinline__ uint64_t exc_spread(uint64_t x, const tq_excitation& e) {
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    if (b < e.k) {
+      const int p = e.bits[b];
+      x = ((x >> p) << (p + 1)) | (x & ((1ull << p) - 1));
+    }
+  }
+  return x;
+}
+
+template <typename R>
+__global__ void k_exc_apply(typename C2<R>::T* __restrict__ psi, int n, const tq_excitation* __restrict__ exc, int j,
+                            const double* __restrict__ sincos, int reverse) {
+  const tq_excitation e = exc[j];
+  if (!exc_ok(e, n)) return;
+  const R s = (R)(reverse ? -sincos[2 * j] : sincos[2 * j]), c = (R)sincos[2 * j + 1];
+  const uint64_t np = 1ull << (n - e.k);
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < np; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t base = exc_spread(t, e), sn = base | e.m_neg, sp = base | e.m_pos;
+    const R f = (__popcll(sn & e.zmask) & 1) ? (e.sign > 0 ? s : -s) : (e.sign > 0 ? -s : s);
+    const typename C2<R>::T a = psi[sn], b = psi[sp];
+    typename C2<R>::T a2, b2;
+    a2.x = c * a.x + f * b.x;
+    a2.y = c * a.y + f * b.y;
+    b2.x = c * b.x - f * a.x;
+    b2.y = c * b.y - f * a.y;
+    psi[sn] = a2;
+    psi[sp] = b2;
+  }
+}
+
+// Un-apply excitation j to psi and lam, then this block's part of
+// Re sum conj(lam) F psi = sum over pairs phi (Re conj(lam_n) psi_p - Re conj(lam_p) psi_n).
+template <typename R>
+__global__ void k_exc_adjoint(typename C2<R>::T* __restrict__ psi, typename C2<R>::T* __restrict__ lam, int n,
+                              const tq_excitation* __restrict__ exc, int j, const double* __restrict__ sincos,
+                              double* __restrict__ part) {
+  __shared__ double sh[32];
+  const tq_excitation e = exc[j];
+  double acc = 0.0;
+  if (exc_ok(e, n)) {
+    const R s = (R)(-sincos[2 * j]), c = (R)sincos[2 * j + 1];
+    const uint64_t np = 1ull << (n - e.k);
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < np;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+      const uint64_t base = exc_spread(t, e), sn = base | e.m_neg, sp = base | e.m_pos;
+      const bool odd = __popcll(sn & e.zmask) & 1;
+      const bool phi_pos = odd == (e.sign > 0);
+      const R f = phi_pos ? s : -s;
+      typename C2<R>::T a = psi[sn], b = psi[sp], la = lam[sn], lb = lam[sp];
+      typename C2<R>::T a2, b2, la2, lb2;
+      a2.x = c * a.x + f * b.x;
+      a2.y = c * a.y + f * b.y;
+      b2.x = c * b.x - f * a.x;
+      b2.y = c * b.y - f * a.y;
+      la2.x = c * la.x + f * lb.x;
+      la2.y = c * la.y + f * lb.y;
+      lb2.x = c * lb.x - f * la.x;
+      lb2.y = c * lb.y - f * la.y;
+      psi[sn] = a2;
+      psi[sp] = b2;
+      lam[sn] = la2;
+      lam[sp] = lb2;
+      const double g = (double)la2.x * (double)b2.x + (double)la2.y * (double)b2.y -
+                       ((double)lb2.x * (double)a2.x + (double)lb2.y * (double)a2.y);
+      acc += phi_pos ? g : -g;
+    }
+  }
+  acc = ci_block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+static int exc_blocks(int n) {
+  // one grid size for every excitation of a state (fixed partial count per excitation)
+  const int64_t pairs = n >= 2 ? (1ll << (n - 2)) : 1;
+  int64_t b = (pairs + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  return (int)(b < 1 ? 1 : b);
+}
+
 static int ci_blocks(int64_t D) {
   int64_t b = (D + 255) / 256;
   if (b > 1216) b = 1216;
@@ -470,5 +573,55 @@ extern "C" int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const 
 #undef TQ_CI_SWEEPS
   k_ci_segsum<<<grad ? 1 + n_ex : 1, 256, 0, s>>>(part, part_start, out);
   TQ_CHECK_LAUNCH("tq_ci_energy_grad");
+  return TQ_OK;
+}
+
+extern "C" int tq_sv_apply_excitations(void* psi, int n, int dtype, const tq_excitation* exc, int n_ex,
+                                       const double* sincos, int reverse, void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (n_ex < 0 || n < 2) return fail(TQ_ERR_ARG, "tq_sv_apply_excitations: n=%d, n_ex=%d", n, n_ex);
+  if (n_ex == 0) return TQ_OK;
+  if (!psi || !exc || !sincos) return fail(TQ_ERR_ARG, "tq_sv_apply_excitations: NULL pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = exc_blocks(n);
+  for (int q = 0; q < n_ex; ++q) {
+    const int j = reverse ? n_ex - 1 - q : q;
+    if (dtype == TQ_C64)
+      k_exc_apply<float><<<nb, 256, 0, s>>>((float2*)psi, n, exc, j, sincos, reverse);
+    else
+      k_exc_apply<double><<<nb, 256, 0, s>>>((double2*)psi, n, exc, j, sincos, reverse);
+  }
+  TQ_CHECK_LAUNCH("tq_sv_apply_excitations");
+  return TQ_OK;
+}
+
+extern "C" size_t tq_sv_excitation_adjoint_workspace_bytes(int n, int n_ex) {
+  if (n < 2 || n_ex < 0) return 0;
+  return sizeof(double) * (size_t)exc_blocks(n) * (size_t)(n_ex > 0 ? n_ex : 1);
+}
+
+extern "C" int tq_sv_excitation_adjoint(void* psi, void* lam, int n, int dtype, const tq_excitation* exc, int n_ex,
+                                        const double* sincos, double* grads, void* ws, size_t ws_bytes, void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (n_ex < 0 || n < 2) return fail(TQ_ERR_ARG, "tq_sv_excitation_adjoint: n=%d, n_ex=%d", n, n_ex);
+  if (n_ex == 0) return TQ_OK;
+  if (!psi || !lam || !exc || !sincos || !grads) return fail(TQ_ERR_ARG, "tq_sv_excitation_adjoint: NULL pointer");
+  const size_t need = tq_sv_excitation_adjoint_workspace_bytes(n, n_ex);
+  if (!ws || ws_bytes < need)
+    return fail(TQ_ERR_WORKSPACE, "tq_sv_excitation_adjoint: workspace of %zu bytes < %zu", ws_bytes, need);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = exc_blocks(n);
+  double* part = (double*)ws;
+  for (int j = n_ex - 1; j >= 0; --j) {
+    if (dtype == TQ_C64)
+      k_exc_adjoint<float><<<nb, 256, 0, s>>>((float2*)psi, (float2*)lam, n, exc, j, sincos, part + (int64_t)j * nb);
+    else
+      k_exc_adjoint<double><<<nb, 256, 0, s>>>((double2*)psi, (double2*)lam, n, exc, j, sincos,
+                                               part + (int64_t)j * nb);
+  }
+  k_ci_finalize<<<n_ex, 256, 0, s>>>(part, nb, grads);
+  TQ_CHECK_LAUNCH("tq_sv_excitation_adjoint");
   return TQ_OK;
 }

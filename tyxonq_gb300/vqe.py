@@ -8,9 +8,10 @@ parameters, ``energy(params)`` and ``energy_and_grad(params)`` returning
 (float, float64 ndarray) like hea.py:231-266.  Gradients come from the adjoint
 kernels instead of autograd / finite differences.
 
-``UCCSD`` mirrors the statevector numeric path of
-applications/chem/algorithms/ucc.py:416-510 for integrals given explicitly:
-trotterised UCCSD from the Hartree-Fock bitstring (tyxonq_gb300.chem).
+``UCCSD`` mirrors the numeric paths of applications/chem/algorithms/
+ucc.py:416-510 for integrals given explicitly: UCCSD from the Hartree-Fock
+bitstring (tyxonq_gb300.chem) with exact excitations on the statevector, as
+Pauli-string exponentials (trotter=True), or in CI space (engine="civector").
 Molecule construction through pyscf is outside this package.
 """
 from __future__ import annotations
@@ -89,13 +90,17 @@ class HEA:
 
 
 class UCCSD:
-    """engine="statevector" (default): trotterised Pauli rotations on the
-    n-qubit state with adjoint gradients; engine="civector": the CI-space
+    """engine="statevector" (default): the excitations applied exactly on the
+    n-qubit state (statevector_ops.py evolve_excitation; tyxonq_gb300.excitation)
+    with a reverse-sweep gradient, or with trotter=True the same ansatz as
+    products of Pauli-string exponentials (the circuit form of ucc.py with
+    trotter=True; exact too, as the Pauli words of one excitation commute)
+    through the fused-pass adjoint engine; engine="civector": the CI-space
     evolution of civector_ops.py on the determinants with n_elec / 2 electrons
-    per spin (tyxonq_gb300.ci), FP64."""
+    per spin (tyxonq_gb300.ci), FP64.  One parameter per excitation."""
 
     def __init__(self, int1e: np.ndarray, int2e: np.ndarray, n_elec: int, e_core: float = 0.0,
-                 dtype=torch.complex64, device="cuda", engine: str = "statevector"):
+                 dtype=torch.complex64, device="cuda", engine: str = "statevector", trotter: bool = False):
         from .chem import hf_basis, molecular_hamiltonian, uccsd_param_gates
 
         self.int1e, self.int2e = np.asarray(int1e), np.asarray(int2e)
@@ -108,6 +113,7 @@ class UCCSD:
         self.param_gates = pg
         self.init_guess = np.zeros(self.n_params)
         self.engine = engine
+        self.trotter = bool(trotter)
         if engine == "civector":
             from .ci import CIVectorUCC
 
@@ -115,9 +121,15 @@ class UCCSD:
             # same parametrisation as the statevector engine: one angle per excitation
             self._est = CIVectorUCC(self.n_qubits, (no, no), self.ex_ops, list(range(len(self.ex_ops))),
                                     self.hamiltonian, device=device)
-        elif engine == "statevector":
+        elif engine == "statevector" and trotter:
             self._est = ParametricEstimator(self.n_qubits, pg, self.n_params, self.hamiltonian, dtype=dtype,
                                             device=device, init_basis=hf_basis(self.n_qubits, self.n_elec // 2))
+        elif engine == "statevector":
+            from .excitation import ExcitationEstimator
+
+            self._est = ExcitationEstimator(self.n_qubits, self.ex_ops, list(range(len(self.ex_ops))),
+                                            self.n_params, self.hamiltonian, dtype=dtype, device=device,
+                                            init_basis=hf_basis(self.n_qubits, self.n_elec // 2))
         else:
             raise ValueError(f"unknown UCC engine {engine!r} (statevector | civector)")
 
