@@ -167,7 +167,9 @@ TQ_API int tq_sv_sample_noalloc(const void* psi, int n, int dtype, int64_t shots
 /* A Pauli-sum Hamiltonian H = sum_k c_k P_k in flip-mask groups.
  * Term k: P_k |i> = i^{ny_k} (-1)^{popc(i & zy_k)} |i ^ flip>, with
  * flip = bits carrying X or Y, zy = bits carrying Y or Z, ny = #Y.
- * weight = c_k * i^{ny_k} (complex: one of re/im is zero).
+ * weight = c_k * i^{ny_k} (complex: one of re/im is zero); f_re / f_im hold
+ * the weight rounded to float, read by the complex64 kernels (this GPU runs
+ * double -> float conversions at its FP64 rate, a small fraction of FP32).
  * Groups are contiguous term ranges sharing one flip mask.  Tables live in
  * device memory.  Semantics equal pauli_string_to_matrix / pauli_string_sum_dense
  * (tyxonq/libs/quantum_library/kernels/pauli.py:65-87) without forming 4^n. */
@@ -181,6 +183,8 @@ typedef struct {
   uint64_t zy;
   double w_re;
   double w_im;
+  float f_re;
+  float f_im;
 } tq_pauli_term;
 
 /* E = <psi|H|psi> (real part) into *out_dev, FP64 accumulation, deterministic.

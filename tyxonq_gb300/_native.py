@@ -39,7 +39,8 @@ class PauliGroup(ctypes.Structure):
 
 
 class PauliTerm(ctypes.Structure):
-    _fields_ = [("zy", ctypes.c_uint64), ("w_re", ctypes.c_double), ("w_im", ctypes.c_double)]
+    _fields_ = [("zy", ctypes.c_uint64), ("w_re", ctypes.c_double), ("w_im", ctypes.c_double),
+                ("f_re", ctypes.c_float), ("f_im", ctypes.c_float)]
 
 
 _P = c_void_p

@@ -86,7 +86,8 @@ __device__ void eval_resident(const BatchArgs& A, const tq_batch_inst& I, int in
       const int sbase = gtid ^ m;
       for (int tt = 0; tt < cnt; ++tt) {
         const int zy = (int)__ldg(&A.terms[first + tt].zy);
-        const R wr = (R)__ldg(&A.terms[first + tt].w_re), wi = (R)__ldg(&A.terms[first + tt].w_im);
+        const cplx<R> w_ = term_w<R>(&A.terms[first + tt]);
+        const R wr = w_.x, wi = w_.y;
         const int p0 = __popc(sbase & zy) & 1;
         const int kz = zy >> lg;
 #pragma unroll

@@ -46,6 +46,23 @@ __device__ __forceinline__ cplx<R> cconjmul(cplx<R> a, cplx<R> b) {
   return cplx<R>(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
 
+// Weight of a Pauli term in the working precision: complex64 kernels read the
+// float copies, so no double -> float conversion (an FP64-pipe instruction)
+// runs per term and thread.
+template <typename R> struct TermW;
+template <> struct TermW<float> {
+  static __device__ __forceinline__ cplx<float> get(const tq_pauli_term* t) {
+    return cplx<float>(__ldg(&t->f_re), __ldg(&t->f_im));
+  }
+};
+template <> struct TermW<double> {
+  static __device__ __forceinline__ cplx<double> get(const tq_pauli_term* t) {
+    return cplx<double>(__ldg(&t->w_re), __ldg(&t->w_im));
+  }
+};
+template <typename R>
+__device__ __forceinline__ cplx<R> term_w(const tq_pauli_term* t) { return TermW<R>::get(t); }
+
 // 2x2 and 4x4 complex matrices passed by value as kernel parameters.
 template <typename R> struct Mat2 { cplx<R> m[4]; };
 template <typename R> struct Mat4 { cplx<R> m[16]; };

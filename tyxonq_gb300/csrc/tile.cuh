@@ -187,7 +187,8 @@ __device__ __forceinline__ cplx<R> group_f(const tq_pauli_term* __restrict__ ter
   R fr = 0, fi = 0;
   for (int t = 0; t < cnt; ++t) {
     const uint64_t zy = __ldg(&terms[first + t].zy);
-    const R wr = (R)__ldg(&terms[first + t].w_re), wi = (R)__ldg(&terms[first + t].w_im);
+    const cplx<R> w_ = term_w<R>(&terms[first + t]);
+    const R wr = w_.x, wi = w_.y;
     const bool neg = __popcll(i & zy) & 1;
     fr += neg ? -wr : wr;
     fi += neg ? -wi : wi;

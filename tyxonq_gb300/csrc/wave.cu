@@ -207,7 +207,8 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
           // few terms: signs per amplitude directly
           for (int tt = 0; tt < cnt; ++tt) {
             const uint64_t zy = __ldg(&terms[first + tt].zy);
-            const R wr = (R)__ldg(&terms[first + tt].w_re), wi = (R)__ldg(&terms[first + tt].w_im);
+            const cplx<R> w_ = term_w<R>(&terms[first + tt]);
+            const R wr = w_.x, wi = w_.y;
             const int p0 = __popcll(sbase & zy) & 1;
             const int c = (int)(zy >> 8) & (PER - 1);
 #pragma unroll
@@ -224,7 +225,8 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
           R sr = 0, si = 0;
           for (int tt = 0; tt < cnt; ++tt) {
             const uint64_t zy = __ldg(&terms[first + tt].zy);
-            const R wr = (R)__ldg(&terms[first + tt].w_re), wi = (R)__ldg(&terms[first + tt].w_im);
+            const cplx<R> w_ = term_w<R>(&terms[first + tt]);
+            const R wr = w_.x, wi = w_.y;
             const int c = (int)(zy >> 8) & (PER - 1);
             if (c != cur) {  // same for every thread: the term is shared
 #pragma unroll

@@ -21,7 +21,7 @@ from typing import Iterable, Sequence
 import numpy as np
 
 GROUP_DTYPE = np.dtype([("flip", "<u8"), ("first_term", "<i4"), ("n_terms", "<i4")])
-TERM_DTYPE = np.dtype([("zy", "<u8"), ("w_re", "<f8"), ("w_im", "<f8")])
+TERM_DTYPE = np.dtype([("zy", "<u8"), ("w_re", "<f8"), ("w_im", "<f8"), ("f_re", "<f4"), ("f_im", "<f4")])
 _CODE = {"I": 0, "X": 1, "Y": 2, "Z": 3}
 _I_POW = [(1.0, 0.0), (0.0, 1.0), (-1.0, 0.0), (0.0, -1.0)]
 
@@ -105,6 +105,8 @@ class PauliSum:
         terms["zy"] = zy[order]
         terms["w_re"] = self.coeffs[order] * pw[:, 0] if self.n_terms else 0
         terms["w_im"] = self.coeffs[order] * pw[:, 1] if self.n_terms else 0
+        terms["f_re"] = terms["w_re"]  # float copies for the complex64 kernels
+        terms["f_im"] = terms["w_im"]
         fs = flip[order]
         starts = np.flatnonzero(np.r_[True, fs[1:] != fs[:-1]]) if self.n_terms else np.zeros(0, np.int64)
         g = np.zeros(len(starts), dtype=GROUP_DTYPE)
