@@ -359,6 +359,24 @@ TQ_API int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_ite
                        const tq_tile_op* ops, const tq_pauli_group* groups, const tq_pauli_term* terms,
                        const double* theta, void* pool, double* partials, int max_pass_ops, void* stream);
 
+/* H psi and / or <psi|H|psi> of one state (n >= 12) through the wave H psi
+ * kernel: output tiles of 4096 amplitudes, 16 per thread, each group's terms
+ * summed per class of the bits that tell a thread's amplitudes apart, then a
+ * 16-point Walsh-Hadamard transform; partner tiles staged in shared memory
+ * once per distinct flip >> 12.  The group list is cut into slices (more CTAs
+ * for small states) whose partial outputs are added in slice order.  Same
+ * semantics as tq_sv_apply_pauli_sum / tq_sv_pauli_expectation; groups must
+ * be sorted by flip, and terms sorted by bits 8..11 of zy within each group
+ * run fastest.  out or energy_out (device FP64) may be NULL, not both (with
+ * out NULL no output is written at all); ws holds
+ * tq_sv_pauli_sum_tiled_workspace_bytes(n, dtype, n_groups, out != NULL)
+ * bytes (partial outputs only when there are several slices and an output).
+ * Fixed-order sums: bit-identical replays. */
+TQ_API size_t tq_sv_pauli_sum_tiled_workspace_bytes(int n, int dtype, int n_groups, int with_out);
+TQ_API int tq_sv_pauli_sum_tiled(const void* psi, void* out, int n, int dtype, const tq_pauli_group* groups,
+                                 int n_groups, const tq_pauli_term* terms, int n_terms, double* energy_out, void* ws,
+                                 size_t ws_bytes, void* stream);
+
 /* Fixed-order reductions of wave partials: out[k] (+)= scale[k] * sum of
  * partials[first[k] + j * stride[k]] for j < count[k]; accumulate != 0 adds. */
 TQ_API int tq_wave_reduce(const double* partials, const int32_t* first, const int32_t* count, const int32_t* stride,

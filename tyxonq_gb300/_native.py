@@ -90,6 +90,8 @@ SIGNATURES: dict[str, tuple] = {
     "tq_ci_embed": (c_int, [_P, _P, c_int64, _P, c_int, c_int, _P]),
     "tq_ci_gather": (c_int, [_P, _P, c_int64, c_int, _P, _P]),
     "tq_ci_spmv": (c_int, [_P, _P, _P, c_int64, _P, _P, _P]),
+    "tq_sv_pauli_sum_tiled_workspace_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
+    "tq_sv_pauli_sum_tiled": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_apply_excitations": (c_int, [_P, c_int, c_int, _P, c_int, _P, c_int, _P]),
     "tq_sv_excitation_adjoint_workspace_bytes": (c_size_t, [c_int, c_int]),
     "tq_sv_excitation_adjoint": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, _P, _P, c_size_t, _P]),

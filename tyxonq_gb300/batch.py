@@ -29,7 +29,7 @@ import torch
 
 from . import _native as nat
 from . import kernels as K
-from .hamiltonian import GROUP_DTYPE, TERM_DTYPE, PauliSum
+from .hamiltonian import GROUP_DTYPE, TERM_DTYPE, PauliSum, sort_terms_by_class
 from .ir import Gate, _rot_gate
 from .program import TILE_OP_DTYPE, PassPlan, TilePass, encode_passes, plan_passes
 
@@ -80,21 +80,6 @@ class Schedule:
         if n <= self.res1_max:
             return "res1", 1, 1024
         return "streamed", 1, 1024
-
-
-def sort_terms_by_class(groups: np.ndarray, terms: np.ndarray, hbits: int) -> np.ndarray:
-    """Order each group's terms by their Z/Y bits 8 .. hbits-1 (the bits that
-    tell apart the amplitudes one thread of the wave H psi kernel holds), so
-    the kernel's per-class sums switch class at most 2^(hbits-8) - 1 times per
-    group.  Groups keep their term ranges; only the order inside changes."""
-    if len(terms) == 0 or hbits <= 8:
-        return terms
-    gid = np.repeat(np.arange(len(groups)), groups["n_terms"])
-    first = np.repeat(groups["first_term"], groups["n_terms"])
-    order_in = np.arange(len(terms)) - first  # position inside the group (groups are contiguous, in order)
-    cls = (terms["zy"] >> np.uint64(8)) & np.uint64((1 << (hbits - 8)) - 1)
-    idx = np.lexsort((order_in, cls.astype(np.int64), gid))
-    return terms[idx]
 
 
 def structure_gates(structure) -> tuple[list[Gate], dict]:

@@ -147,7 +147,7 @@ template <typename R, int PER>
 __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restrict__ items, int n_items, int hbits,
                                                    const tq_pauli_group* __restrict__ groups,
                                                    const tq_pauli_term* __restrict__ terms, void* pool,
-                                                   double* partials) {
+                                                   void* lam_pool, double* partials) {
   typedef typename C2<R>::T T2;
   extern __shared__ __align__(16) unsigned char smem[];
   cplx<R>* src = reinterpret_cast<cplx<R>*>(smem);
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
     const int hb = I.n < hbits ? I.n : hbits;
     const int HN = 1 << hb;
     const T2* psi = reinterpret_cast<const T2*>(pool) + I.psi_off;
-    T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
+    T2* lam = lam_pool ? reinterpret_cast<T2*>(lam_pool) + I.lam_off : nullptr;  // null: energy partials only
     const int64_t tile = I.tile;
     const int64_t t0 = tile << hb;
     cplx<R> acc[PER];
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
         T2 o;
         o.x = acc[k].x;
         o.y = acc[k].y;
-        lam[t0 + j] = o;
+        if (lam) lam[t0 + j] = o;
       }
     }
     double v = (double)eloc;
@@ -433,7 +433,7 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
 #define TQ_HPSI(PER_)                                                                                          \
   e = cudaFuncSetAttribute(k_wave_hpsi<R, PER_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);        \
   if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");                                  \
-  k_wave_hpsi<R, PER_><<<grid, 256, sm, s>>>(items, n_items, hbits, groups, terms, pool, partials);
+  k_wave_hpsi<R, PER_><<<grid, 256, sm, s>>>(items, n_items, hbits, groups, terms, pool, pool, partials);
     switch (hbits) {
       case 8: TQ_HPSI(1) break;
       case 9: TQ_HPSI(2) break;
@@ -477,9 +477,144 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
   return TQ_OK;
 }
 
+// ---------------------------------------------------------------------------
+// One state through k_wave_hpsi: items = (output tile, group slice).  Slice s
+// of tile t writes its partial H psi to buf[s] (straight to out when there is
+// one slice; nowhere for the energy alone) and its energy partial to
+// partials[t * S + s].
+constexpr int kTiledHb = 12;
+
+__global__ void k_tiled_items(tq_wave_item* items, int n, int tiles, int slices, int n_groups, int64_t slice_stride) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= tiles * slices) return;
+  const int t = it / slices, sl = it % slices;
+  const int g0 = (int)((int64_t)n_groups * sl / slices), g1 = (int)((int64_t)n_groups * (sl + 1) / slices);
+  tq_wave_item I;
+  I.psi_off = 0;
+  I.lam_off = (int64_t)sl * slice_stride;
+  I.pass = 0;
+  I.tile = t;
+  I.theta_off = 0;
+  I.part_off = it;
+  I.n = n;
+  I.group_begin = g0;
+  I.group_count = g1 - g0;
+  I.basis_lo = -1;
+  items[it] = I;
+}
+
+template <typename R>
+__global__ void k_slice_sum(const typename C2<R>::T* __restrict__ buf, int slices, int64_t N,
+                            typename C2<R>::T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    typename C2<R>::T a = buf[i];
+    for (int sl = 1; sl < slices; ++sl) {
+      const typename C2<R>::T b = buf[(int64_t)sl * N + i];
+      a.x += b.x;
+      a.y += b.y;
+    }
+    out[i] = a;
+  }
+}
+
+__global__ void k_sum_partials(const double* __restrict__ p, int n, double* out) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += p[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    out[0] = s;
+  }
+}
+
+static void tiled_shape(int n, int n_groups, int& tiles, int& slices) {
+  tiles = 1 << (n - kTiledHb);
+  slices = (2 * 152 + tiles - 1) / tiles;
+  if (slices > 16) slices = 16;
+  if (slices > n_groups) slices = n_groups;
+  if (slices < 1) slices = 1;
+}
+
+static size_t tiled_buf_amps(int n, int slices, bool have_out) {
+  return (have_out && slices > 1) ? (size_t)slices << n : 0;
+}
+
 }  // namespace tq
 
 using namespace tq;
+
+extern "C" size_t tq_sv_pauli_sum_tiled_workspace_bytes(int n, int dtype, int n_groups, int with_out) {
+  if (n < kTiledHb || n > 40 || (dtype != TQ_C64 && dtype != TQ_C128) || n_groups < 0) return 0;
+  int tiles, slices;
+  tiled_shape(n, n_groups, tiles, slices);
+  const size_t S = dtype == TQ_C64 ? 8 : 16;
+  const size_t items = (size_t)tiles * slices;
+  size_t b = items * sizeof(tq_wave_item);
+  b = (b + 255) & ~(size_t)255;
+  b += items * sizeof(double);
+  b = (b + 255) & ~(size_t)255;
+  return b + S * tiled_buf_amps(n, slices, with_out != 0);
+}
+
+extern "C" int tq_sv_pauli_sum_tiled(const void* psi, void* out, int n, int dtype, const tq_pauli_group* groups,
+                                     int n_groups, const tq_pauli_term* terms, int n_terms, double* energy_out,
+                                     void* ws, size_t ws_bytes, void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (n < kTiledHb) return fail(TQ_ERR_ARG, "tq_sv_pauli_sum_tiled: n=%d below %d", n, kTiledHb);
+  if (!psi || (!out && !energy_out)) return fail(TQ_ERR_ARG, "tq_sv_pauli_sum_tiled: nothing to compute");
+  if (out == psi) return fail(TQ_ERR_ARG, "tq_sv_pauli_sum_tiled: out aliases psi");
+  if (n_groups < 0 || n_terms < 0 || (n_groups > 0 && (!groups || !terms)))
+    return fail(TQ_ERR_ARG, "tq_sv_pauli_sum_tiled: bad Pauli tables");
+  const size_t need = tq_sv_pauli_sum_tiled_workspace_bytes(n, dtype, n_groups, out != nullptr);
+  if (!ws || ws_bytes < need)
+    return fail(TQ_ERR_WORKSPACE, "tq_sv_pauli_sum_tiled: workspace of %zu bytes < %zu", ws_bytes, need);
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t S = dtype == TQ_C64 ? 8 : 16;
+  const int64_t N = int64_t(1) << n;
+  if (n_groups == 0) {
+    cudaError_t e = cudaSuccess;
+    if (out) e = cudaMemsetAsync(out, 0, S * (size_t)N, s);
+    if (e == cudaSuccess && energy_out) e = cudaMemsetAsync(energy_out, 0, sizeof(double), s);
+    if (e != cudaSuccess) return cuda_status(e, "tq_sv_pauli_sum_tiled: clear");
+    return TQ_OK;
+  }
+  int tiles, slices;
+  tiled_shape(n, n_groups, tiles, slices);
+  const int items = tiles * slices;
+  unsigned char* w = (unsigned char*)ws;
+  tq_wave_item* it = (tq_wave_item*)w;
+  size_t off = ((size_t)items * sizeof(tq_wave_item) + 255) & ~(size_t)255;
+  double* part = (double*)(w + off);
+  off = (off + (size_t)items * sizeof(double) + 255) & ~(size_t)255;
+  void* buf = tiled_buf_amps(n, slices, out != nullptr) ? (void*)(w + off) : out;  // null: energy only
+  k_tiled_items<<<(items + 255) / 256, 256, 0, s>>>(it, n, tiles, slices, n_groups, N);
+  const size_t sm = 2 * (S << kTiledHb);
+  cudaError_t e;
+  if (dtype == TQ_C64) {
+    e = cudaFuncSetAttribute(k_wave_hpsi<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return cuda_status(e, "tq_sv_pauli_sum_tiled: smem attribute");
+    k_wave_hpsi<float, 16><<<items, 256, sm, s>>>(it, items, kTiledHb, groups, terms, const_cast<void*>(psi), buf,
+                                                  part);
+    if (out && buf != out)
+      k_slice_sum<float><<<grid_for(N, 256), 256, 0, s>>>((const float2*)buf, slices, N, (float2*)out);
+  } else {
+    e = cudaFuncSetAttribute(k_wave_hpsi<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return cuda_status(e, "tq_sv_pauli_sum_tiled: smem attribute");
+    k_wave_hpsi<double, 16><<<items, 256, sm, s>>>(it, items, kTiledHb, groups, terms, const_cast<void*>(psi), buf,
+                                                   part);
+    if (out && buf != out)
+      k_slice_sum<double><<<grid_for(N, 256), 256, 0, s>>>((const double2*)buf, slices, N, (double2*)out);
+  }
+  if (energy_out) k_sum_partials<<<1, 256, 0, s>>>(part, items, energy_out);
+  TQ_CHECK_LAUNCH("tq_sv_pauli_sum_tiled");
+  return TQ_OK;
+}
 
 extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
                            int stage_bits, const tq_tile_pass* passes, const tq_tile_stage* stages,

@@ -130,13 +130,45 @@ class PauliSum:
             return hit
         g, t = self.pack()
         gd = torch.from_numpy(np.frombuffer(g.tobytes() or b"\0" * 16, dtype=np.uint8).copy()).to(device)
-        td = torch.from_numpy(np.frombuffer(t.tobytes() or b"\0" * 24, dtype=np.uint8).copy()).to(device)
+        td = torch.from_numpy(np.frombuffer(t.tobytes() or b"\0" * 32, dtype=np.uint8).copy()).to(device)
+        out = (gd, td, int(g.shape[0]), int(t.shape[0]))
+        self._device_cache[key] = out
+        return out
+
+    def to_device_classed(self, device, hbits: int = 12):
+        """Like to_device, with each group's terms sorted by bits 8 .. hbits-1 of
+        zy (the order the tiled H psi kernel reads fastest), cached per device."""
+        import torch
+
+        key = f"classed{hbits}:{device}"
+        hit = self._device_cache.get(key)
+        if hit is not None:
+            return hit
+        g, t = self.pack()
+        t = sort_terms_by_class(g, t, hbits)
+        gd = torch.from_numpy(np.frombuffer(g.tobytes() or b"\0" * 16, dtype=np.uint8).copy()).to(device)
+        td = torch.from_numpy(np.frombuffer(t.tobytes() or b"\0" * 32, dtype=np.uint8).copy()).to(device)
         out = (gd, td, int(g.shape[0]), int(t.shape[0]))
         self._device_cache[key] = out
         return out
 
     def one_norm(self) -> float:
         return float(np.abs(self.coeffs).sum())
+
+
+def sort_terms_by_class(groups: np.ndarray, terms: np.ndarray, hbits: int) -> np.ndarray:
+    """Order each group's terms by their Z/Y bits 8 .. hbits-1 (the bits that
+    tell apart the amplitudes one thread of the wave H psi kernel holds), so
+    the kernel's per-class sums switch class at most 2^(hbits-8) - 1 times per
+    group.  Groups keep their term ranges; only the order inside changes."""
+    if len(terms) == 0 or hbits <= 8:
+        return terms
+    gid = np.repeat(np.arange(len(groups)), groups["n_terms"])
+    first = np.repeat(groups["first_term"], groups["n_terms"])
+    order_in = np.arange(len(terms)) - first  # position inside the group (groups are contiguous, in order)
+    cls = (terms["zy"] >> np.uint64(8)) & np.uint64((1 << (hbits - 8)) - 1)
+    idx = np.lexsort((order_in, cls.astype(np.int64), gid))
+    return terms[idx]
 
 
 def as_pauli_sum(H, n: int | None = None) -> PauliSum:

@@ -290,14 +290,29 @@ def sample(psi: torch.Tensor, shots: int, seed: int) -> torch.Tensor:
     return out
 
 
+TILED_MIN_N = 12  # H psi and <H> through the tiled kernel (tq_sv_pauli_sum_tiled) from this size up
+
+
+def _pauli_sum_tiled(psi: torch.Tensor, H, nn: int, out: torch.Tensor | None, energy: torch.Tensor | None) -> None:
+    gd, td, ng, nt = H.to_device_classed(psi.device)
+    lib = nat.load()
+    p, cap = _ws(lib.tq_sv_pauli_sum_tiled_workspace_bytes(nn, dtype_tag(psi), ng, int(out is not None)), psi.device)
+    nat.call("tq_sv_pauli_sum_tiled", _ptr(psi), _ptr(out) if out is not None else None, nn, dtype_tag(psi),
+             _ptr(gd), ng, _ptr(td), nt, _ptr(energy) if energy is not None else None, p, cap,
+             stream_ptr(psi.device))
+
+
 def pauli_expectation(psi: torch.Tensor, H, n: int | None = None) -> torch.Tensor:
     """Re <psi|H|psi> for a Pauli sum (float64 device tensor of shape (1,))."""
     nn = _check_state(psi, n)
     H = as_pauli_sum(H, nn)
     if H.n != nn:
         raise ValueError(f"Hamiltonian has {H.n} qubits, state {nn}")
-    gd, td, ng, nt = H.to_device(psi.device)
     out = torch.empty(1, dtype=torch.float64, device=psi.device)
+    if nn >= TILED_MIN_N:
+        _pauli_sum_tiled(psi, H, nn, None, out)
+        return out
+    gd, td, ng, nt = H.to_device(psi.device)
     lib = nat.load()
     p, cap = _ws(lib.tq_sv_pauli_expectation_workspace_bytes(nn, ng), psi.device)
     nat.call("tq_sv_pauli_expectation", _ptr(psi), nn, dtype_tag(psi), _ptr(gd), ng, _ptr(td), nt, _ptr(out), p, cap,
@@ -309,10 +324,13 @@ def apply_pauli_sum(psi: torch.Tensor, H, out: torch.Tensor | None = None) -> to
     """H psi into a new (or given) tensor."""
     nn = _check_state(psi)
     H = as_pauli_sum(H, nn)
-    gd, td, ng, nt = H.to_device(psi.device)
     if out is None:
         out = torch.empty_like(psi)
     _check_state(out, nn)
+    if nn >= TILED_MIN_N:
+        _pauli_sum_tiled(psi, H, nn, out, None)
+        return out
+    gd, td, ng, nt = H.to_device(psi.device)
     nat.call("tq_sv_apply_pauli_sum", _ptr(psi), _ptr(out), nn, dtype_tag(psi), _ptr(gd), ng, _ptr(td), nt,
              stream_ptr(psi.device))
     return out
