@@ -82,6 +82,7 @@ class ExcitationEstimator:
         self.psi = torch.empty(1 << self.n, dtype=dtype, device=self.device)
         self.lam = torch.empty_like(self.psi)
         self.grads = torch.zeros(max(self.n_ex, 1), dtype=torch.float64, device=self.device)
+        self._graphs: dict = {}
 
     def _upload(self, params) -> None:
         th = np.asarray(params, dtype=np.float64)[self.param_ids]
@@ -94,31 +95,60 @@ class ExcitationEstimator:
         self._copied = torch.cuda.Event()
         self._copied.record()
 
-    def state(self, params) -> torch.Tensor:
-        """The evolved statevector (device tensor, reused across calls)."""
+    def _evolve(self) -> None:
         P = ctypes.c_void_p
-        self._upload(params)
         st = K.stream_ptr(self.device)
         nat.call("tq_sv_init_basis", P(self.psi.data_ptr()), self.n, K.dtype_tag(self.psi), self.init_basis, st)
         nat.call("tq_sv_apply_excitations", P(self.psi.data_ptr()), self.n, K.dtype_tag(self.psi),
                  P(self.records.data_ptr()), self.n_ex, P(self.sincos.data_ptr()), 0, st)
-        return self.psi
 
-    def energy(self, params) -> float:
-        return float(K.pauli_expectation(self.state(params), self.H).item())
-
-    def energy_and_grad(self, params) -> tuple[float, np.ndarray]:
+    def _launch(self, grad: bool) -> torch.Tensor:
+        """Forward, <H> (and H psi + reverse sweep); angles from self.sincos."""
         P = ctypes.c_void_p
-        params = np.asarray(params, dtype=np.float64)
-        psi = self.state(params)
-        K.apply_pauli_sum(psi, self.H, out=self.lam)
-        e = K.inner_re(psi, self.lam)
+        self._evolve()
+        if not grad:
+            return K.pauli_expectation(self.psi, self.H)
+        K.apply_pauli_sum(self.psi, self.H, out=self.lam)
+        e = K.inner_re(self.psi, self.lam)
         if self.n_ex:
             lib = nat.load()
             ws, cap = K._ws(lib.tq_sv_excitation_adjoint_workspace_bytes(self.n, self.n_ex), self.device)
-            nat.call("tq_sv_excitation_adjoint", P(psi.data_ptr()), P(self.lam.data_ptr()), self.n,
-                     K.dtype_tag(psi), P(self.records.data_ptr()), self.n_ex, P(self.sincos.data_ptr()),
+            nat.call("tq_sv_excitation_adjoint", P(self.psi.data_ptr()), P(self.lam.data_ptr()), self.n,
+                     K.dtype_tag(self.psi), P(self.records.data_ptr()), self.n_ex, P(self.sincos.data_ptr()),
                      P(self.grads.data_ptr()), ws, cap, K.stream_ptr(self.device))
+        return e
+
+    def _replay(self, grad: bool) -> torch.Tensor:
+        """Run _launch as a CUDA graph (captured on first use: some 400 small
+        launches per evaluation, one per excitation and sweep)."""
+        if self.device.type != "cuda":
+            return self._launch(grad)
+        key = bool(grad)
+        hit = self._graphs.get(key)
+        if hit is None:
+            self._launch(grad)  # warm-up outside capture: workspaces, shared-memory attributes
+            torch.cuda.synchronize(self.device)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                out = self._launch(grad)
+            hit = self._graphs[key] = (g, out)
+        hit[0].replay()
+        return hit[1]
+
+    def state(self, params) -> torch.Tensor:
+        """The evolved statevector (device tensor, reused across calls)."""
+        self._upload(params)
+        self._evolve()
+        return self.psi
+
+    def energy(self, params) -> float:
+        self._upload(params)
+        return float(self._replay(False).item())
+
+    def energy_and_grad(self, params) -> tuple[float, np.ndarray]:
+        params = np.asarray(params, dtype=np.float64)
+        self._upload(params)
+        e = self._replay(True)
         gj = self.grads[:self.n_ex].cpu().numpy()
         g = np.zeros(self.n_params)
         np.add.at(g, self.param_ids, gj)
