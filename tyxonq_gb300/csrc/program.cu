@@ -121,6 +121,8 @@ __global__ void k_tile_forward(typename C2<R>::T* psi, int n, const PassArgs P, 
 
 // Adjoint pass: psi and lam tiles; per op: gradient term then un-apply.
 // Per-block slot sums go to partials[block * n_slots + slot].
+constexpr int kAdjChunk = 64;  // ops per gradient-partial flush in k_tile_adjoint
+
 template <typename R>
 __global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, int n, const PassArgs P,
                                const tq_tile_op* __restrict__ ops, const double* __restrict__ theta, int n_slots,
@@ -131,9 +133,11 @@ __global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, i
   cplx<R>* sl = reinterpret_cast<cplx<R>*>(smem + tb);
   int64_t* hoff = reinterpret_cast<int64_t*>(smem + 2 * tb);
   double* acc = reinterpret_cast<double*>(smem + 2 * tb + (sizeof(int64_t) << (P.t - P.nlow)));
-  __shared__ double red[32];
-  build_hoff(hoff, P);
   const int nops = P.op_end - P.op_begin;
+  // per-warp gradient partials of up to kAdjChunk ops, summed over warps once per chunk
+  R* wpart = reinterpret_cast<R*>(acc + nops);
+  const int nwarps = (int)(blockDim.x >> 5), warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  build_hoff(hoff, P);
   for (int k = threadIdx.x; k < nops; k += blockDim.x) acc[k] = 0.0;
   __syncthreads();
   const int64_t ntiles = int64_t(1) << (n - P.t);
@@ -145,25 +149,29 @@ __global__ void k_tile_adjoint(typename C2<R>::T* psi, typename C2<R>::T* lam, i
     for (int k = 0; k < nops; ++k) {
       const tq_tile_op& o = ops[P.op_begin + k];
       if (o.slot >= 0) {
+        // warp sums in the working precision (FP64 issues slowly on this GPU);
+        // warps are added in order at the end of the chunk
         const R phr[4] = {R(1), R(0), R(-1), R(0)}, phi[4] = {R(0), R(1), R(0), R(-1)};
         const cplx<R> ph(phr[o.gny & 3], phi[o.gny & 3]);
-        const R part = zsign<R>(o, (uint64_t)base, 0) *
-                       tile_grad_partial<R>(sp, sl, P.t, o.gxm, o.gzm, o.gcm, ph, threadIdx.x, blockDim.x);
-        double v = (double)part;
+        R v = zsign<R>(o, (uint64_t)base, 0) *
+              tile_grad_partial<R>(sp, sl, P.t, o.gxm, o.gzm, o.gcm, ph, threadIdx.x, blockDim.x);
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          double sum = 0;
-          for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += red[w];
-          acc[k] += sum;
-        }
-        __syncthreads();
+        if (lane == 0) wpart[(k % kAdjChunk) * nwarps + warp] = v;
       }
       tile_apply<R>(sp, P.t, o, threadIdx.x, blockDim.x, true, theta, (uint64_t)base);
       tile_apply<R>(sl, P.t, o, threadIdx.x, blockDim.x, true, theta, (uint64_t)base);
       __syncthreads();
+      if (k % kAdjChunk == kAdjChunk - 1 || k == nops - 1) {  // the barrier above published wpart
+        const int k0 = k - k % kAdjChunk;
+        for (int q = threadIdx.x; q <= k - k0; q += blockDim.x) {
+          if (ops[P.op_begin + k0 + q].slot < 0) continue;
+          R sum = R(0);
+          for (int w = 0; w < nwarps; ++w) sum += wpart[q * nwarps + w];
+          acc[k0 + q] += (double)sum;
+        }
+        __syncthreads();
+      }
     }
     tile_store<R>(sp, psi, base, hoff, P);
     tile_store<R>(sl, lam, base, hoff, P);
@@ -259,7 +267,8 @@ static int run_adj(void* psi, void* lam, int n, const tq_tile_pass* passes, int 
     const PassArgs P = to_args(passes[p]);
     const int nops = P.op_end - P.op_begin;
     if (nops == 0) continue;
-    const size_t smem = 2 * (sizeof(cplx<R>) << P.t) + (sizeof(int64_t) << (P.t - P.nlow)) + sizeof(double) * nops;
+    const size_t smem = 2 * (sizeof(cplx<R>) << P.t) + (sizeof(int64_t) << (P.t - P.nlow)) + sizeof(double) * nops +
+                        sizeof(R) * kAdjChunk * (tile_threads(P.t) / 32);
     if (smem > 227 * 1024) return fail(TQ_ERR_ARG, "tq_sv_adjoint_tiles: pass %d needs %zu B shared memory", p, smem);
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(k_tile_adjoint<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
