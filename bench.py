@@ -397,6 +397,17 @@ def run_case(args):
     if args.case == "small":
         print(json.dumps({"case": "small", **bench_small_configs()}))
         return
+    if args.case == "civector":
+        from tyxonq_gb300 import chem
+        from tyxonq_gb300.vqe import UCCSD
+
+        h, g = chem.random_integrals(8, seed=7)
+        m = UCCSD(h, g, n_elec=4, engine="civector")
+        p = np.random.default_rng(2).uniform(-0.3, 0.3, m.n_params)
+        for _ in range(args.warmup + args.steps):
+            e, _ = m.energy_and_grad(p)
+        print(json.dumps({"case": "civector", "D": m._est.D, "energy": e}))
+        return
     from tyxonq_gb300.batch import BatchedVQE
     from tyxonq_gb300.workloads import batched_vqe
 
@@ -424,8 +435,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--count", type=int, default=4096)
-    ap.add_argument("--case", default="full", choices=["full", "gates", "batched", "small"],
-                    help="gates / batched: run only that part (profiling captures); full: the benchmark line")
+    ap.add_argument("--case", default="full", choices=["full", "gates", "batched", "small", "civector"],
+                    help="gates / batched / small / civector (16-qubit UCCSD in CI space): run only that part "
+                         "(profiling captures); full: the benchmark line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
