@@ -445,11 +445,13 @@ TQ_API int tq_ci_spmv(const int64_t* row_ptr, const int32_t* col, const double* 
  * {i, (p << 1) | (fphase_j[i] < 0)} with p = fperm_j[i] > i, fphase_j[p] =
  * -fphase_j[i] and f2phase_j = -1 on both (every other determinant has
  * fphase_j = f2phase_j = 0); excitation j owns pairs pair_start[j] ..
- * pair_start[j + 1] (int64 [n_ex + 1], device), at most max_pairs <= 2048
- * of them (TQ_ERR_RANGE above).
- * part_start (int64 [n_ex + 2], device) places the partial sums:
- * part_start[0] = 0, part_start[1] = min(D, 1024), part_start[2 + j] =
- * part_start[1 + j] + min(pairs of j, 1024); n_partials = part_start[n_ex + 1].
+ * pair_start[j + 1] (int64 [n_ex + 1], device), at most max_pairs <= 2 *
+ * threads of them (TQ_ERR_RANGE above).  threads (256 or 1024) is the CTA
+ * size of the sweeps: 256 keeps the per-excitation barrier short when every
+ * excitation has at most 512 pairs.  part_start (int64 [n_ex + 2], device)
+ * places the partial sums: part_start[0] = 0, part_start[1] = min(D,
+ * threads), part_start[2 + j] = part_start[1 + j] + min(pairs of j,
+ * threads); n_partials = part_start[n_ex + 1].
  * sin_omc: DEVICE FP64 [n_ex][2] = {sin t_j, 1 - cos t_j}.  ket_out (D
  * doubles, device) receives the evolved ket unless NULL; ws holds
  * tq_ci_energy_grad_workspace_bytes(D, n_partials) bytes.  Pairs outside
@@ -459,8 +461,8 @@ TQ_API size_t tq_ci_energy_grad_workspace_bytes(int64_t D, int64_t n_partials);
 TQ_API int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const int32_t* pairs,
                              const int64_t* pair_start, int64_t max_pairs, const int64_t* part_start,
                              int64_t n_partials, const double* sin_omc, const int64_t* row_ptr, const int32_t* col,
-                             const double* val, int grad, double* ket_out, double* out, void* ws, size_t ws_bytes,
-                             void* stream);
+                             const double* val, int grad, int threads, double* ket_out, double* out, void* ws,
+                             size_t ws_bytes, void* stream);
 
 /* One fermionic excitation on the n-qubit statevector (fermion mode m =
  * basis bit m, i.e. qubit n-1-m).  F = T - T^dagger changes only the basis

@@ -46,12 +46,13 @@ def _csr_apply(strings, H):
 
 
 @pytest.mark.parametrize("n_orb,n_elec,fused", [(4, 4, True), (4, 4, False), (7, 6, True), (7, 6, False),
-                                                (8, 8, True)])
+                                                (8, 6, True), (8, 8, True)])
 def test_civector_one_cta_and_stepwise_paths(n_orb, n_elec, fused):
     """Both GPU paths (one single-CTA launch for D up to the shared-memory
     limit; one launch per excitation step) against the oracle's reverse sweep
     with H as the CI-space CSR (checked against the full-space H on the CPU).
-    (8, 8): D = 4900 with up to 1400 pairs per excitation, two per thread."""
+    Sweep CTAs: (4, 4) 256 threads, one pair each; (7, 6) 256 threads, up to
+    two; (8, 6) 1024 threads, one; (8, 8) D = 4900, 1024 threads, up to two."""
     from tyxonq_gb300.ci import CIVectorUCC
 
     no = n_elec // 2

@@ -146,7 +146,13 @@ def ci_hamiltonian_csr(strings: np.ndarray, H) -> tuple[np.ndarray, np.ndarray, 
     return np.cumsum(row_ptr), c[o].astype(np.int32), v[o]
 
 
-CI_SWEEP_THREADS = 1024  # threads of the one-CTA sweeps in csrc/ci.cu (partials per sum: at most this many)
+CI_SWEEP_THREADS = 1024  # largest CTA of the one-CTA sweeps in csrc/ci.cu
+
+
+def sweep_threads(max_pairs: int) -> int:
+    """CTA size of the sweeps: 256 (a shorter per-excitation barrier) when no
+    excitation has more than 512 pairs, else 1024."""
+    return 256 if max_pairs <= 512 else CI_SWEEP_THREADS
 
 
 def excitation_pairs(fperm: np.ndarray, fphase: np.ndarray, f2phase: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
@@ -175,10 +181,10 @@ def excitation_pairs(fperm: np.ndarray, fphase: np.ndarray, f2phase: np.ndarray)
     return pairs, np.asarray(starts, dtype=np.int64)
 
 
-def partial_starts(D: int, pair_start: np.ndarray) -> np.ndarray:
+def partial_starts(D: int, pair_start: np.ndarray, threads: int = CI_SWEEP_THREADS) -> np.ndarray:
     """part_start of tq_ci_energy_grad: the energy's partial sums, then each
     excitation's gradient partials (one per sweep thread that holds a pair)."""
-    cnt = np.r_[min(D, CI_SWEEP_THREADS), np.minimum(np.diff(pair_start), CI_SWEEP_THREADS)]
+    cnt = np.r_[min(D, threads), np.minimum(np.diff(pair_start), threads)]
     return np.r_[0, np.cumsum(cnt)].astype(np.int64)
 
 
@@ -216,7 +222,8 @@ class CIVectorUCC:
         self.val = torch.from_numpy(val).to(dev)
         self.strings = torch.from_numpy(strings.astype(np.int64)).to(dev)
         if self.fused:
-            part_start = partial_starts(self.D, pair_start)
+            self.threads = sweep_threads(self.max_pairs)
+            part_start = partial_starts(self.D, pair_start, self.threads)
             self.n_partials = int(part_start[-1])
             self.pairs = torch.from_numpy(pairs).to(dev)
             self.pair_start = torch.from_numpy(pair_start).to(dev)
@@ -258,7 +265,7 @@ class CIVectorUCC:
         ws, cap = K._ws(lib.tq_ci_energy_grad_workspace_bytes(self.D, self.n_partials), self.device)
         nat.call("tq_ci_energy_grad", self.D, 0, self.n_ex, P(self.pairs.data_ptr()), P(self.pair_start.data_ptr()),
                  self.max_pairs, P(self.part_start.data_ptr()), self.n_partials, P(self.sin_omc.data_ptr()),
-                 P(self.row_ptr.data_ptr()), P(self.col.data_ptr()), P(self.val.data_ptr()), int(grad),
+                 P(self.row_ptr.data_ptr()), P(self.col.data_ptr()), P(self.val.data_ptr()), int(grad), self.threads,
                  P(self.ket.data_ptr()), P(self.out.data_ptr()), ws, cap, K.stream_ptr(self.device))
 
     def _evolve(self, params) -> None:

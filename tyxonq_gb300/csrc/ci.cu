@@ -134,25 +134,26 @@ __global__ void k_ci_spmv(const int64_t* __restrict__ rp, const int32_t* __restr
 // excitations.  The entries of the next two excitations are prefetched into
 // registers while the current one is applied.
 //
+// The CTA has NT = 256 or 1024 threads (256 when no excitation has more than
+// 512 pairs: a shorter barrier per excitation).
 // FP64 issues at a small fraction of the FP32 rate on this GPU (and a CTA
 // runs on one SM), so signs are applied by flipping the sign bit with integer
 // operations and cross-thread sums are left to k_ci_segsum on many SMs: each
 // thread stores its in-thread partial of grad_j (and of the energy) to
 // part[part_start[...] + tid].
-constexpr int kCiThreads = 1024;
 
 __device__ __forceinline__ double ci_neg_if(double x, unsigned neg) {
   return __longlong_as_double(__double_as_longlong(x) ^ ((long long)neg << 63));
 }
 
-template <int IT>
+template <int IT, int NT>
 __device__ __forceinline__ void ci_load_pairs(int2 (&r)[IT], const int2* __restrict__ pairs,
                                               const int64_t* ps, int j, int n_ex) {
   if (j < 0 || j >= n_ex) return;
   const int64_t a = ps[j], np = ps[j + 1] - a;
 #pragma unroll
   for (int m = 0; m < IT; ++m) {
-    const int64_t k = threadIdx.x + (int64_t)m * kCiThreads;
+    const int64_t k = threadIdx.x + (int64_t)m * NT;
     r[m] = k < np ? __ldg(pairs + a + k) : make_int2(-1, 0);
   }
 }
@@ -178,8 +179,8 @@ __device__ __forceinline__ bool ci_pair_ok(int2 e, int D) {
 }
 
 // Shared memory layout of both sweeps: [vectors][sin, omc per excitation][pair_start][part_start].
-template <int IT>
-__global__ void __launch_bounds__(kCiThreads, 1)
+template <int IT, int NT>
+__global__ void __launch_bounds__(NT, 1)
     k_ci_forward(int D, int init, int n_ex, const int2* __restrict__ pairs, const int64_t* __restrict__ pair_start,
                  const double* __restrict__ sin_omc, double* __restrict__ ket) {
   extern __shared__ double sm[];
@@ -187,15 +188,15 @@ __global__ void __launch_bounds__(kCiThreads, 1)
   double* so = sm + D;
   int64_t* ps = (int64_t*)(so + 2 * n_ex);
   const int tid = threadIdx.x;
-  for (int i = tid; i < 2 * n_ex; i += kCiThreads) so[i] = sin_omc[i];
-  for (int i = tid; i <= n_ex; i += kCiThreads) ps[i] = pair_start[i];
-  for (int i = tid; i < D; i += kCiThreads) c[i] = (i == init) ? 1.0 : 0.0;
+  for (int i = tid; i < 2 * n_ex; i += NT) so[i] = sin_omc[i];
+  for (int i = tid; i <= n_ex; i += NT) ps[i] = pair_start[i];
+  for (int i = tid; i < D; i += NT) c[i] = (i == init) ? 1.0 : 0.0;
   __syncthreads();
   int2 cur[IT], nx1[IT], nx2[IT];
-  ci_load_pairs<IT>(cur, pairs, ps, 0, n_ex);
-  ci_load_pairs<IT>(nx1, pairs, ps, 1, n_ex);
+  ci_load_pairs<IT, NT>(cur, pairs, ps, 0, n_ex);
+  ci_load_pairs<IT, NT>(nx1, pairs, ps, 1, n_ex);
   for (int j = 0; j < n_ex; ++j) {
-    ci_load_pairs<IT>(nx2, pairs, ps, j + 2, n_ex);
+    ci_load_pairs<IT, NT>(nx2, pairs, ps, j + 2, n_ex);
     const double s = so[2 * j], mo = ci_neg_if(so[2 * j + 1], 1u);
 #pragma unroll
     for (int m = 0; m < IT; ++m)
@@ -203,14 +204,14 @@ __global__ void __launch_bounds__(kCiThreads, 1)
     __syncthreads();
     ci_rotate<IT>(cur, nx1, nx2);
   }
-  for (int i = tid; i < D; i += kCiThreads) ket[i] = c[i];
+  for (int i = tid; i < D; i += NT) ket[i] = c[i];
 }
 
 // Energy partials <ket, bra> and, when grad != 0, the reverse sweep: un-apply
 // excitation j to ket and bra, then grad_j partial = sum over j's pairs of
 // b_i phi k_p - b_p phi k_i (= sum_i bra_i fphase_j[i] ket[fperm_j[i]]).
-template <int IT>
-__global__ void __launch_bounds__(kCiThreads, 1)
+template <int IT, int NT>
+__global__ void __launch_bounds__(NT, 1)
     k_ci_reverse(int D, int n_ex, int grad, const int2* __restrict__ pairs, const int64_t* __restrict__ pair_start,
                  const int64_t* __restrict__ part_start, const double* __restrict__ sin_omc,
                  const double* __restrict__ ket, const double* __restrict__ bra, double* __restrict__ part) {
@@ -220,23 +221,23 @@ __global__ void __launch_bounds__(kCiThreads, 1)
   double* so = sm + 2 * D;
   int64_t* ps = (int64_t*)(so + 2 * n_ex);
   const int tid = threadIdx.x;
-  for (int i = tid; i < 2 * n_ex; i += kCiThreads) so[i] = sin_omc[i];
-  for (int i = tid; i <= n_ex; i += kCiThreads) ps[i] = pair_start[i];
+  for (int i = tid; i < 2 * n_ex; i += NT) so[i] = sin_omc[i];
+  for (int i = tid; i <= n_ex; i += NT) ps[i] = pair_start[i];
   double e = 0.0;
-  for (int i = tid; i < D; i += kCiThreads) {
+  for (int i = tid; i < D; i += NT) {
     const double kv = ket[i], bv = bra[i];
     k[i] = kv;
     b[i] = bv;
     e = fma(kv, bv, e);
   }
-  if (tid < (D < kCiThreads ? D : kCiThreads)) part[part_start[0] + tid] = e;
+  if (tid < (D < NT ? D : NT)) part[part_start[0] + tid] = e;
   if (!grad) return;
   __syncthreads();
   int2 cur[IT], nx1[IT], nx2[IT];
-  ci_load_pairs<IT>(cur, pairs, ps, n_ex - 1, n_ex);
-  ci_load_pairs<IT>(nx1, pairs, ps, n_ex - 2, n_ex);
+  ci_load_pairs<IT, NT>(cur, pairs, ps, n_ex - 1, n_ex);
+  ci_load_pairs<IT, NT>(nx1, pairs, ps, n_ex - 2, n_ex);
   for (int j = n_ex - 1; j >= 0; --j) {
-    ci_load_pairs<IT>(nx2, pairs, ps, j - 2, n_ex);
+    ci_load_pairs<IT, NT>(nx2, pairs, ps, j - 2, n_ex);
     const double s = ci_neg_if(so[2 * j], 1u), mo = ci_neg_if(so[2 * j + 1], 1u);
     double acc = 0.0;
 #pragma unroll
@@ -530,17 +531,19 @@ extern "C" size_t tq_ci_energy_grad_workspace_bytes(int64_t D, int64_t n_partial
 extern "C" int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const int32_t* pairs,
                                  const int64_t* pair_start, int64_t max_pairs, const int64_t* part_start,
                                  int64_t n_partials, const double* sin_omc, const int64_t* row_ptr, const int32_t* col,
-                                 const double* val, int grad, double* ket_out, double* out, void* ws, size_t ws_bytes,
-                                 void* stream) {
+                                 const double* val, int grad, int threads, double* ket_out, double* out, void* ws,
+                                 size_t ws_bytes, void* stream) {
   if (D < 1 || n_ex < 0 || init_index < 0 || init_index >= D || max_pairs < 0 || n_partials < 1)
     return fail(TQ_ERR_ARG, "tq_ci_energy_grad: D=%lld, n_ex=%d, init=%lld, max_pairs=%lld, n_partials=%lld",
                 (long long)D, n_ex, (long long)init_index, (long long)max_pairs, (long long)n_partials);
   if (D > tq_ci_pairs_max_dim(n_ex))
     return fail(TQ_ERR_RANGE, "tq_ci_energy_grad: D=%lld above the one-CTA limit %lld for %d excitations",
                 (long long)D, (long long)tq_ci_pairs_max_dim(n_ex), n_ex);
-  if (max_pairs > 2 * (int64_t)kCiThreads)
-    return fail(TQ_ERR_RANGE, "tq_ci_energy_grad: %lld pairs in one excitation (at most %d)", (long long)max_pairs,
-                2 * kCiThreads);
+  if (threads != 256 && threads != 1024)
+    return fail(TQ_ERR_ARG, "tq_ci_energy_grad: %d threads per sweep (256 or 1024)", threads);
+  if (max_pairs > 2 * (int64_t)threads)
+    return fail(TQ_ERR_RANGE, "tq_ci_energy_grad: %lld pairs in one excitation (at most %d with %d threads)",
+                (long long)max_pairs, 2 * threads, threads);
   if (!pair_start || !part_start || !row_ptr || !col || !val || !out || (n_ex > 0 && (!pairs || !sin_omc)))
     return fail(TQ_ERR_ARG, "tq_ci_energy_grad: NULL pointer");
   const size_t need = tq_ci_energy_grad_workspace_bytes(D, n_partials);
@@ -552,24 +555,31 @@ extern "C" int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const 
   double* part = bra + D;
   const int2* pr = (const int2*)pairs;
   const size_t smem_f = ci_sweep_smem(1, D, n_ex), smem_r = ci_sweep_smem(2, D, n_ex);
-#define TQ_CI_SWEEPS(IT)                                                                                         \
+#define TQ_CI_SWEEPS(IT, NT)                                                                                     \
   do {                                                                                                           \
-    cudaError_t e = cudaFuncSetAttribute(k_ci_forward<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize,         \
+    cudaError_t e = cudaFuncSetAttribute(k_ci_forward<IT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
                                          (int)smem_f);                                                           \
     if (e == cudaSuccess)                                                                                        \
-      e = cudaFuncSetAttribute(k_ci_reverse<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r);     \
+      e = cudaFuncSetAttribute(k_ci_reverse<IT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r); \
     if (e != cudaSuccess) return cuda_status(e, "tq_ci_energy_grad: shared memory");                             \
-    k_ci_forward<IT><<<1, kCiThreads, smem_f, s>>>((int)D, (int)init_index, n_ex, pr, pair_start, sin_omc, ket); \
+    k_ci_forward<IT, NT><<<1, NT, smem_f, s>>>((int)D, (int)init_index, n_ex, pr, pair_start, sin_omc, ket);     \
     k_ci_spmv<<<spmv_blocks, 256, 0, s>>>(row_ptr, col, val, D, ket, bra);                                      \
-    k_ci_reverse<IT><<<1, kCiThreads, smem_r, s>>>((int)D, n_ex, grad, pr, pair_start, part_start, sin_omc, ket, \
-                                                   bra, part);                                                   \
+    k_ci_reverse<IT, NT><<<1, NT, smem_r, s>>>((int)D, n_ex, grad, pr, pair_start, part_start, sin_omc, ket,     \
+                                               bra, part);                                                       \
   } while (0)
   int64_t spmv_blocks = (D + 7) / 8;
   if (spmv_blocks > 152 * 16) spmv_blocks = 152 * 16;
-  if (max_pairs <= kCiThreads)
-    TQ_CI_SWEEPS(1);
-  else
-    TQ_CI_SWEEPS(2);
+  if (threads == 256) {
+    if (max_pairs <= 256)
+      TQ_CI_SWEEPS(1, 256);
+    else
+      TQ_CI_SWEEPS(2, 256);
+  } else {
+    if (max_pairs <= 1024)
+      TQ_CI_SWEEPS(1, 1024);
+    else
+      TQ_CI_SWEEPS(2, 1024);
+  }
 #undef TQ_CI_SWEEPS
   k_ci_segsum<<<grad ? 1 + n_ex : 1, 256, 0, s>>>(part, part_start, out);
   TQ_CHECK_LAUNCH("tq_ci_energy_grad");
