@@ -334,3 +334,55 @@ def test_tiled_pauli_sum_matches_oracle_and_sweep_kernels(n, dtype):
     e_dev = torch.ones(1, dtype=torch.float64, device="cuda")
     K._pauli_sum_tiled(psi, empty, n, out, e_dev)
     assert float(e_dev.item()) == 0.0 and not bool(out.abs().any())
+
+
+@pytest.mark.parametrize("dtype", [C128, C64])
+def test_staged_single_state_reverse_sweep_matches_tile_passes(dtype, monkeypatch):
+    """ParametricEstimator from 14 qubits runs its reverse sweep as register-
+    staged wave adjoint passes (one-instance plan).  Against the shared-memory
+    tile-pass sweep (forced by raising the size threshold) and the oracle's
+    central differences, on every rotation kind, fixed gates, a scaled
+    multi-qubit Pauli rotation with Z strings and a phase gate."""
+    import tyxonq_gb300.adjoint as A
+    from tyxonq_gb300.adjoint import ParamGate, ParametricEstimator
+    from tyxonq_gb300.hamiltonian import random_pauli_sum
+    from tyxonq_gb300.ir import Gate, _rot_gate, pauli_rotation
+
+    rng = np.random.default_rng(11)
+    n = 14
+    H = random_pauli_sum(n, 120, rng)
+    pg, p = [], 0
+    for layer in range(3):
+        for q in range(n):
+            nm = ("rx", "ry", "rz")[(q + layer) % 3]
+            pg.append(ParamGate(_rot_gate(nm, (q,), 0.0), p))
+            p += 1
+        for q in range(layer % 2, n - 1, 2):
+            pg.append(ParamGate(Gate("cx", (q, q + 1))))
+        pg.append(ParamGate(_rot_gate("rzz", (0, n - 1), 0.0), p))
+        p += 1
+        pg.append(ParamGate(Gate("cz", (2, 9))))
+        pg.append(ParamGate(pauli_rotation(((1, "X"), (4, "Z"), (7, "Y"), (12, "Z")), 0.0), p, 2.0))
+        p += 1
+    theta = rng.uniform(0, 2 * np.pi, p)
+    staged = ParametricEstimator(n, pg, p, H, dtype=dtype)
+    assert staged._staged is not None
+    e, g = staged.energy_and_grad(theta)
+    monkeypatch.setattr(A, "STAGED_ADJOINT_MIN_N", 99)
+    tiles = ParametricEstimator(n, pg, p, H, dtype=dtype)
+    assert tiles._staged is None
+    e2, g2 = tiles.energy_and_grad(theta)
+    nrm = H.one_norm()
+    tol = 1e-10 if dtype == C128 else 2e-4 * nrm
+    assert abs(e - e2) < (1e-12 if dtype == C128 else 1e-5 * nrm)
+    np.testing.assert_allclose(g, g2, atol=tol)
+    # repeated calls give identical results (fixed-order reductions)
+    e3, g3 = staged.energy_and_grad(theta)
+    assert e3 == e and np.array_equal(g3, g)
+    if dtype == C128:  # central differences through the same engine's energies
+        for k in rng.choice(p, 6, replace=False):
+            tp, tm = theta.copy(), theta.copy()
+            tp[k] += 1e-4
+            tm[k] -= 1e-4
+            fd = (staged.energy(tp) - staged.energy(tm)) / 2e-4
+            assert abs(fd - g[k]) < 1e-6, (k, fd, g[k])

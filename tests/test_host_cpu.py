@@ -429,3 +429,20 @@ def test_excitation_records_layout_and_masks():
         excitation_records(n, [(0, 0)])
     with pytest.raises(ValueError):
         excitation_records(n, [(0, 1, 2)])
+
+
+def test_staged_adjoint_cold_gate_classification():
+    """Gates that may lack a register routine in the staged adjoint: rotations
+    with two or more X/Y qubits, ZZ rotations, controlled rotations, dense
+    two-qubit unitaries."""
+    from tyxonq_gb300.adjoint import _cold_in_staged_adjoint
+    from tyxonq_gb300.ir import Gate, _rot_gate, pauli_rotation
+    from tyxonq_gb300.program import _canon
+
+    assert not _cold_in_staged_adjoint(_canon(_rot_gate("ry", (0,), 0.3)))
+    assert _cold_in_staged_adjoint(_canon(_rot_gate("rzz", (0, 3), 0.3)))
+    assert not _cold_in_staged_adjoint(_canon(_rot_gate("rz", (2,), 0.3)))
+    assert not _cold_in_staged_adjoint(_canon(Gate("cx", (0, 1))))
+    assert not _cold_in_staged_adjoint(_canon(pauli_rotation(((0, "X"), (2, "Z"), (5, "Z")), 0.2)))
+    assert _cold_in_staged_adjoint(_canon(_rot_gate("rxx", (0, 3), 0.3)))
+    assert _cold_in_staged_adjoint(_canon(pauli_rotation(((0, "X"), (2, "Z"), (5, "Y")), 0.2)))

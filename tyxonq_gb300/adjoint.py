@@ -160,6 +160,63 @@ def build_parametric(pgates: Sequence[ParamGate], n: int, n_params: int, dtype, 
                           coef * np.asarray(slot_scale, dtype=np.float64), n_params)
 
 
+# From this size up the reverse sweep of ParametricEstimator runs as
+# register-staged adjoint passes (the batched path's wave kernels on a
+# one-instance plan) instead of the shared-memory tile passes, unless more
+# than STAGED_ADJOINT_MAX_COLD of its gates may have no register routine there
+# (rotations with two or more X/Y qubits, ZZ rotations, controlled rotations,
+# dense 4x4 gates: they
+# run from shared memory, which measured slower than the tile passes for
+# UCCSD's Pauli-string exponentials at 16 qubits).
+STAGED_ADJOINT_MIN_N = 14
+STAGED_ADJOINT_MAX_COLD = 0.1
+
+
+def _cold_in_staged_adjoint(g: Gate) -> bool:
+    from .ir import ROTATION_GENERATORS
+
+    if g.rot is None:
+        return g.kind == "u2"
+    name = g.rot[0]
+    if name == "cry":
+        return True
+    letters = [p for _, p in g.pauli] if name == "prot" else list(ROTATION_GENERATORS.get(name, ""))
+    nxy = sum(p in "XY" for p in letters)
+    # register routines: one X/Y qubit (Z factors become signs), or a single Z
+    return not (nxy == 1 or (nxy == 0 and len(letters) == 1))
+
+
+class _StagedReverse:
+    """The reverse sweep of one state as wave adjoint passes (kind 2 of
+    tq_wave_run on a single-instance WavePlan): psi and lam live in the plan's
+    pool, and the fixed-order reductions write dE/dtheta per parameter."""
+
+    def __init__(self, n: int, pgates: Sequence[ParamGate], n_params: int, dtype, device):
+        from .waves import WavePlan
+
+        gates = [_canon(p.gate) for p in pgates]
+        for g in gates:
+            if not tileable(g):
+                raise NotImplementedError(f"adjoint gradient through a '{g.kind}' gate is not supported")
+        params = {i: (int(p.param), float(p.scale)) for i, p in enumerate(pgates) if p.param is not None}
+        entry = {"idx": 0, "n": n, "gates": gates, "params": params, "key": 0, "theta_off": 0, "theta_offset": 0,
+                 "grad_offset": 0, "basis": 0, "group_begin": 0, "group_count": 0}
+        t = min(n, 13 if dtype == torch.complex64 else 12)
+        self.plan = WavePlan([entry], dtype, device, t=t, hbits=min(12, n), budget=0, max_ops=256)
+        N = 1 << n
+        self.psi = self.plan.pool[:N]
+        self.lam = self.plan.pool[N:2 * N]
+        self.grads = torch.zeros(max(n_params, 1), dtype=torch.float64, device=device)
+        self._none = torch.zeros(1, dtype=torch.uint8, device=device)
+        self.n_params = n_params
+
+    def run(self, theta: torch.Tensor) -> torch.Tensor:
+        self.grads.zero_()
+        self.plan.launch(self._none, self._none, theta, self.grads, self.grads, K.stream_ptr(self.grads.device),
+                         kinds=(2,))
+        return self.grads[:self.n_params]
+
+
 class ParametricEstimator:
     """Energy / adjoint gradient of one circuit structure, compiled once; each
     call takes a parameter vector (host array or float64 device tensor)."""
@@ -174,12 +231,23 @@ class ParametricEstimator:
         self.init_basis = int(init_basis)
         self.prog = build_parametric(pgates, self.n, self.n_params, dtype)
         self.theta = torch.zeros(max(self.n_params, 1), dtype=torch.float64, device=self.device)
-        self.psi = torch.empty(1 << self.n, dtype=dtype, device=self.device)
-        self.lam = None
+        self._staged = None
+        cold = sum(_cold_in_staged_adjoint(_canon(p.gate)) for p in pgates) / max(len(pgates), 1)
+        if self.n >= STAGED_ADJOINT_MIN_N and self.device.type == "cuda" and cold <= STAGED_ADJOINT_MAX_COLD:
+            try:
+                self._staged = _StagedReverse(self.n, pgates, self.n_params, dtype, self.device)
+            except NotImplementedError:  # a pass the wave kernels do not take: tile passes instead
+                self._staged = None
+        if self._staged is not None:
+            self.psi, self.lam = self._staged.psi, self._staged.lam
+        else:
+            self.psi = torch.empty(1 << self.n, dtype=dtype, device=self.device)
+            self.lam = None
 
     def footprint_bytes(self, grad: bool) -> int:
         S = 8 if self.dtype == torch.complex64 else 16
-        return (2 if grad else 1) * (S << self.n)
+        # the staged reverse sweep keeps psi and lam in one pool from the start
+        return (2 if grad or self._staged is not None else 1) * (S << self.n)
 
     def _forward(self, theta) -> torch.Tensor:
         if isinstance(theta, torch.Tensor) and theta.is_cuda:
@@ -196,16 +264,21 @@ class ParametricEstimator:
         return K.pauli_expectation(psi, self.H)
 
     def energy_and_grad_async(self, theta) -> tuple[torch.Tensor, torch.Tensor]:
-        """Enqueue energy + adjoint gradient; returns (device energy, device slot values)."""
+        """Enqueue energy + adjoint gradient; returns (device energy, device
+        slot values -- per-parameter gradients on the staged path)."""
         psi = self._forward(theta)
         if self.lam is None:
             self.lam = torch.empty_like(self.psi)
         K.apply_pauli_sum(psi, self.H, out=self.lam)
         e = K.inner_re(psi, self.lam)
+        if self._staged is not None:
+            return e, self._staged.run(self.theta)
         sv = reverse_sweep(self.prog, psi, self.lam, self.theta)
         return e, sv
 
     def grad_from_slots(self, slot_vals: np.ndarray) -> np.ndarray:
+        if self._staged is not None:
+            return np.asarray(slot_vals, dtype=np.float64).copy()
         return slots_to_grad(self.prog, slot_vals)
 
     def energy(self, theta) -> float:

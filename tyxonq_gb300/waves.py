@@ -251,13 +251,19 @@ class WavePlan:
         return {"fwd": fwd, "adj": adj}
 
     # ------------------------------------------------------------ execution
-    def launch(self, groups_dev, terms_dev, theta, energies, grads, stream, lane_streams=None) -> None:
-        """Enqueue every launch; lane l's on lane_streams[l] when given, else all on `stream`."""
+    def launch(self, groups_dev, terms_dev, theta, energies, grads, stream, lane_streams=None,
+               kinds=(0, 1, 2)) -> None:
+        """Enqueue every launch; lane l's on lane_streams[l] when given, else all on `stream`.
+        kinds: the phases to run (0 forward, 1 H psi + energy reduction, 2 adjoint +
+        gradient reductions)."""
         P = ctypes.c_void_p
         isz = WAVE_ITEM_DTYPE.itemsize
         for L, lane in zip(self.launches, self.launch_lanes):
             if lane_streams is not None:
                 stream = lane_streams[lane]
+            phase = L[1] if L[0] == "run" else (1 if L[0] == "reduce_e" else 2)
+            if phase not in kinds:
+                continue
             if L[0] == "run":
                 _, kind, b, c = L
                 if c == 0:
