@@ -366,12 +366,15 @@ def test_staged_single_state_reverse_sweep_matches_tile_passes(dtype, monkeypatc
         p += 1
     theta = rng.uniform(0, 2 * np.pi, p)
     staged = ParametricEstimator(n, pg, p, H, dtype=dtype)
-    assert staged._staged is not None
+    e_only = staged.energy(theta)  # energy alone does not build the staged sweep
+    assert staged._staged is None
     e, g = staged.energy_and_grad(theta)
+    assert staged._staged is not None
+    assert abs(e_only - e) < (1e-12 if dtype == C128 else 1e-5 * H.one_norm())
     monkeypatch.setattr(A, "STAGED_ADJOINT_MIN_N", 99)
     tiles = ParametricEstimator(n, pg, p, H, dtype=dtype)
-    assert tiles._staged is None
     e2, g2 = tiles.energy_and_grad(theta)
+    assert tiles._staged is None
     nrm = H.one_norm()
     tol = 1e-10 if dtype == C128 else 2e-4 * nrm
     assert abs(e - e2) < (1e-12 if dtype == C128 else 1e-5 * nrm)

@@ -188,32 +188,95 @@ def _cold_in_staged_adjoint(g: Gate) -> bool:
 
 class _StagedReverse:
     """The reverse sweep of one state as wave adjoint passes (kind 2 of
-    tq_wave_run on a single-instance WavePlan): psi and lam live in the plan's
-    pool, and the fixed-order reductions write dE/dtheta per parameter."""
+    tq_wave_run): the passes are encoded as the batched path encodes an
+    instance, the work items (one per tile and pass) and the fixed-order
+    gradient reductions are built with numpy, psi and lam live in one pool
+    (psi_off 0, lam_off 2^n), and the reductions write dE/dtheta per
+    parameter."""
 
     def __init__(self, n: int, pgates: Sequence[ParamGate], n_params: int, dtype, device):
-        from .waves import WavePlan
+        from collections import defaultdict
+
+        from .program import STAGE_DTYPE, TILE_OP_DTYPE
+        from .waves import PASS_DTYPE, WAVE_ITEM_DTYPE, WavePlan, _dev
 
         gates = [_canon(p.gate) for p in pgates]
         for g in gates:
             if not tileable(g):
                 raise NotImplementedError(f"adjoint gradient through a '{g.kind}' gate is not supported")
         params = {i: (int(p.param), float(p.scale)) for i, p in enumerate(pgates) if p.param is not None}
-        entry = {"idx": 0, "n": n, "gates": gates, "params": params, "key": 0, "theta_off": 0, "theta_offset": 0,
-                 "grad_offset": 0, "basis": 0, "group_begin": 0, "group_count": 0}
         t = min(n, 13 if dtype == torch.complex64 else 12)
-        self.plan = WavePlan([entry], dtype, device, t=t, hbits=min(12, n), budget=0, max_ops=256)
+        enc_plan = WavePlan([], dtype, device, t=t, hbits=min(12, n), max_ops=256)  # tables only
+        enc = enc_plan._encode(n, gates, params)
+        self.t, self.dt, self.rb = t, enc_plan.dt, enc_plan.adj_rb
+        self.max_ops = enc_plan.adj_max_ops
         N = 1 << n
-        self.psi = self.plan.pool[:N]
-        self.lam = self.plan.pool[N:2 * N]
+        ntile = 1 << (n - t)
+        blocks, rows, base = [], [], 0
+        self.runs = []  # (first item, item count) per adjoint pass
+        for pid, nops, pslots in enc["adj"]:
+            it = np.zeros(ntile, dtype=WAVE_ITEM_DTYPE)
+            it["lam_off"] = N
+            it["pass"] = pid
+            it["tile"] = np.arange(ntile)
+            it["part_off"] = base + np.arange(ntile) * nops
+            it["n"] = n
+            it["basis_lo"] = -1
+            self.runs.append((ntile * len(blocks), ntile))
+            blocks.append(it)
+            rows += [(base + kk, ntile, nops, coef, slot) for kk, slot, coef in pslots]
+            base += ntile * nops
+        if base >= 2 ** 31:
+            raise NotImplementedError("too many gradient partials for one reverse sweep")
+        # a parameter shared by several ops gets one row per op: rows of one
+        # reduction launch must write distinct outputs
+        seen, layers = defaultdict(int), defaultdict(list)
+        for r in rows:
+            layers[seen[r[4]]].append(r)
+            seen[r[4]] += 1
+        rows = [r for lay in sorted(layers) for r in layers[lay]]
+        self.layers = []
+        o = 0
+        for lay in sorted(layers):
+            self.layers.append((o, len(layers[lay])))
+            o += len(layers[lay])
+        items = np.concatenate(blocks) if blocks else np.zeros(0, dtype=WAVE_ITEM_DTYPE)
+        pa = np.zeros(len(enc_plan.passes), dtype=PASS_DTYPE)
+        for k, (tt, nl, b0, e0, pos) in enumerate(enc_plan.passes):
+            pa[k] = (tt, nl, b0, e0, pos)
+        self.items_dev = _dev(items, device)
+        self.passes_dev = _dev(pa, device)
+        self.stages_dev = _dev(np.concatenate(enc_plan.stages) if enc_plan.stages else np.zeros(1, STAGE_DTYPE),
+                               device)
+        self.ops_dev = _dev(np.concatenate(enc_plan.ops) if enc_plan.ops else np.zeros(1, TILE_OP_DTYPE), device)
+        self.r_first = torch.tensor([r[0] for r in rows] or [0], dtype=torch.int32, device=device)
+        self.r_count = torch.tensor([r[1] for r in rows] or [0], dtype=torch.int32, device=device)
+        self.r_stride = torch.tensor([r[2] for r in rows] or [0], dtype=torch.int32, device=device)
+        self.r_scale = torch.tensor([r[3] for r in rows] or [0.0], dtype=torch.float64, device=device)
+        self.r_out = torch.tensor([r[4] for r in rows] or [0], dtype=torch.int32, device=device)
+        self.partials = torch.zeros(max(base, 1), dtype=torch.float64, device=device)
+        self.pool = torch.empty(2 * N, dtype=dtype, device=device)
+        self.psi, self.lam = self.pool[:N], self.pool[N:]
         self.grads = torch.zeros(max(n_params, 1), dtype=torch.float64, device=device)
-        self._none = torch.zeros(1, dtype=torch.uint8, device=device)
         self.n_params = n_params
 
     def run(self, theta: torch.Tensor) -> torch.Tensor:
+        from .waves import WAVE_ITEM_DTYPE
+
+        P = ctypes.c_void_p
+        st = K.stream_ptr(self.grads.device)
+        isz = WAVE_ITEM_DTYPE.itemsize
         self.grads.zero_()
-        self.plan.launch(self._none, self._none, theta, self.grads, self.grads, K.stream_ptr(self.grads.device),
-                         kinds=(2,))
+        for first, count in self.runs:
+            nat.call("tq_wave_run", 2, self.dt, P(self.items_dev.data_ptr() + isz * first), count, self.t, 12,
+                     self.rb, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
+                     P(self.ops_dev.data_ptr()), None, None, P(theta.data_ptr()), P(self.pool.data_ptr()),
+                     P(self.partials.data_ptr()), self.max_ops, st)
+        for b, c in self.layers:
+            nat.call("tq_wave_reduce", P(self.partials.data_ptr()), P(self.r_first.data_ptr() + 4 * b),
+                     P(self.r_count.data_ptr() + 4 * b), P(self.r_stride.data_ptr() + 4 * b),
+                     P(self.r_scale.data_ptr() + 8 * b), P(self.r_out.data_ptr() + 4 * b), c,
+                     P(self.grads.data_ptr()), 1, st)
         return self.grads[:self.n_params]
 
 
@@ -233,21 +296,25 @@ class ParametricEstimator:
         self.theta = torch.zeros(max(self.n_params, 1), dtype=torch.float64, device=self.device)
         self._staged = None
         cold = sum(_cold_in_staged_adjoint(_canon(p.gate)) for p in pgates) / max(len(pgates), 1)
-        if self.n >= STAGED_ADJOINT_MIN_N and self.device.type == "cuda" and cold <= STAGED_ADJOINT_MAX_COLD:
-            try:
-                self._staged = _StagedReverse(self.n, pgates, self.n_params, dtype, self.device)
-            except NotImplementedError:  # a pass the wave kernels do not take: tile passes instead
-                self._staged = None
-        if self._staged is not None:
-            self.psi, self.lam = self._staged.psi, self._staged.lam
-        else:
-            self.psi = torch.empty(1 << self.n, dtype=dtype, device=self.device)
-            self.lam = None
+        # built on the first gradient call (energy-only use never pays for it)
+        self._staged_pending = (list(pgates) if self.n >= STAGED_ADJOINT_MIN_N and self.device.type == "cuda"
+                                and cold <= STAGED_ADJOINT_MAX_COLD else None)
+        self.psi = torch.empty(1 << self.n, dtype=dtype, device=self.device)
+        self.lam = None
 
     def footprint_bytes(self, grad: bool) -> int:
         S = 8 if self.dtype == torch.complex64 else 16
-        # the staged reverse sweep keeps psi and lam in one pool from the start
-        return (2 if grad or self._staged is not None else 1) * (S << self.n)
+        return (2 if grad else 1) * (S << self.n)
+
+    def _ensure_staged(self) -> None:
+        if self._staged_pending is None:
+            return
+        pg, self._staged_pending = self._staged_pending, None
+        try:
+            self._staged = _StagedReverse(self.n, pg, self.n_params, self.dtype, self.device)
+        except NotImplementedError:  # a pass the wave kernels do not take: tile passes instead
+            return
+        self.psi, self.lam = self._staged.psi, self._staged.lam
 
     def _forward(self, theta) -> torch.Tensor:
         if isinstance(theta, torch.Tensor) and theta.is_cuda:
@@ -266,6 +333,7 @@ class ParametricEstimator:
     def energy_and_grad_async(self, theta) -> tuple[torch.Tensor, torch.Tensor]:
         """Enqueue energy + adjoint gradient; returns (device energy, device
         slot values -- per-parameter gradients on the staged path)."""
+        self._ensure_staged()
         psi = self._forward(theta)
         if self.lam is None:
             self.lam = torch.empty_like(self.psi)
