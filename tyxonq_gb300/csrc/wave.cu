@@ -196,13 +196,38 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
         for (int k = 0; k < PER; ++k) {
           const int j = threadIdx.x + k * blockDim.x;
           pv[k] = (full || j < HN) ? cb[j ^ ml] : cplx<R>(0, 0);
-          W[k] = cplx<R>(0, 0);
         }
         // src_k = (t0 | tid | k << 8) ^ m with disjoint bit fields (t0 is a multiple
         // of 2^hb = PER * 256), so parity(src_k & zy) = parity(((t0 | tid) ^ m) & zy)
         // XOR parity(k & c) with c = (zy >> 8) & (PER - 1): one popcount per term
         // and thread.
         const uint64_t sbase = (uint64_t)((t0 | (int64_t)threadIdx.x) ^ (int64_t)m);
+        if (cnt == 1) {
+          // one term (most groups of a random Pauli sum): its weight is real or
+          // imaginary, so each amplitude takes two FMAs with a signed weight
+          const uint64_t zy = __ldg(&terms[first].zy);
+          const cplx<R> w = term_w<R>(&terms[first]);
+          const int p0 = __popcll(sbase & zy) & 1;
+          const int c = (int)(zy >> 8) & (PER - 1);
+          if (w.y == R(0)) {
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+              const R sw = ((p0 ^ __popc(k & c)) & 1) ? -w.x : w.x;
+              acc[k].x = fma(sw, pv[k].x, acc[k].x);
+              acc[k].y = fma(sw, pv[k].y, acc[k].y);
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+              const R sw = ((p0 ^ __popc(k & c)) & 1) ? -w.y : w.y;
+              acc[k].x = fma(-sw, pv[k].y, acc[k].x);
+              acc[k].y = fma(sw, pv[k].x, acc[k].y);
+            }
+          }
+          continue;
+        }
+#pragma unroll
+        for (int k = 0; k < PER; ++k) W[k] = cplx<R>(0, 0);
         if (cnt <= 2 || PER == 1) {
           // few terms: signs per amplitude directly
           for (int tt = 0; tt < cnt; ++tt) {
