@@ -446,3 +446,45 @@ def test_staged_adjoint_cold_gate_classification():
     assert not _cold_in_staged_adjoint(_canon(pauli_rotation(((0, "X"), (2, "Z"), (5, "Z")), 0.2)))
     assert _cold_in_staged_adjoint(_canon(_rot_gate("rxx", (0, 3), 0.3)))
     assert _cold_in_staged_adjoint(_canon(pauli_rotation(((0, "X"), (2, "Z"), (5, "Y")), 0.2)))
+
+
+def test_staged_reverse_tables_cover_every_parametrised_op():
+    """Host tables of the single-state staged reverse sweep (built on the CPU
+    here): one work item per (adjoint pass, tile), disjoint partial ranges, a
+    reduction row for every parametrised op, and reduction launches that never
+    write one gradient twice (a parameter shared by several rotations)."""
+    import torch
+
+    from tyxonq_gb300.adjoint import ParamGate, _StagedReverse
+    from tyxonq_gb300.ir import Gate, _rot_gate, pauli_rotation
+    from tyxonq_gb300.waves import WAVE_ITEM_DTYPE
+
+    n = 15
+    pg, p = [], 0
+    for layer in range(2):
+        for q in range(n):
+            pg.append(ParamGate(_rot_gate("ry", (q,), 0.0), p))
+            p += 1
+        for q in range(n - 1):
+            pg.append(ParamGate(Gate("cx", (q, q + 1))))
+    shared = p
+    pg.append(ParamGate(pauli_rotation(((0, "X"), (7, "Z")), 0.0), shared, 2.0))
+    pg.append(ParamGate(pauli_rotation(((3, "Y"), (9, "Z")), 0.0), shared, -1.0))
+    p += 1
+    sr = _StagedReverse(n, pg, p, torch.complex64, "cpu")
+    items = np.frombuffer(sr.items_dev.numpy().tobytes(), dtype=WAVE_ITEM_DTYPE)
+    assert sr.t == 13 and len(items) == sum(c for _, c in sr.runs) == len(sr.runs) * (1 << (n - sr.t))
+    assert np.all(items["psi_off"] == 0) and np.all(items["lam_off"] == 1 << n)
+    # every tile of every pass owns its own block of partial slots
+    ranges = sorted(zip(items["part_off"], items["pass"]))
+    assert len({int(o) for o, _ in ranges}) == len(items)
+    first = sr.r_first.numpy()
+    count, stride, out = sr.r_count.numpy(), sr.r_stride.numpy(), sr.r_out.numpy()
+    assert np.all(count == 1 << (n - sr.t))
+    assert np.all(first + (count - 1) * stride < sr.partials.numel())
+    # one row per parametrised op; the shared parameter has two rows in different launches
+    assert len(out) == sum(1 for g in pg if g.param is not None)
+    for b, c in sr.layers:
+        lay = out[b:b + c]
+        assert len(set(lay.tolist())) == len(lay)
+    assert sorted(set(out.tolist())) == list(range(p))
