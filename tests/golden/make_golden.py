@@ -2,7 +2,9 @@
 
 Run from the repository root, in a checkout that has the reference sources:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference/src
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <TyxonQ src folder>
+
+(or with the folder in the environment variable TYXONQ_SRC).
 
 It imports TyxonQ from the given source tree and records, for seeded inputs:
   * final states of small circuits through StatevectorEngine.state() and the
@@ -242,4 +244,7 @@ def main(ref_src: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TYXONQ_SRC")
+    if not src:
+        sys.exit("usage: make_golden.py <TyxonQ src folder>  (or set TYXONQ_SRC)")
+    main(src)

@@ -1,6 +1,8 @@
 """Multi-rank host logic on CPU (gloo, world size 2): shards cover the
-instances exactly once, the step time is the max over ranks, and results
-gather on rank 0 in rank order."""
+instances exactly once, the step time is the max over ranks, and a
+strong-scaling split of one VQE workload (cost-balanced shards, evaluated per
+rank) gathers energies and gradients on rank 0 in instance order, equal to a
+serial evaluation."""
 import os
 import socket
 
@@ -37,23 +39,43 @@ def _free_port():
     return p
 
 
+def _oracle_eval(inst):
+    from oracle import sv
+
+    gates = [(nm, list(qs), p, 1.0) for nm, qs, p in inst.structure()]
+    return sv.grad_adjoint(inst.n, gates, inst.theta, inst.H.codes, inst.H.coeffs)
+
+
 def _worker(rank, world, port, out):
+    """One rank of a strong-scaling split: evaluate this rank's cost-balanced
+    shard of one VQE workload (the oracle stands in for the device engine on
+    CPU), then gather energies and gradients in instance order on rank 0."""
+    from tyxonq_gb300.distributed import gather_instances, shard_instances
+    from tyxonq_gb300.workloads import batched_vqe
+
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        ids = list(shard_range(10, rank, world))
-        local = np.array([float(i) ** 2 for i in ids])
+        insts = batched_vqe(14, seed=11, n_range=(3, 8), depth_range=(1, 3), terms_range=(5, 30))
+        ids = shard_instances(insts, rank, world)
+        res = [_oracle_eval(insts[i]) for i in ids]
         t = max_over_ranks(1.5 if rank == 0 else 2.5)
-        allr = gather_results(local)
+        got = gather_instances(ids, [e for e, _ in res], [g for _, g in res], len(insts))
         if rank == 0:
-            out.put((t, allr.tolist()))
+            E, G = got
+            out.put((t, sorted(ids), E.tolist(), [g.tolist() for g in G]))
+        else:
+            assert got is None
+            out.put(("ids", sorted(ids)))
         dist.barrier()
     finally:
         dist.destroy_process_group()
 
 
-def test_two_rank_gloo_sharded_evaluation():
+def test_two_rank_gloo_strong_scaling_evaluation():
+    from tyxonq_gb300.workloads import batched_vqe
+
     ctx = mp.get_context("spawn")
     q = ctx.SimpleQueue()
     port = _free_port()
@@ -61,11 +83,20 @@ def test_two_rank_gloo_sharded_evaluation():
     for p in procs:
         p.start()
     for p in procs:
-        p.join(timeout=120)
+        p.join(timeout=300)
         assert p.exitcode == 0
-    t, vals = q.get()
+    msgs = [q.get(), q.get()]
+    root = [m for m in msgs if m[0] != "ids"][0]
+    other = [m for m in msgs if m[0] == "ids"][0]
+    t, ids0, E, G = root
     assert t == 2.5
-    assert vals == [float(i) ** 2 for i in range(10)]
+    # the two shards partition the workload
+    assert sorted(ids0 + other[1]) == list(range(14)) and ids0 and other[1]
+    insts = batched_vqe(14, seed=11, n_range=(3, 8), depth_range=(1, 3), terms_range=(5, 30))
+    for k, inst in enumerate(insts):
+        e, g = _oracle_eval(inst)
+        assert E[k] == e
+        np.testing.assert_array_equal(G[k], g)
 
 
 @pytest.mark.parametrize("world", [1])

@@ -10,9 +10,9 @@ import pytest
 
 
 def _tyxonq_available():
-    for p in (os.environ.get("TYXONQ_SRC"), "/root/reference/src"):
-        if p and os.path.isdir(p) and p not in sys.path:
-            sys.path.append(p)
+    p = os.environ.get("TYXONQ_SRC")  # a TyxonQ source tree (its src/ folder)
+    if p and os.path.isdir(p) and p not in sys.path:
+        sys.path.append(p)
     try:
         import tyxonq.devices.simulators.driver  # noqa: F401
 

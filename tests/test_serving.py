@@ -38,6 +38,10 @@ class _FakeServer(VqeServer):
         ticket["left"] -= 1
         return ticket["left"] < 0
 
+    def _footprint(self, req):
+        # admission logic under test: states only (psi, plus lam for gradients)
+        return (2 if req.grad else 1) * (8 << req.n)
+
 
 def _req(session, n, grad=False):
     return VqeRequest(session, n, [], 3, None, np.zeros(3), grad)
@@ -119,3 +123,27 @@ def test_results_same_alone_and_in_the_mix():
         psi, _ = sv.run_ops(r.n, [(nm, *qs) if p is None else (nm, *qs, float(r.theta[p])) for nm, qs, p in r.structure])
         e_ref = sv.pauli_expectation(psi, r.H.codes, r.H.coeffs)
         assert abs(r.energy - e_ref) < 1e-5 * r.H.one_norm()
+
+
+def test_footprint_counts_tables_workspace_and_partials():
+    """The admission footprint of a gradient session covers psi, lam, the op and
+    Pauli tables, the tiled H psi workspace and the reverse-sweep partials."""
+    from tyxonq_gb300.adjoint import TILE_OP_RECORD_BYTES, estimate_footprint
+    from tyxonq_gb300.hamiltonian import random_pauli_sum
+    from tyxonq_gb300.workloads import hea_rz_ops_params
+
+    n = 20
+    H = random_pauli_sum(n, 500, np.random.default_rng(1))
+    struct = hea_rz_ops_params(n, 4)
+    n_param = sum(1 for _, _, p in struct if p is not None)
+    e = estimate_footprint(n, len(struct), n_param, H.n_groups, H.n_terms, False, torch.complex64)
+    g = estimate_footprint(n, len(struct), n_param, H.n_groups, H.n_terms, True, torch.complex64)
+    states = 8 << n
+    tables = 2 * len(struct) * TILE_OP_RECORD_BYTES + 16 * H.n_groups + 32 * H.n_terms
+    partials = 8 * n_param * (1 << (n - 13))
+    assert e > states + tables  # plus the H psi workspace
+    assert g - e == states + partials
+    srv = VqeServer(device="cpu", hbm_budget=1 << 40, streams=[None])
+    req = VqeRequest("s", n, struct, n_param, H, np.zeros(n_param), True)
+    assert srv._footprint(req) == g
+

@@ -25,7 +25,9 @@ from . import _native as nat
 from . import kernels as K
 from .hamiltonian import PauliSum, as_pauli_sum
 from .ir import Gate, lower_ops
-from .program import DEFAULT_NLOW, _canon, compile_forward, encode_passes, plan_passes, tileable
+from .program import DEFAULT_NLOW, TILE_OP_DTYPE, _canon, compile_forward, encode_passes, plan_passes, tileable
+
+TILE_OP_RECORD_BYTES = TILE_OP_DTYPE.itemsize
 
 
 @dataclass
@@ -280,6 +282,26 @@ class _StagedReverse:
         return self.grads[:self.n_params]
 
 
+def estimate_footprint(n: int, n_gates: int, n_param_ops: int, n_groups: int, n_terms: int, grad: bool, dtype,
+                       staged_reverse: bool | None = None) -> int:
+    """Device bytes of one estimator session: psi (and lam for gradients),
+    the forward and reverse op tables, the Pauli tables, the tiled H psi
+    workspace and, for the register-staged reverse sweep (n >= 14), its FP64
+    gradient partials (one per parametrised op and tile of 2^t amplitudes)."""
+    S = 8 if dtype == torch.complex64 else 16
+    N = 1 << int(n)
+    b = (2 if grad else 1) * S * N
+    b += 2 * n_gates * TILE_OP_RECORD_BYTES + n_groups * 16 + n_terms * 32
+    if n >= K.TILED_MIN_N:
+        b += int(nat.load().tq_sv_pauli_sum_tiled_workspace_bytes(int(n), 0 if S == 8 else 1, int(n_groups), 1))
+    if staged_reverse is None:
+        staged_reverse = n >= STAGED_ADJOINT_MIN_N
+    if grad and staged_reverse:
+        t = min(int(n), 13 if S == 8 else 12)
+        b += 8 * n_param_ops * (1 << (int(n) - t))
+    return int(b)
+
+
 class ParametricEstimator:
     """Energy / adjoint gradient of one circuit structure, compiled once; each
     call takes a parameter vector (host array or float64 device tensor)."""
@@ -292,6 +314,7 @@ class ParametricEstimator:
         self.dtype = dtype
         self.device = torch.device(device)
         self.init_basis = int(init_basis)
+        self._pgates = list(pgates)
         self.prog = build_parametric(pgates, self.n, self.n_params, dtype)
         self.theta = torch.zeros(max(self.n_params, 1), dtype=torch.float64, device=self.device)
         self._staged = None
@@ -303,8 +326,11 @@ class ParametricEstimator:
         self.lam = None
 
     def footprint_bytes(self, grad: bool) -> int:
-        S = 8 if self.dtype == torch.complex64 else 16
-        return (2 if grad else 1) * (S << self.n)
+        """Device bytes a session of this estimator holds: see estimate_footprint."""
+        n_param_ops = sum(1 for pg in self._pgates if pg.param is not None)
+        staged = self._staged is not None or self._staged_pending is not None
+        return estimate_footprint(self.n, len(self._pgates), n_param_ops, self.H.n_groups, self.H.n_terms, grad,
+                                  self.dtype, staged_reverse=staged)
 
     def _ensure_staged(self) -> None:
         if self._staged_pending is None:

@@ -680,11 +680,35 @@ extern "C" int tq_sv_sample(const void* psi, int n, int dtype, int64_t shots, ui
 #define TQ_NOALLOC_SCRATCH_BYTES (size_t(8) << 20)
 static __device__ __align__(256) unsigned char g_sample_scratch[TQ_NOALLOC_SCRATCH_BYTES];
 
+#include <cuda.h>
 #include <mutex>
 
 namespace tq {
+// The scratch array's device address, cached per device ordinal together with
+// the CUDA context it was looked up in.  A device reset (or a primary context
+// released and created again) reloads the module, so the address is looked up
+// again whenever the current context differs from the cached one.
+struct ScratchAddr {
+  CUcontext ctx;
+  void* ptr;
+};
 static std::mutex g_scratch_mu;
-static void* g_scratch_ptr[64] = {nullptr};
+static ScratchAddr g_scratch_addr[64] = {};
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+
+static CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(f);
+  }
+  return fn;
+}
 }  // namespace tq
 
 extern "C" int tq_sv_sample_noalloc(const void* psi, int n, int dtype, int64_t shots, uint64_t seed,
@@ -702,16 +726,24 @@ extern "C" int tq_sv_sample_noalloc(const void* psi, int n, int dtype, int64_t s
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_status(e, "tq_sv_sample_noalloc: cudaGetDevice");
   if (dev < 0 || dev >= 64) return fail(TQ_ERR_RANGE, "tq_sv_sample_noalloc: device ordinal %d", dev);
+  // a thread whose context the runtime has not made current yet reads a null
+  // context: the address is then looked up again (which also makes it current)
+  CUcontext ctx = nullptr;
+  if (CtxGetCurrentFn f = ctx_get_current()) {
+    if (f(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+  }
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    ScratchAddr& a = g_scratch_addr[dev];
+    if (!a.ptr || !ctx || a.ctx != ctx) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_sample_scratch);
       if (e != cudaSuccess) return cuda_status(e, "tq_sv_sample_noalloc: cudaGetSymbolAddress");
-      g_scratch_ptr[dev] = p;
+      a.ptr = p;
+      a.ctx = ctx;
     }
-    scratch = g_scratch_ptr[dev];
+    scratch = a.ptr;
   }
   // Every scratch word the sampler reads is written earlier in the same call
   // (chunk sums, scans, spacings), so the previous call's contents need no clearing.

@@ -202,11 +202,13 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
         // XOR parity(k & c) with c = (zy >> 8) & (PER - 1): one popcount per term
         // and thread.
         const uint64_t sbase = (uint64_t)((t0 | (int64_t)threadIdx.x) ^ (int64_t)m);
-        if (cnt == 1) {
-          // one term (most groups of a random Pauli sum): its weight is real or
-          // imaginary, so each amplitude takes two FMAs with a signed weight
+        const cplx<R> w1 = cnt == 1 ? term_w<R>(&terms[first]) : cplx<R>(0, 0);
+        if (cnt == 1 && (w1.x == R(0) || w1.y == R(0))) {
+          // one term (most groups of a random Pauli sum) with a real or imaginary
+          // weight (c * i^ny for real c): each amplitude takes two FMAs with a
+          // signed weight.  A general complex weight takes the path below.
           const uint64_t zy = __ldg(&terms[first].zy);
-          const cplx<R> w = term_w<R>(&terms[first]);
+          const cplx<R> w = w1;
           const int p0 = __popcll(sbase & zy) & 1;
           const int c = (int)(zy >> 8) & (PER - 1);
           if (w.y == R(0)) {

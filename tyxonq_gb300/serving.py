@@ -4,8 +4,9 @@ Requests (energy, or energy + adjoint gradient) of 10-26+ qubits arrive
 over time.  The server
 
   * admits a request when a stream slot is free and its session's device
-    footprint (psi, plus lam for gradients: 2^n * 8 B each in complex64) fits
-    the HBM budget -- evicting idle sessions least-recently-used first;
+    footprint (psi, plus lam for gradients: 2^n * 8 B each in complex64; op
+    and Pauli tables, H psi workspace, reverse-sweep partials) fits the HBM
+    budget -- evicting idle sessions least-recently-used first;
   * keeps each session's statevectors and compiled circuit resident across
     its optimizer iterations (angles are read on the device, so a new
     parameter vector costs one small copy, no re-planning);
@@ -89,8 +90,13 @@ class VqeServer:
 
     # ------------------------------------------------------------ memory
     def _footprint(self, req: VqeRequest) -> int:
-        S = 8 if self.dtype == torch.complex64 else 16
-        return (2 if req.grad else 1) * (S << req.n)
+        """Device bytes of the request's session: states, op and Pauli tables,
+        H psi workspace and reverse-sweep partials (adjoint.estimate_footprint)."""
+        from .adjoint import estimate_footprint
+
+        n_param = sum(1 for _, _, p in req.structure if p is not None)
+        return estimate_footprint(req.n, len(req.structure), n_param, req.H.n_groups, req.H.n_terms, req.grad,
+                                  self.dtype)
 
     def _evict_for(self, need: int) -> bool:
         for key in list(self.sessions):
