@@ -184,8 +184,10 @@ def _events():
 
 
 def bench_gate_kernels(args, dev):
-    """28 qubits, depth 40 random circuit, complex64: fused tile passes (per-launch
-    events) and the one-launch-per-gate engine."""
+    """28 qubits, depth 40 random circuit, complex64: fused tile passes with the
+    interpreting kernel (per-launch events) and with the circuit-specialised
+    kernels (events around the whole program), the one-launch-per-gate engine,
+    full probabilities and 8192 shots."""
     import ctypes
 
     import torch
@@ -202,6 +204,7 @@ def bench_gate_kernels(args, dev):
             self.num_qubits, self.ops = n, ops
 
     n2 = 28
+    N, S = 1 << n2, 8
     gates, _ = lower_ops(_C(n2, random_circuit(n2, 40, seed=1)), mode="run")
     prog = compile_forward(gates, n2, torch.complex64)
     psi = K.init_statevector(n2, dtype=torch.complex64)
@@ -233,6 +236,42 @@ def bench_gate_kernels(args, dev):
         torch.cuda.synchronize()
         step_ms.append(a.elapsed_time(b))
         launch_ms += [x.elapsed_time(y) for x, y in evs]
+    avg_launch = sum(launch_ms) / len(launch_ms)
+    # circuit-specialised kernels (compiled at run time, cached per structure)
+    t0 = time.perf_counter()
+    n_spec = prog.specialise(torch.complex64)
+    spec_build_s = time.perf_counter() - t0
+    for _ in range(2):
+        prog.run(psi)
+    torch.cuda.synchronize()
+    spec_ms = []
+    for _ in range(3):
+        a, b = _events()
+        a.record(st)
+        prog.run(psi)
+        b.record(st)
+        torch.cuda.synchronize()
+        spec_ms.append(a.elapsed_time(b))
+    spec_total = sum(spec_ms) / len(spec_ms)
+    spec_pass = spec_total / prog.n_passes
+    # full probabilities (float32) and 8192 shots of the final state
+    probs = K.probabilities(psi)
+    K.sample(psi, 8192, seed=1)
+    torch.cuda.synchronize()
+    prob_ms, shot_ms = [], []
+    for r in range(3):
+        a, b = _events()
+        a.record(st)
+        K.probabilities(psi, out=probs)
+        b.record(st)
+        c, d = _events()
+        c.record(st)
+        K.sample(psi, 8192, seed=2 + r)
+        d.record(st)
+        torch.cuda.synchronize()
+        prob_ms.append(a.elapsed_time(b))
+        shot_ms.append(c.elapsed_time(d))
+    del probs
     psi2 = K.init_statevector(n2, dtype=torch.complex64)
     execute_plain(psi2, gates[:40])
     torch.cuda.synchronize()
@@ -244,11 +283,16 @@ def bench_gate_kernels(args, dev):
     plain_ms = a.elapsed_time(b)
     del psi, psi2
     torch.cuda.empty_cache()
-    N, S = 1 << n2, 8
-    avg_launch = sum(launch_ms) / len(launch_ms)
-    return {"fused_ms": sum(step_ms) / len(step_ms), "plain_ms": plain_ms, "passes": prog.n_passes,
-            "gates": len(gates), "avg_pass_ms": avg_launch, "pass_alg_bytes": 2 * N * S,
-            "pass_gbs": 2 * N * S / (avg_launch * 1e-3) / 1e9, "single_gate": bench_single_gates(n2)}
+    pm, sm = sum(prob_ms) / len(prob_ms), sum(shot_ms) / len(shot_ms)
+    return {"fused_ms": spec_total, "fused_interpreter_ms": sum(step_ms) / len(step_ms), "plain_ms": plain_ms,
+            "passes": prog.n_passes, "gates": len(gates), "pass_alg_bytes": 2 * N * S,
+            "avg_pass_ms": spec_pass, "pass_gbs": 2 * N * S / (spec_pass * 1e-3) / 1e9,
+            "specialised_passes": n_spec, "specialise_s": spec_build_s,
+            "interpreter_avg_pass_ms": avg_launch,
+            "interpreter_pass_gbs": 2 * N * S / (avg_launch * 1e-3) / 1e9,
+            "probabilities": {"ms": pm, "alg_bytes": N * (S + 4), "gbs": N * (S + 4) / (pm * 1e-3) / 1e9},
+            "shots_8192": {"ms": sm, "alg_bytes": N * S, "gbs": N * S / (sm * 1e-3) / 1e9},
+            "single_gate": bench_single_gates(n2)}
 
 
 def bench_small_configs(reps: int = 10) -> dict:
@@ -435,6 +479,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="weak: every rank evaluates its own --count instances; strong: one --count workload "
+                         "split over the ranks by estimated cost")
     ap.add_argument("--case", default="full", choices=["full", "gates", "batched", "small", "civector"],
                     help="gates / batched / small / civector (16-qubit UCCSD in CI space): run only that part "
                          "(profiling captures); full: the benchmark line")
@@ -463,8 +510,17 @@ def main():
 
         dist.init_process_group("nccl")
 
-    # ---------------- batched workload: every rank evaluates its own 4096 instances (weak scaling)
-    insts = batched_vqe(args.count, seed=3 + 1000 * rank)
+    # ---------------- batched workload: weak scaling = every rank evaluates its own 4096 instances;
+    # strong scaling = one 4096-instance workload split over the ranks by estimated cost
+    if args.scaling == "strong":
+        from tyxonq_gb300.distributed import shard_instances
+
+        insts_all = batched_vqe(args.count, seed=3)
+        insts = [insts_all[i] for i in shard_instances(insts_all, rank, world)]
+        job_count = len(insts_all)
+    else:
+        insts = batched_vqe(args.count, seed=3 + 1000 * rank)
+        job_count = world * len(insts)
     t0 = time.perf_counter()
     bv = BatchedVQE(insts, dtype=torch.complex64)
     build_s = time.perf_counter() - t0
@@ -494,7 +550,7 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * len(insts) / (ms * 1e-3)
+    value = job_count / (ms * 1e-3)
 
     # ---------------- e2e: host theta -> device, evaluate, energies + gradients -> host
     e_host = torch.empty(bv.count, dtype=torch.float64).pin_memory()
@@ -511,7 +567,12 @@ def main():
         b.record()
         torch.cuda.synchronize()
         e2e_ms.append(a.elapsed_time(b))
-    e2e = world * len(insts) / (sum(e2e_ms) / len(e2e_ms) * 1e-3)
+    e2e_local = sum(e2e_ms) / len(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_local], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_local = float(t.item())
+    e2e = job_count / (e2e_local * 1e-3)
     h2d = theta_host.numel() * 8
     d2h = (e_host.numel() + g_host.numel()) * 8
     energies = e_host.numpy().copy()
@@ -574,7 +635,7 @@ def main():
     launches_per_step = bv.kernel_launches()
     line = {
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": args.scaling,
         "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
         "config": {"workload": f"batched_vqe_{len(insts)}: n~U{{8..20}}, HEA depth~U{{2..8}} [RY;RZ;CX ladder], "
                                "50-500 random Pauli terms (weight 1-4, N(0,1)), energy + adjoint gradient",
@@ -589,8 +650,8 @@ def main():
                                 "20-1000 Pauli terms, 30% energy+gradient, complex64"},
         "gate_kernels_28q": gk,
         "small_configs": small,
-        "roofline": {"kernel": "k_staged_forward (28-qubit complex64 fused pass of the depth-40 random circuit, "
-                               "2*N*8 B per launch)", "bound": "hbm",
+        "roofline": {"kernel": "tq_jit_staged_pass (circuit-specialised fused pass of the 28-qubit complex64 "
+                               "depth-40 random circuit, 2*N*8 B per launch)", "bound": "hbm",
                      "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,
                      "traffic": STAGED_PASS_DRAM_BYTES, "peak_kind": peak_kind},
         "cpu_baseline": cpu,

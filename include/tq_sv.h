@@ -26,8 +26,10 @@
 #ifndef TQ_SV_H
 #define TQ_SV_H
 
+#ifndef __CUDACC_RTC__
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #if defined(__GNUC__)
 #define TQ_API __attribute__((visibility("default")))
@@ -156,6 +158,9 @@ TQ_API int tq_sv_sample(const void* psi, int n, int dtype, int64_t shots, uint64
  * exceeds 8 MiB fail with TQ_ERR_RANGE (at 28 qubits that is about 980,000
  * shots).  The first call on a device looks the scratch address up
  * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * The address is cached per device and CUDA context: after a device reset
+ * (or a primary context released and created again) the next call looks it
+ * up again, and that call too should come before any stream capture.
  * All calls share the one scratch array: calls that overlap on the GPU
  * (different streams, or different host threads) race and must be ordered by
  * the caller.  Results equal tq_sv_sample's for the same arguments. */
@@ -263,6 +268,42 @@ typedef struct {
  * 9 <= t <= 14 (complex64) / 13 (complex128); CTAs of 2^(t-4) threads. */
 TQ_API int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
                             const tq_tile_stage* stages, const tq_tile_op* ops, const double* theta, void* stream);
+
+/* ------------------------------------------------------------ circuit-specialised passes */
+
+/* Runtime compilation (NVRTC, sm_103a) of staged forward pass kernels whose op
+ * lists are straight-line code.  `source` is CUDA C++ written by
+ * tyxonq_gb300/jit.py: it includes the library's device headers (found
+ * through `include_dirs`) and defines one extern "C" kernel with the
+ * parameters (T* psi, int n, PassArgs P, const tq_tile_stage* stages,
+ * const tq_tile_op* ops, const ROp<R>* op_records, int dbuf).  On success
+ * *cubin (host memory, release with tq_jit_free_host) holds the compiled
+ * code; `log` (optional) receives the compiler log on failure.  These replace
+ * the same interpreter loop as tq_sv_run_staged (engine.py:52-374 /
+ * :914-1039), specialised per circuit structure; angles and matrices stay data
+ * (op table and theta). */
+TQ_API int tq_jit_build(const char* source, const char* const* include_dirs, int n_include_dirs, void** cubin,
+                        size_t* cubin_size, char* log, size_t log_cap);
+TQ_API void tq_jit_free_host(void* p);
+
+/* Load a cubin of tq_jit_build on the current device; *kernel_out is the
+ * handle of its kernel `kernel_name` (release with tq_jit_unload). */
+TQ_API int tq_jit_load(const void* cubin, size_t cubin_size, const char* kernel_name, void** kernel_out);
+TQ_API int tq_jit_unload(void* kernel);
+
+/* Workspace of tq_jit_run_staged: the compiled op records of an n_ops table. */
+TQ_API size_t tq_jit_rops_bytes(int dtype, int n_ops);
+
+/* Staged forward passes with specialised kernels: pass p runs kernels[p]
+ * (a tq_jit_load handle), or the library's interpreting kernel where
+ * kernels[p] is NULL.  Tables as tq_sv_run_staged (ops holds n_ops records;
+ * stages_host is a host copy of `stages`, for launch sizes); at most 256 ops
+ * per specialised pass; ws: tq_jit_rops_bytes(dtype, n_ops) bytes, 16-byte
+ * aligned. */
+TQ_API int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dtype, const tq_tile_pass* passes,
+                             int n_passes, const tq_tile_stage* stages_host, const tq_tile_stage* stages,
+                             const tq_tile_op* ops, int n_ops, const double* theta, void* ws, size_t ws_bytes,
+                             void* stream);
 
 /* Largest t supported for a dtype (shared-memory capacity). */
 TQ_API int tq_sv_tile_max_bits(int dtype);

@@ -86,7 +86,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     tmp = LIB_DIR / (LIB_NAME + ".tmp")
-    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs)]
+    cuda_lib = Path(nvcc).resolve().parent.parent / "lib64"
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs), "-L", str(cuda_lib), "-lnvrtc",
+           "-Xlinker", f"-rpath={cuda_lib}"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

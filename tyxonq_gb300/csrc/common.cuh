@@ -7,11 +7,24 @@
 // points translate qubit indices with tq_bit(n, q) exactly once.
 #pragma once
 
+#ifdef __CUDACC_RTC__
+// Runtime-compiled kernels (tyxonq_gb300/csrc/jit.cu) see only device code:
+// fixed-width integer types without the host headers.
+typedef signed char int8_t;
+typedef unsigned char uint8_t;
+typedef short int16_t;
+typedef unsigned short uint16_t;
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+#else
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
+#endif
 
-#include "../../include/tq_sv.h"
+#include "tq_sv.h"
 
 namespace tq {
 
@@ -77,6 +90,7 @@ __host__ __device__ __forceinline__ int64_t insert_zero2(int64_t i, int plo, int
   return insert_zero(insert_zero(i, plo), phi);
 }
 
+#ifndef __CUDACC_RTC__
 // ----------------------------------------------------------------- errors
 // Host-side error reporting: each failing entry point records a message that
 // tq_last_error() returns (thread-local, like errno).
@@ -113,5 +127,7 @@ inline unsigned grid_for(int64_t items, int threads) {
   const int64_t cap = int64_t(152) * 64;  // 152 SMs x 64 resident blocks worth
   return (unsigned)(b < cap ? b : cap);
 }
+
+#endif  // __CUDACC_RTC__
 
 }  // namespace tq

@@ -1,0 +1,214 @@
+// Runtime compilation of circuit-specialised pass kernels (NVRTC) and their
+// launches.
+//
+// tyxonq_gb300/jit.py writes CUDA source for each register-staged forward
+// pass of a circuit structure (straight-line register code per stage, see
+// jit_staged.cuh).  tq_jit_build compiles one such source for sm_103a in
+// process with NVRTC and hands back the cubin (the host side caches it on
+// disk); tq_jit_load loads a cubin as a CUDA library and keeps its kernel.
+// tq_jit_run_staged compiles the program's op records once (k_rops_compile,
+// the same rop_build as the library's interpreting kernel) and launches every
+// pass with its specialised kernel, or with the interpreting kernel
+// (tq_sv_run_staged) where the host gave none.
+#include <nvrtc.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "staged_io.cuh"
+
+namespace tq {
+
+struct JitKernel {
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kernel = nullptr;
+};
+
+static int nvrtc_fail(nvrtcResult r, const char* where) {
+  return fail(TQ_ERR_CUDA, "%s: %s", where, nvrtcGetErrorString(r));
+}
+
+template <typename R>
+static size_t jit_smem_bytes(int t, int nlow, int nops, int dbuf) {
+  return (size_t)(dbuf ? 2 : 1) * padded_len(t) * sizeof(cplx<R>) + staged_hoff_bytes(t, nlow) +
+         (size_t)nops * sizeof(ROp<R>);
+}
+
+// Forward op records of the whole op table (one thread per op).
+template <typename R>
+__global__ void k_rops_compile(ROp<R>* out, const tq_tile_op* __restrict__ ops, int n_ops,
+                               const double* __restrict__ theta) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n_ops) rop_build<R>(out[k], ops, k, theta, false, false);
+}
+
+}  // namespace tq
+
+using namespace tq;
+
+extern "C" int tq_jit_build(const char* source, const char* const* include_dirs, int n_include_dirs, void** cubin,
+                            size_t* cubin_size, char* log, size_t log_cap) {
+  if (!source || !cubin || !cubin_size) return fail(TQ_ERR_ARG, "tq_jit_build: NULL argument");
+  *cubin = nullptr;
+  *cubin_size = 0;
+  if (log && log_cap) log[0] = 0;
+  nvrtcProgram prog;
+  nvrtcResult r = nvrtcCreateProgram(&prog, source, "tq_jit.cu", 0, nullptr, nullptr);
+  if (r != NVRTC_SUCCESS) return nvrtc_fail(r, "tq_jit_build: nvrtcCreateProgram");
+  // unannotated declarations of the C ABI header are device-side in runtime compilation
+  std::vector<std::string> opts = {"-arch=sm_103a", "-std=c++17", "-lineinfo", "-default-device"};
+  for (int i = 0; i < n_include_dirs; ++i)
+    if (include_dirs && include_dirs[i]) opts.push_back(std::string("--include-path=") + include_dirs[i]);
+  std::vector<const char*> copts;
+  for (auto& o : opts) copts.push_back(o.c_str());
+  r = nvrtcCompileProgram(prog, (int)copts.size(), copts.data());
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string msg(n, '\0');
+    if (n) nvrtcGetProgramLog(prog, &msg[0]);
+    if (log && log_cap) {
+      const size_t k = msg.size() < log_cap - 1 ? msg.size() : log_cap - 1;
+      msg.copy(log, k);
+      log[k] = 0;
+    }
+    nvrtcDestroyProgram(&prog);
+    return fail(TQ_ERR_CUDA, "tq_jit_build: NVRTC compilation failed (%s): %.300s", nvrtcGetErrorString(r),
+                msg.c_str());
+  }
+  size_t size = 0;
+  r = nvrtcGetCUBINSize(prog, &size);
+  if (r != NVRTC_SUCCESS || size == 0) {
+    nvrtcDestroyProgram(&prog);
+    return nvrtc_fail(r, "tq_jit_build: nvrtcGetCUBINSize");
+  }
+  void* buf = std::malloc(size);
+  if (!buf) {
+    nvrtcDestroyProgram(&prog);
+    return fail(TQ_ERR_RANGE, "tq_jit_build: no host memory for a %zu-byte cubin", size);
+  }
+  r = nvrtcGetCUBIN(prog, static_cast<char*>(buf));
+  nvrtcDestroyProgram(&prog);
+  if (r != NVRTC_SUCCESS) {
+    std::free(buf);
+    return nvrtc_fail(r, "tq_jit_build: nvrtcGetCUBIN");
+  }
+  *cubin = buf;
+  *cubin_size = size;
+  return TQ_OK;
+}
+
+extern "C" void tq_jit_free_host(void* p) { std::free(p); }
+
+extern "C" int tq_jit_load(const void* cubin, size_t cubin_size, const char* kernel_name, void** kernel_out) {
+  if (!cubin || !cubin_size || !kernel_name || !kernel_out) return fail(TQ_ERR_ARG, "tq_jit_load: NULL argument");
+  *kernel_out = nullptr;
+  JitKernel* k = new JitKernel();
+  cudaError_t e = cudaLibraryLoadData(&k->lib, cubin, nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) {
+    delete k;
+    return cuda_status(e, "tq_jit_load: cudaLibraryLoadData");
+  }
+  e = cudaLibraryGetKernel(&k->kernel, k->lib, kernel_name);
+  if (e != cudaSuccess) {
+    cudaLibraryUnload(k->lib);
+    delete k;
+    return fail(TQ_ERR_CUDA, "tq_jit_load: kernel '%s' not found: %s", kernel_name, cudaGetErrorString(e));
+  }
+  *kernel_out = k;
+  return TQ_OK;
+}
+
+extern "C" int tq_jit_unload(void* kernel) {
+  if (!kernel) return TQ_OK;
+  JitKernel* k = static_cast<JitKernel*>(kernel);
+  cudaError_t e = cudaLibraryUnload(k->lib);
+  delete k;
+  return e == cudaSuccess ? TQ_OK : cuda_status(e, "tq_jit_unload");
+}
+
+extern "C" size_t tq_jit_rops_bytes(int dtype, int n_ops) {
+  return (size_t)(n_ops > 0 ? n_ops : 0) * (dtype == TQ_C64 ? sizeof(ROp<float>) : sizeof(ROp<double>));
+}
+
+extern "C" int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
+                                const tq_tile_stage* stages, const tq_tile_op* ops, const double* theta,
+                                void* stream);
+
+extern "C" int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dtype, const tq_tile_pass* passes,
+                                 int n_passes, const tq_tile_stage* stages_host, const tq_tile_stage* stages,
+                                 const tq_tile_op* ops, int n_ops, const double* theta, void* ws, size_t ws_bytes,
+                                 void* stream) {
+  int rc = check_n(n, dtype);
+  if (rc) return rc;
+  if (n_passes <= 0) return TQ_OK;
+  if (!kernels || !passes || !stages_host || !stages || !ops || !psi)
+    return fail(TQ_ERR_ARG, "tq_jit_run_staged: NULL argument");
+  if (n_ops <= 0) return fail(TQ_ERR_ARG, "tq_jit_run_staged: empty op table");
+  const size_t need = tq_jit_rops_bytes(dtype, n_ops);
+  if (!ws || ws_bytes < need)
+    return fail(TQ_ERR_WORKSPACE, "tq_jit_run_staged: workspace of %zu bytes, %zu needed", ws_bytes, need);
+  if ((reinterpret_cast<uintptr_t>(ws) & 15) != 0) return fail(TQ_ERR_ARG, "tq_jit_run_staged: workspace not 16-byte aligned");
+  const int tmax = dtype == TQ_C64 ? 13 : 12;
+  for (int p = 0; p < n_passes; ++p) {
+    const tq_tile_pass& tp = passes[p];
+    if (tp.op_end == tp.op_begin || !kernels[p]) continue;
+    if (tp.t < 9 || tp.t > tmax || tp.t > n || tp.nlow < 1 || tp.nlow > tp.t)
+      return fail(TQ_ERR_ARG, "tq_jit_run_staged: pass %d has t=%d nlow=%d (n=%d)", p, tp.t, tp.nlow, n);
+    const int op0 = stages_host[tp.op_begin].op_begin, op1 = stages_host[tp.op_end - 1].op_end;
+    if (op0 < 0 || op1 > n_ops || op1 - op0 <= 0 || op1 - op0 > kStagedRopCap)
+      return fail(TQ_ERR_RANGE, "tq_jit_run_staged: pass %d has ops [%d, %d) (table %d, at most %d per pass)", p,
+                  op0, op1, n_ops, kStagedRopCap);
+  }
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned cb = (unsigned)((n_ops + 127) / 128);
+  if (dtype == TQ_C64)
+    k_rops_compile<float><<<cb, 128, 0, s>>>(static_cast<ROp<float>*>(ws), ops, n_ops, theta);
+  else
+    k_rops_compile<double><<<cb, 128, 0, s>>>(static_cast<ROp<double>*>(ws), ops, n_ops, theta);
+  TQ_CHECK_LAUNCH("tq_jit_run_staged: op records");
+  for (int p = 0; p < n_passes; ++p) {
+    const tq_tile_pass& tp = passes[p];
+    if (tp.op_end == tp.op_begin) continue;
+    if (!kernels[p]) {  // the interpreting kernel for this pass
+      rc = tq_sv_run_staged(psi, n, dtype, &tp, 1, stages, ops, theta, stream);
+      if (rc) return rc;
+      continue;
+    }
+    PassArgs P;
+    P.t = tp.t;
+    P.nlow = tp.nlow;
+    P.op_begin = tp.op_begin;
+    P.op_end = tp.op_end;
+    for (int i = 0; i < TQ_TILE_MAX_BITS; ++i) P.pos[i] = tp.pos[i];
+    const int nops = stages_host[tp.op_end - 1].op_end - stages_host[tp.op_begin].op_begin;
+    const int threads = 1 << (tp.t - kRB);
+    const int64_t ntiles = int64_t(1) << (n - tp.t);
+    cudaKernel_t k = static_cast<JitKernel*>(kernels[p])->kernel;
+    // occupancy with double buffering sets the grid; one buffer when every CTA owns one tile
+    size_t smem = dtype == TQ_C64 ? jit_smem_bytes<float>(tp.t, tp.nlow, nops, 1)
+                                  : jit_smem_bytes<double>(tp.t, tp.nlow, nops, 1);
+    cudaError_t e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem, dev);
+    if (e != cudaSuccess) return cuda_status(e, "tq_jit_run_staged: shared memory attribute");
+    int occ = 1;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, threads, smem);
+    if (e != cudaSuccess) return cuda_status(e, "tq_jit_run_staged: occupancy");
+    if (occ < 1) occ = 1;
+    const int64_t cap = (int64_t)sms * occ;
+    int dbuf = ntiles > cap ? 1 : 0;
+    if (!dbuf)
+      smem = dtype == TQ_C64 ? jit_smem_bytes<float>(tp.t, tp.nlow, nops, 0)
+                             : jit_smem_bytes<double>(tp.t, tp.nlow, nops, 0);
+    const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
+    void* rops = ws;
+    void* args[] = {&psi, &n, &P, (void*)&stages, (void*)&ops, &rops, &dbuf};
+    e = cudaLaunchKernel((const void*)k, dim3(grid), dim3(threads), args, smem, s);
+    if (e != cudaSuccess) return cuda_status(e, "tq_jit_run_staged: launch");
+  }
+  return TQ_OK;
+}

@@ -1,0 +1,135 @@
+// Runtime-specialised register-staged forward passes.
+//
+// The library's k_staged_forward interprets each pass's op list: every op is
+// a switch over its compiled code, and every op writes all 16 registers of
+// the other register array, so a pass of a random circuit spends most of its
+// instructions on dispatch and register moves.  Here the op list of a pass is
+// turned into straight-line code instead (tyxonq_gb300/jit.py writes one body
+// per pass and this header wraps it; the source is compiled at run time by
+// NVRTC, csrc/jit.cu).  Register bits, stage layouts and op shapes become
+// compile-time constants: permutations (CX, SWAP) are register renames, CZ a
+// few sign flips, rotations their FMAs.  Coefficients are still compiled
+// from the op table and theta into op records (rop_build, by the library's
+// k_rops_compile once per program run) that each CTA copies to shared memory,
+// so one body serves every angle vector of the same circuit structure.
+#pragma once
+
+#include "staged_io.cuh"
+
+namespace tq {
+
+// In-place dense 4x4 on register bits (A = matrix high bit, B = low bit).
+template <typename R, int A, int B>
+__device__ __forceinline__ void j_u2(cplx<R>* x, const tq_tile_op& o) {
+  cplx<R> u[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) u[e] = op_m<R>(o, e);
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) {
+    if (((i >> A) & 1) || ((i >> B) & 1)) continue;
+    const int id[4] = {i, i | (1 << B), i | (1 << A), i | (1 << A) | (1 << B)};
+    const cplx<R> v[4] = {x[id[0]], x[id[1]], x[id[2]], x[id[3]]};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      cplx<R> acc = cmul(u[4 * r], v[0]);
+      acc = cfma(u[4 * r + 1], v[1], acc);
+      acc = cfma(u[4 * r + 2], v[2], acc);
+      acc = cfma(u[4 * r + 3], v[3], acc);
+      x[id[r]] = acc;
+    }
+  }
+}
+
+// In-place Pauli rotation exp(-i a/2 P) on register bits: X/Y bits XM, Z/Y bits
+// ZM, control bits CM (all compile-time), coefficients c = m0 (real part used,
+// as the library's t_prot) and w = sign * m1.
+template <typename R, int XM, int ZM, int CM>
+__device__ __forceinline__ void j_prot(cplx<R>* x, cplx<R> c, cplx<R> w) {
+  if constexpr (XM == 0) {
+#pragma unroll
+    for (int i = 0; i < kNR; ++i) {
+      if ((i & CM) != CM) continue;
+      const R sg = (__popc(i & ZM) & 1) ? R(-1) : R(1);
+      x[i] = cmul(cplx<R>(c.x + sg * w.x, sg * w.y), x[i]);
+    }
+  } else {
+    constexpr int H = (XM & 8) ? 3 : (XM & 4) ? 2 : (XM & 2) ? 1 : 0;
+#pragma unroll
+    for (int i = 0; i < kNR; ++i) {
+      if ((i >> H) & 1) continue;
+      if ((i & CM) != CM) continue;
+      const int j = i ^ XM;
+      const R si = (__popc(i & ZM) & 1) ? R(-1) : R(1);
+      const R sj = (__popc(j & ZM) & 1) ? R(-1) : R(1);
+      const cplx<R> a = x[i], b = x[j];
+      x[i] = cfma(cplx<R>(w.x * sj, w.y * sj), b, cplx<R>(c.x * a.x, c.x * a.y));
+      x[j] = cfma(cplx<R>(w.x * si, w.y * si), a, cplx<R>(c.x * b.x, c.x * b.y));
+    }
+  }
+}
+
+// Load / store the 16 registers of a stage: off[i] = padded offset of register
+// pattern i (compile-time), p0 = padded address of the thread's base index.
+template <typename R>
+__device__ __forceinline__ void j_load(cplx<R>* x, const cplx<R>* s, int p0, const int (&off)[kNR]) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) x[i] = s[p0 + off[i]];
+}
+template <typename R>
+__device__ __forceinline__ void j_store(const cplx<R>* x, cplx<R>* s, int p0, const int (&off)[kNR]) {
+#pragma unroll
+  for (int i = 0; i < kNR; ++i) s[p0 + off[i]] = x[i];
+}
+
+// The tile loop of one forward pass (same memory schedule as k_staged_forward:
+// persistent CTAs, cp.async double buffering when a CTA owns several tiles,
+// the pass's op records in shared memory).  body(s, rops, gbase) applies every
+// stage of the pass to the padded tile s and ends with a barrier.
+template <typename R, typename Body>
+__device__ __forceinline__ void jit_staged_forward(typename C2<R>::T* psi, int n, const PassArgs& P,
+                                                   const tq_tile_stage* __restrict__ stages,
+                                                   const ROp<R>* __restrict__ rops_g, int dbuf, Body body) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int PT = padded_len(P.t);
+  cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem);
+  cplx<R>* buf1 = buf0 + (dbuf ? PT : 0);
+  int64_t* hoff = reinterpret_cast<int64_t*>(smem + (size_t)(dbuf ? 2 : 1) * PT * sizeof(cplx<R>));
+  ROp<R>* rops = reinterpret_cast<ROp<R>*>(reinterpret_cast<unsigned char*>(hoff) + staged_hoff_bytes(P.t, P.nlow));
+  build_hoff(hoff, P);
+  // the pass's compiled op records (k_rops_compile, once per program run)
+  const int op0 = stages[P.op_begin].op_begin;
+  const int nwords = (stages[P.op_end - 1].op_end - op0) * (int)(sizeof(ROp<R>) / 16);
+  const uint4* src = reinterpret_cast<const uint4*>(rops_g + op0);
+  uint4* dst = reinterpret_cast<uint4*>(rops);
+  for (int w = threadIdx.x; w < nwords; w += blockDim.x) dst[w] = __ldg(&src[w]);
+  __syncthreads();
+  const int64_t ntiles = int64_t(1) << (n - P.t);
+  int64_t g = blockIdx.x;
+  if (g < ntiles) staged_issue_load<R>(buf0, psi, tile_base(g, P), hoff, P);
+  cp_async_commit();
+  int cur = 0;
+  for (; g < ntiles; g += gridDim.x) {
+    const int64_t gn = g + gridDim.x;
+    cplx<R>* s = cur ? buf1 : buf0;
+    if (dbuf) {
+      if (gn < ntiles) staged_issue_load<R>(cur ? buf0 : buf1, psi, tile_base(gn, P), hoff, P);
+      cp_async_commit();
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
+    }
+    __syncthreads();
+    const uint64_t gbase = (uint64_t)tile_base(g, P);
+    body(s, rops, gbase);
+    staged_store<R>(s, psi, (int64_t)gbase, hoff, P);
+    __syncthreads();
+    if (!dbuf && gn < ntiles) {
+      staged_issue_load<R>(buf0, psi, tile_base(gn, P), hoff, P);
+      cp_async_commit();
+    }
+    cur ^= dbuf;
+  }
+  cp_async_wait_group<0>();
+}
+
+}  // namespace tq

@@ -6,16 +6,11 @@
 // back once: algorithmic bytes 2*N*S per pass (4*N*S for the adjoint pass,
 // which carries psi and lambda), however many gates the pass holds.
 #include "stage.cuh"
+#include "staged_io.cuh"
 
 namespace tq {
 
 static const int kTileGridCap = 152 * 8;
-
-struct PassArgs {
-  int t, nlow;
-  int op_begin, op_end;
-  int pos[TQ_TILE_MAX_BITS];
-};
 
 static PassArgs to_args(const tq_tile_pass& p) {
   PassArgs a;
@@ -25,23 +20,6 @@ static PassArgs to_args(const tq_tile_pass& p) {
   a.op_end = p.op_end;
   for (int i = 0; i < TQ_TILE_MAX_BITS; ++i) a.pos[i] = p.pos[i];
   return a;
-}
-
-// hoff[h] = global offset of local index (h << nlow).
-__device__ __forceinline__ void build_hoff(int64_t* hoff, const PassArgs& P) {
-  const int nh = 1 << (P.t - P.nlow);
-  for (int h = threadIdx.x; h < nh; h += blockDim.x) {
-    int64_t off = 0;
-    for (int k = 0; k < P.t - P.nlow; ++k)
-      if ((h >> k) & 1) off |= int64_t(1) << P.pos[P.nlow + k];
-    hoff[h] = off;
-  }
-}
-
-__device__ __forceinline__ int64_t tile_base(int64_t g, const PassArgs& P) {
-  int64_t x = g << P.nlow;
-  for (int k = P.nlow; k < P.t; ++k) x = insert_zero(x, P.pos[k]);
-  return x;
 }
 
 // Tile <-> global copies.  complex64 moves two amplitudes per 16-byte access.
@@ -389,46 +367,6 @@ extern "C" int tq_sv_generator_im(const void* psi, const void* lam, int n, int d
 
 // ----------------------------------------------------------------- register-staged forward passes
 namespace tq {
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-// Issue (without waiting) the async copy of one tile into a padded buffer.
-template <typename R>
-__device__ __forceinline__ void staged_issue_load(cplx<R>* s, const typename C2<R>::T* g, int64_t base,
-                                                  const int64_t* hoff, const PassArgs& P) {
-  constexpr int A = 16 / sizeof(cplx<R>);
-  const int nc = (1 << P.t) / A;
-  const int lm = (1 << P.nlow) - 1;
-  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-    const int j = c * A;
-    cp_async16(&s[pphys(j)], &g[base + hoff[j >> P.nlow] + (j & lm)]);
-  }
-}
-
-template <typename R>
-__device__ __forceinline__ void staged_store(const cplx<R>* s, typename C2<R>::T* g, int64_t base,
-                                             const int64_t* hoff, const PassArgs& P) {
-  constexpr int A = 16 / sizeof(cplx<R>);
-  const int nc = (1 << P.t) / A;
-  const int lm = (1 << P.nlow) - 1;
-  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-    const int j = c * A;
-    *reinterpret_cast<float4*>(&g[base + hoff[j >> P.nlow] + (j & lm)]) =
-        *reinterpret_cast<const float4*>(&s[pphys(j)]);
-  }
-}
-
-// Compiled ops of one pass kept in shared memory for all its tiles.
-constexpr int kStagedRopCap = 256;
-
-// Offset-table bytes of a staged pass, rounded up to 16 (the compiled ops follow it).
-__host__ __device__ __forceinline__ size_t staged_hoff_bytes(int t, int nlow) {
-  return ((sizeof(int64_t) << (t - nlow)) + 15) & ~size_t(15);
-}
 
 // Shared memory: one or two padded tiles | offset table | compiled ops.
 template <typename R>

@@ -1,0 +1,351 @@
+"""Circuit-specialised register-staged passes (runtime-compiled CUDA).
+
+A staged forward program (``program.encode_staged``) is normally run by the
+library's interpreting kernel, which dispatches every op through a switch and
+moves all 16 registers per op.  ``specialise`` writes CUDA C++ in which each
+pass is straight-line register code: the stage layouts, register bits and op
+shapes are literals, permutations are register renames, and only the
+coefficients (compiled from the op table and theta on the device, exactly as
+the interpreter does) remain data.  The source is compiled for sm_103a in
+process by NVRTC (``tq_jit_build``, one kernel per distinct pass, built in
+parallel threads), cached as cubins on disk and per process, so programs with
+the same gate structure and different angles share the kernels.
+
+Coverage: every op code of the forward register stages (dense / real /
+imaginary / diagonal single-bit ops, runs fused on the device, CX / SWAP / CZ,
+dense 4x4, general Pauli rotations, Z signs from outside the stage).  A pass
+with more than 256 ops keeps the interpreter.
+"""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import os
+import threading
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from . import _native as nat
+
+CSRC = Path(__file__).resolve().parent / "csrc"
+INCLUDE = Path(__file__).resolve().parent.parent / "include"
+ROP_CAP = 256  # kStagedRopCap
+
+TOP_U1, TOP_D1, TOP_U2, TOP_CX, TOP_CZ, TOP_SWAP, TOP_PROT = 1, 2, 3, 4, 5, 6, 7
+
+
+def _one_bit(m: int) -> bool:
+    return m != 0 and (m & (m - 1)) == 0
+
+
+def _ffs(m: int) -> int:
+    return (m & -m).bit_length() - 1
+
+
+def _insz(b: str, p: int) -> str:
+    return f"b = ((b >> {p}) << {p + 1}) | (b & {(1 << p) - 1});"
+
+
+def _pphys(j: int) -> int:
+    return j + ((j >> 4) << 1)
+
+
+def _mat(o, e: int, double: bool) -> complex:
+    m = o["md"] if double else o["mf"]
+    return complex(m[2 * e], m[2 * e + 1])
+
+
+def _op_code(o, double: bool) -> tuple:
+    """(routine, args) the device compiles op record o into (rop_build, forward,
+    not fused); routine None = no-op."""
+    kind = int(o["kind"])
+    a, b = int(o["a"]) & 3, int(o["b"]) & 3
+    if kind == TOP_U1:
+        return "u1", a
+    if kind == TOP_D1:
+        if int(o["pidx"]) >= 0:
+            return "dh", a
+        d0 = _mat(o, 0, double)
+        return ("dh" if (d0.real == 1.0 and d0.imag == 0.0) else "d", a)
+    if kind == TOP_U2:
+        return ("u2", (int(o["a"]), int(o["b"]))) if o["a"] != o["b"] else (None, None)
+    if kind in (TOP_CX, TOP_SWAP, TOP_CZ):
+        mode = {TOP_CX: 0, TOP_SWAP: 1, TOP_CZ: 2}[kind]
+        return ("perm", (mode, a, b)) if a != b else (None, None)
+    if kind == TOP_PROT:
+        xm, zm, cm = int(o["xm"]) & 15, int(o["zm"]) & 15, int(o["cm"]) & 15
+        if cm == 0 and _one_bit(xm) and (zm & ~xm) == 0:
+            K = _ffs(xm)
+            if int(o["pidx"]) >= 0:
+                ny = bin(int(o["xm"]) & int(o["zm"])).count("1") & 3
+                return ("rr" if ny & 1 else "ri"), K
+            c, w = _mat(o, 0, double), _mat(o, 1, double)
+            if c.imag == 0.0 and w.imag == 0.0:
+                return "rr", K
+            if c.imag == 0.0 and w.real == 0.0:
+                return "ri", K
+            return "u1", K
+        if cm == 0 and xm == 0 and _one_bit(zm):
+            return "d", _ffs(zm)
+        if int(o["cm"]) >= 16:
+            return None, None  # the interpreter's (i & cm) == cm never holds: no-op
+        return "prot", (xm, int(o["zm"]) & 15, int(o["cm"]))
+    return None, None
+
+
+def _single_bit(o) -> int | None:
+    """Register bit of a fusable op (device op_mat2), else None."""
+    if int(o["zo"]) or int(o["zg"]):
+        return None
+    kind = int(o["kind"])
+    if kind in (TOP_U1, TOP_D1):
+        return int(o["a"]) & 3
+    if kind == TOP_PROT:
+        xm, zm, cm = int(o["xm"]) & 15, int(o["zm"]) & 15, int(o["cm"]) & 15
+        if cm:
+            return None
+        if _one_bit(xm) and (zm & ~xm) == 0:
+            return _ffs(xm)
+        if xm == 0 and _one_bit(zm):
+            return _ffs(zm)
+    return None
+
+
+def _emit_op(lines: list, k_rel: int, o, routine: str, arg, signed: bool) -> None:
+    r = f"rops[{k_rel}]"
+    s = "sg * " if signed else ""
+    pre = f"const ROp<R>& r = {r}; " + ("const R sg = rop_sign<R>(r, gbase, b); " if signed else "")
+    if routine == "u1":
+        call = (f"r_u1<R, kNR, {arg}>(x, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y), "
+                f"cplx<R>({s}r.m[2].x, {s}r.m[2].y), r.m[3]);")
+    elif routine == "rr":
+        call = f"r_rr<R, kNR, {arg}>(x, r.m[0].x, {s}r.m[1].x, {s}r.m[2].x);"
+    elif routine == "ri":
+        call = f"r_ri<R, kNR, {arg}>(x, r.m[0].x, {s}r.m[1].y, {s}r.m[2].y);"
+    elif routine == "d":
+        if signed:
+            call = f"r_d1<R, kNR, {arg}>(x, sg < R(0) ? r.m[1] : r.m[0], sg < R(0) ? r.m[0] : r.m[1]);"
+        else:
+            call = f"r_d1<R, kNR, {arg}>(x, r.m[0], r.m[1]);"
+    elif routine == "dh":
+        call = f"r_dh<R, kNR, {arg}>(x, r.m[1]);"
+    elif routine == "perm":
+        mode, a, b = arg
+        call = f"r_perm<R, kNR, {mode}, {a}, {b}>(x);"
+        pre = ""
+    elif routine == "u2":
+        A, B = arg
+        call = f"j_u2<R, {A}, {B}>(x, ops[r.op]);"
+    elif routine == "prot":
+        xm, zm, cm = arg
+        call = f"j_prot<R, {xm}, {zm}, {cm}>(x, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y));"
+    else:
+        return
+    lines.append(f"    {{ {pre}{call} }}")
+
+
+def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool) -> list[str] | None:
+    """Body lines of one pass (stages[p.op_begin:p.op_end]), or None if the
+    interpreter must run it."""
+    sb, se = int(p.op_begin), int(p.op_end)
+    if se <= sb:
+        return None
+    op0 = int(stages[sb]["op_begin"])
+    nops = int(stages[se - 1]["op_end"]) - op0
+    if nops <= 0 or nops > ROP_CAP:
+        return None
+    lines = []
+    for si in range(sb, se):
+        st = stages[si]
+        bits = [int(v) for v in st["bits"]]
+        if any(v < 0 for v in bits) or sorted(bits) != bits:
+            return None
+        lines.append(f"  {{  // stage bits {bits}")
+        lines.append("    int b = tid;")
+        for bb in bits:
+            lines.append("    " + _insz("b", bb))
+        lines.append("    const int p0 = b + ((b >> 4) << 1);")
+        offs = []
+        for i in range(16):
+            j = 0
+            for k in range(4):
+                if (i >> k) & 1:
+                    j |= 1 << bits[k]
+            offs.append(_pphys(j))
+        lines.append("    " + " ".join(f"x[{i}] = s[p0 + {offs[i]}];" for i in range(16)))
+        k, k1 = int(st["op_begin"]), int(st["op_end"])
+        while k < k1:
+            o = ops[k]
+            fuse = int(o["fuse_next"])
+            if fuse > 0 and _single_bit(o) is not None:
+                K = _single_bit(o)
+                j = 1
+                while j <= fuse and j < 16 and k + j < len(ops) and _single_bit(ops[k + j]) == K:
+                    j += 1
+                _emit_op(lines, k - op0, o, "u1", K, False)
+                k += j
+                continue
+            routine, arg = _op_code(o, double)
+            signed = bool(int(o["zo"]) or int(o["zg"]))
+            _emit_op(lines, k - op0, o, routine, arg, signed)
+            k += 1
+        lines.append("    " + " ".join(f"s[p0 + {offs[i]}] = x[{i}];" for i in range(16)))
+        lines.append("    __syncthreads();")
+        lines.append("  }")
+    return lines
+
+
+@dataclass
+class JitStaged:
+    """Specialised kernels of one staged segment: per pass a kernel handle
+    (0: the interpreting kernel runs that pass) and the op-record workspace."""
+
+    kernels: ctypes.Array
+    n_kernels: int
+    ws: torch.Tensor | None = None
+
+
+_kernels: dict = {}  # (source hash, device) -> kernel handle
+_lock = threading.Lock()
+
+
+def cache_dir() -> Path:
+    """Cubin cache: $TQ_JIT_CACHE, else ~/.cache/tyxonq_gb300/jit."""
+    d = os.environ.get("TQ_JIT_CACHE")
+    return Path(d) if d else Path.home() / ".cache" / "tyxonq_gb300" / "jit"
+
+
+def pass_source(t: int, body: str, double: bool) -> str:
+    R = "double" if double else "float"
+    T2 = "double2" if double else "float2"
+    return "\n".join([
+        '#include "jit_staged.cuh"',
+        "",
+        "namespace tq {",
+        "template <typename R>",
+        "__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ s, const ROp<R>* __restrict__ rops, "
+        "const tq_tile_op* __restrict__ ops, uint64_t gbase) {",
+        "  const int tid = threadIdx.x;",
+        "  cplx<R> x[kNR];",
+        body,
+        "}",
+        "}  // namespace tq",
+        "",
+        f'extern "C" __global__ void __launch_bounds__({1 << (t - 4)}, 1) {KERNEL_NAME}({T2}* psi, int n, '
+        "const tq::PassArgs P, const tq_tile_stage* __restrict__ stages, "
+        f"const tq_tile_op* __restrict__ ops, const tq::ROp<{R}>* __restrict__ rops_g, int dbuf) {{",
+        f"  tq::jit_staged_forward<{R}>(psi, n, P, stages, rops_g, dbuf, "
+        f"[&](tq::cplx<{R}>* s, const tq::ROp<{R}>* rops, uint64_t gbase) "
+        f"{{ tq::jit_body<{R}>(s, rops, ops, gbase); }});",
+        "}",
+        "",
+    ])
+
+
+KERNEL_NAME = "tq_jit_staged_pass"
+
+
+def _headers_digest() -> str:
+    h = hashlib.sha256()
+    for f in sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h")):
+        h.update(f.name.encode())
+        h.update(f.read_bytes())
+    return h.hexdigest()[:16]
+
+
+def _build_cubin(source: str) -> bytes:
+    lib = nat.load()
+    inc = [str(CSRC).encode(), str(INCLUDE).encode()]
+    inc_arr = (ctypes.c_char_p * len(inc))(*inc)
+    out, size = ctypes.c_void_p(), ctypes.c_size_t()
+    log = ctypes.create_string_buffer(8192)
+    rc = lib.tq_jit_build(source.encode(), inc_arr, len(inc), ctypes.byref(out), ctypes.byref(size), log, len(log))
+    if rc != 0:
+        _, msg = nat.last_error()
+        raise nat.TqError(rc, msg + "\n" + log.value.decode(errors="replace")[:4000])
+    try:
+        return ctypes.string_at(out.value, size.value)
+    finally:
+        lib.tq_jit_free_host(out)
+
+
+def kernels_for(sources: list[str], device) -> list[int]:
+    """Kernel handles for the given sources on `device` (built in parallel,
+    cubins cached on disk by source and header digest)."""
+    dev = torch.device(device)
+    digest = _headers_digest()
+    keys = [hashlib.sha256((digest + "\0" + src).encode()).hexdigest() for src in sources]
+    cdir = cache_dir()
+    need = [i for i, k in enumerate(keys) if (k, dev.index) not in _kernels]
+    blobs: dict[int, bytes] = {}
+    todo = []
+    for i in need:
+        f = cdir / f"{keys[i]}.cubin"
+        if f.exists():
+            blobs[i] = f.read_bytes()
+        else:
+            todo.append(i)
+    if todo:
+        with ThreadPoolExecutor(max_workers=min(len(todo), os.cpu_count() or 1, 32)) as ex:
+            for i, blob in zip(todo, ex.map(lambda j: _build_cubin(sources[j]), todo)):
+                blobs[i] = blob
+                try:
+                    cdir.mkdir(parents=True, exist_ok=True)
+                    tmp = cdir / f"{keys[i]}.{os.getpid()}.tmp"
+                    tmp.write_bytes(blob)
+                    os.replace(tmp, cdir / f"{keys[i]}.cubin")
+                except OSError:
+                    pass  # an unwritable cache only costs a rebuild
+    lib = nat.load()
+    with _lock, torch.cuda.device(dev):
+        for i in need:
+            if (keys[i], dev.index) in _kernels:
+                continue
+            h = ctypes.c_void_p()
+            blob = blobs[i]
+            nat.check(lib.tq_jit_load(blob, len(blob), KERNEL_NAME.encode(), ctypes.byref(h)))
+            _kernels[(keys[i], dev.index)] = h.value
+        return [_kernels[(k, dev.index)] for k in keys]
+
+
+def specialise(enc, dtype, device="cuda") -> JitStaged | None:
+    """Specialised kernels for the passes of an EncodedStaged program; None
+    when no pass qualifies."""
+    double = dtype == torch.complex128
+    tmax = 12 if double else 13
+    srcs, where = [], []
+    for pi in range(enc.n_passes):
+        p = enc.passes[pi]
+        if not (9 <= int(p.t) <= tmax):
+            continue
+        lines = _pass_body(enc.stages_host, enc.ops_host, p, double)
+        if lines is None:
+            continue
+        srcs.append(pass_source(int(p.t), "\n".join(lines), double))
+        where.append(pi)
+    if not srcs:
+        return None
+    uniq = list(dict.fromkeys(srcs))
+    handles = dict(zip(uniq, kernels_for(uniq, device)))
+    arr = (ctypes.c_void_p * max(enc.n_passes, 1))()
+    for pi, src in zip(where, srcs):
+        arr[pi] = handles[src]
+    return JitStaged(arr, len(where))
+
+
+def run_staged(js: JitStaged, enc, psi: torch.Tensor, n: int, dtag: int, theta_ptr, stream) -> None:
+    """Launch every pass of enc (specialised kernels; the interpreter for passes without one)."""
+    st_d, ops_d = enc.device_tables(psi.device)
+    lib = nat.load()
+    n_ops = len(enc.ops_host)
+    need = int(lib.tq_jit_rops_bytes(dtag, n_ops))
+    if js.ws is None or js.ws.numel() < need or js.ws.device != psi.device:
+        js.ws = torch.empty(max(need, 16), dtype=torch.uint8, device=psi.device)
+    P = ctypes.c_void_p
+    nat.call("tq_jit_run_staged", js.kernels, P(psi.data_ptr()), n, dtag, enc.passes, enc.n_passes,
+             enc.stages_host.ctypes.data_as(P), P(st_d.data_ptr()), P(ops_d.data_ptr()), n_ops, theta_ptr,
+             P(js.ws.data_ptr()), js.ws.numel(), stream)

@@ -215,11 +215,15 @@ def expect_z(psi: torch.Tensor, qubit: int) -> float:
     return float(expect_z_all(psi)[qubit].item())
 
 
-def probabilities(psi: torch.Tensor) -> torch.Tensor:
-    """|psi|^2 (float32 for complex64 states, float64 for complex128)."""
+def probabilities(psi: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """|psi|^2 (float32 for complex64 states, float64 for complex128), into
+    `out` when given."""
     n = _check_state(psi)
-    out = torch.empty(psi.numel(), dtype=torch.float32 if psi.dtype == torch.complex64 else torch.float64,
-                      device=psi.device)
+    dt = torch.float32 if psi.dtype == torch.complex64 else torch.float64
+    if out is None:
+        out = torch.empty(psi.numel(), dtype=dt, device=psi.device)
+    elif out.dtype != dt or out.numel() != psi.numel() or not out.is_contiguous() or out.device != psi.device:
+        raise ValueError("probabilities: `out` must be a contiguous tensor of the state's size and real dtype")
     nat.call("tq_sv_probabilities", _ptr(psi), n, dtype_tag(psi), _ptr(out), stream_ptr(psi.device))
     return out
 

@@ -486,6 +486,10 @@ class ForwardProgram:
         for kind, obj in self.segments:
             if kind == "gate":
                 execute_plain(psi, [obj])
+            elif kind == "staged" and obj.jit is not None:
+                from . import jit
+
+                jit.run_staged(obj.jit, obj, psi, self.n, dt, th, K.stream_ptr(psi.device))
             elif kind == "staged":
                 st, ops = obj.device_tables(psi.device)
                 nat.call("tq_sv_run_staged", ctypes.c_void_p(psi.data_ptr()), self.n, dt, obj.passes, obj.n_passes,
@@ -496,6 +500,20 @@ class ForwardProgram:
                 nat.call("tq_sv_run_tiles", ctypes.c_void_p(psi.data_ptr()), self.n, dt, obj.passes, obj.n_passes,
                          ctypes.c_void_p(ops.data_ptr()), th, K.stream_ptr(psi.device))
         return psi
+
+    def specialise(self, dtype, device="cuda") -> int:
+        """Compile circuit-specialised kernels (runtime CUDA compilation, cached
+        per structure) for every register-staged segment; returns the number of
+        passes that run them."""
+        from . import jit
+
+        count = 0
+        for kind, obj in self.segments:
+            if kind == "staged" and obj.jit is None:
+                obj.jit = jit.specialise(obj, dtype, device)
+            if kind == "staged" and obj.jit is not None:
+                count += obj.jit.n_kernels
+        return count
 
 
 # ---------------------------------------------------------------- register stages
@@ -601,6 +619,7 @@ class EncodedStaged:
     stages_host: np.ndarray
     ops_host: np.ndarray
     _dev: tuple | None = None
+    jit: object | None = None  # jit.JitStaged: circuit-specialised kernels for these passes
 
     def device_tables(self, device):
         if self._dev is None or self._dev[0].device != torch.device(device):
