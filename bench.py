@@ -295,6 +295,41 @@ def bench_gate_kernels(args, dev):
             "single_gate": bench_single_gates(n2)}
 
 
+def bench_fused_28q(args) -> dict:
+    """The 28-qubit depth-40 random circuit (complex64) through the
+    circuit-specialised fused passes only: warm-up runs, then timed runs."""
+    import torch
+
+    from tyxonq_gb300 import kernels as K
+    from tyxonq_gb300.ir import lower_ops
+    from tyxonq_gb300.program import compile_forward
+    from tyxonq_gb300.workloads import random_circuit
+
+    class _C:
+        def __init__(self, n, ops):
+            self.num_qubits, self.ops = n, ops
+
+    n2 = 28
+    gates, _ = lower_ops(_C(n2, random_circuit(n2, 40, seed=1)), mode="run")
+    prog = compile_forward(gates, n2, torch.complex64)
+    prog.specialise(torch.complex64)
+    psi = K.init_statevector(n2, dtype=torch.complex64)
+    for _ in range(args.warmup):
+        prog.run(psi)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        a, b = _events()
+        a.record()
+        prog.run(psi)
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    m = sum(ms) / len(ms)
+    return {"passes": prog.n_passes, "ms": m, "pass_ms": m / prog.n_passes,
+            "pass_gbs": 2 * (1 << n2) * 8 / (m / prog.n_passes * 1e-3) / 1e9}
+
+
 def bench_small_configs(reps: int = 10) -> dict:
     """Per-call times, host parameters in and host results out, of
     * the 12-qubit HEA (4 layers of [RY on every qubit; CX ladder]) with the
@@ -441,6 +476,9 @@ def run_case(args):
     if args.case == "small":
         print(json.dumps({"case": "small", **bench_small_configs()}))
         return
+    if args.case == "fused":
+        print(json.dumps({"case": "fused", **bench_fused_28q(args)}))
+        return
     if args.case == "civector":
         from tyxonq_gb300 import chem
         from tyxonq_gb300.vqe import UCCSD
@@ -482,8 +520,9 @@ def main():
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="weak: every rank evaluates its own --count instances; strong: one --count workload "
                          "split over the ranks by estimated cost")
-    ap.add_argument("--case", default="full", choices=["full", "gates", "batched", "small", "civector"],
-                    help="gates / batched / small / civector (16-qubit UCCSD in CI space): run only that part "
+    ap.add_argument("--case", default="full", choices=["full", "gates", "fused", "batched", "small", "civector"],
+                    help="gates / fused (28-qubit circuit, specialised passes only) / batched / small / civector "
+                         "(16-qubit UCCSD in CI space): run only that part "
                          "(profiling captures); full: the benchmark line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -498,7 +537,7 @@ def main():
     import __graft_entry__ as ge
 
     ge.build()
-    from tyxonq_gb300.batch import BatchedVQE, plain_energy_and_grad
+    from tyxonq_gb300.batch import BatchedVQE
     from tyxonq_gb300.workloads import batched_vqe
 
     rank = int(os.environ.get("RANK", "0"))
@@ -577,17 +616,33 @@ def main():
     d2h = (e_host.numel() + g_host.numel()) * 8
     energies = e_host.numpy().copy()
 
-    # ---------------- plain single-circuit engine on an every-8th-instance sample
-    sample = list(range(0, len(insts), 8))
-    plain_energy_and_grad(insts[sample[0]])
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    worst = 0.0
+    # ---------------- plain single-circuit engine on an every-16th-instance sample: one launch per
+    # gate, each instance's evaluation captured once as a CUDA graph and replayed (GPU-bound)
+    from tyxonq_gb300.batch import PlainEngine
+
+    sample = list(range(0, len(insts), 16))
+    engines = []
     for i in sample:
-        e_p, _ = plain_energy_and_grad(insts[i])
-        worst = max(worst, abs(e_p - energies[i]) / max(1.0, insts[i].H.one_norm()))
+        eng = PlainEngine(insts[i])
+        eng.capture()
+        engines.append(eng)
+    for eng in engines:
+        eng.run()
     torch.cuda.synchronize()
-    plain_evals = len(sample) / (time.perf_counter() - t0)
+    a, b = _events()
+    a.record()
+    for eng in engines:
+        eng.run()
+    b.record()
+    torch.cuda.synchronize()
+    plain_ms = a.elapsed_time(b)
+    plain_evals = len(sample) / (plain_ms * 1e-3)
+    worst = 0.0
+    for i, eng in zip(sample, engines):
+        e_p, _ = eng.result()
+        worst = max(worst, abs(e_p - energies[i]))
+    del engines
+    torch.cuda.empty_cache()
 
     # ---------------- 28q gate kernels (memory-bound case) + roofline
     gk = bench_gate_kernels(args, dev)
@@ -642,8 +697,10 @@ def main():
                    "l2": "512 MiB buffer written between timed steps", "graph": "CUDA graph replay",
                    "classes": {c.name: len(c.work) for c in bv.launch_order}, "structures": bv.n_structures,
                    "build_s": build_s},
-        "plain_gpu": {"value": plain_evals, "unit": "evals/s", "sample": f"{len(sample)} of {len(insts)} (every 8th)",
-                      "speedup_batched": value / world / plain_evals, "max_energy_diff_rel": worst},
+        "plain_gpu": {"value": plain_evals, "unit": "evals/s",
+                      "sample": f"{len(sample)} of {len(insts)} (every 16th), each evaluation a replayed CUDA graph "
+                                "of one launch per gate",
+                      "speedup_batched": value / world / plain_evals, "max_energy_diff_abs": worst},
         "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "latency": {"p50_ms": serving[-1]["p50_ms"], "p99_ms": serving[-1]["p99_ms"], "sweep": serving,
                     "workload": "Poisson arrivals, 24 sessions x 2 optimizer steps, HEA n~U{10..26} depth~U{2..10}, "

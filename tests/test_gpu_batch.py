@@ -129,3 +129,19 @@ def test_three_bit_adjoint_stages_match_oracle():
         norm = inst.H.one_norm()
         assert abs(e[k] - e_ref) < 1e-5 * norm
         np.testing.assert_allclose(grads[k], g_ref, atol=1e-4 * norm)
+
+
+def test_plain_engine_graph_replay_matches_oracle():
+    """The benchmark's plain baseline: one launch per gate, captured once per
+    instance as a CUDA graph and replayed."""
+    from tyxonq_gb300.batch import PlainEngine
+
+    for inst in _instances(4, 17, (6, 14)):
+        eng = PlainEngine(inst, dtype=torch.complex128)
+        eng.capture()
+        for _ in range(2):  # replays start from |basis> every time
+            eng.run()
+            e, g = eng.result()
+            e_ref, g_ref = _oracle(inst)
+            assert abs(e - e_ref) < 1e-10
+            np.testing.assert_allclose(g, g_ref, atol=1e-10)

@@ -74,3 +74,85 @@ def test_chain_api_mirror_end_to_end():
     np.testing.assert_allclose(r["statevector"], [0, -1j], atol=1e-6)
     psi = Circuit(1).x(0).state()  # state() does not compile
     np.testing.assert_allclose(psi.cpu().numpy(), [0, 1], atol=1e-6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_circuit_expectation_known_answers_on_gpu(dtype, monkeypatch):
+    """The reference tests' known answers of Circuit.expectation
+    (tests_core_module/test_circuit_expectation.py:9-69), on the device."""
+    from tyxonq_gb300.circuit import Circuit
+    from tyxonq_gb300.gates import gate_x, gate_y, gate_z
+
+    monkeypatch.setenv("TYXONQ_GB300_DTYPE", dtype)
+    tol = 1e-10 if dtype == "complex128" else 1e-6
+    assert abs(Circuit(1).h(0).expectation((gate_x(), [0])) - 1.0) < tol
+    assert abs(Circuit(1).expectation((gate_z(), [0])) - 1.0) < tol
+    bell = Circuit(2).h(0).cx(0, 1)
+    assert abs(bell.expectation((gate_z(), [0]), (gate_z(), [1])) - 1.0) < tol
+    assert abs(bell.expectation((gate_x(), [0]), (gate_x(), [1])) - 1.0) < tol
+    assert abs(bell.expval((gate_y(), [0]), (gate_y(), [1])) + 1.0) < tol  # <YY> = -1 on |Phi+>
+    n = 3
+    c = Circuit(n)
+    for i in range(n):
+        c.h(i)
+    e = -sum(c.expectation((gate_x(), [i])) for i in range(n))
+    e += sum(c.expectation((gate_z(), [i]), (gate_z(), [i + 1])) for i in range(n - 1))
+    assert abs(e + 3.0) < tol
+    # callables and two-qubit factors, as the reference accepts them
+    assert abs(bell.expectation((gate_x, [0]), (np.kron(gate_x(), gate_x()), [0, 1])) - 1.0) < tol
+    with pytest.raises(NotImplementedError):
+        bell.expectation((np.eye(8), [0, 1, 1]))
+
+
+@pytest.mark.gpu
+def test_tyxonq_chain_on_gpu_matches_reference_engine():
+    """TyxonQ's own Circuit (sources given by TYXONQ_SRC) through install():
+    compile -> device -> run on the golden circuits gives the reference
+    engine's expectations and result layout; state() and Circuit.expectation
+    match too.  Skipped without TyxonQ sources."""
+    if not _tyxonq_available():
+        pytest.skip("TyxonQ sources not given (TYXONQ_SRC)")
+    import tyxonq as tq
+    import tyxonq.devices.simulators.statevector.engine as sv_mod
+    from tyxonq.libs.quantum_library.kernels.gates import gate_x, gate_z
+
+    from tests import golden_data
+    from tyxonq_gb300 import plugin
+
+    tq.set_backend("numpy")
+    cases = [c for c in golden_data.circuit_cases() if not any(o[0] in ("unitary", "kraus") for o in c[2])]
+    assert cases
+
+    def build(n, ops):
+        c = tq.Circuit(n)
+        c.ops = [tuple(o) for o in ops]
+        return c
+
+    def outputs():
+        out = []
+        for name, n, ops, _uc, _state, _runz in cases:
+            r = build(n, ops).compile().device(provider="simulator", device="statevector").run(shots=0)
+            rm = r[0]["result_meta"] if isinstance(r, list) else r["result_meta"]
+            psi = np.asarray(build(n, ops).state())
+            bell = tq.Circuit(2).h(0).cx(0, 1)
+            ex = bell.expectation((gate_z(), [0]), (gate_z(), [1])), bell.expectation((gate_x(), [0]))
+            out.append((name, dict(rm.get("expectations", {})), sorted(rm.keys()), psi, ex))
+        return out
+
+    ref = outputs()
+    plugin.install(replace_statevector=True)
+    try:
+        from tyxonq_gb300.engine import GpuStatevectorEngine
+
+        assert sv_mod.StatevectorEngine is GpuStatevectorEngine
+        gpu = outputs()
+    finally:
+        plugin.uninstall()
+    for (nm, ez, keys, psi, ex), (_, ez2, keys2, psi2, ex2) in zip(ref, gpu):
+        assert keys == keys2, nm
+        assert ez.keys() == ez2.keys(), nm
+        for k in ez:
+            assert abs(ez[k] - ez2[k]) < 1e-6, (nm, k)
+        np.testing.assert_allclose(psi2, psi, atol=1e-6, err_msg=nm)
+        np.testing.assert_allclose(ex2, ex, atol=1e-6)

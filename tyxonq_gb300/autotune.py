@@ -1,10 +1,20 @@
-"""Schedule autotuner: tile width (local qubits per shared-memory tile pass)
-and batched-kernel launch shape, picked by timing candidates on the device.
+"""Schedule autotuner, timing candidates on the device.
 
-Tuned choices are kept in memory per process and can be saved to / loaded
-from a JSON file (``TYXONQ_GB300_TUNE``, default ``~/.cache/tyxonq_gb300/tune.json``).
-Untuned sizes use defaults derived from shared-memory capacity: a complex64
-tile of 2^13 amplitudes is 64 KiB, so two forward tiles fit per SM.
+* Batched VQE (``tune_batched``): coordinate descent over the launch schedule
+  of ``BatchedVQE`` -- size-class boundaries (which qubit counts stay in one
+  CTA's shared memory), wave tile width, wave L2 budget, number of wave lanes,
+  adjoint register-stage width, ops per wave pass -- each candidate built,
+  captured as a CUDA graph and timed over whole evaluation steps.  The result
+  is saved as JSON (``save_schedule``); ``Schedule.default`` loads the file
+  for the current GPU (``TYXONQ_GB300_SCHEDULE`` or the package's
+  ``tuned/<gpu>.json``), so the benchmark and the tests run the tuned
+  schedule.  ``python -m tyxonq_gb300.autotune`` re-tunes on the benchmark's
+  4096-instance workload and writes the file.
+* Single-state programs (``tune_forward``): tile width (local qubits per
+  shared-memory tile pass) per (n, dtype), kept per process and in
+  ``TYXONQ_GB300_TUNE`` (default ``~/.cache/tyxonq_gb300/tune.json``).
+  Untuned sizes use defaults from shared-memory capacity: a complex64 tile of
+  2^13 amplitudes is 64 KiB.
 """
 from __future__ import annotations
 
@@ -106,4 +116,159 @@ def tune_forward(gates, n: int, dtype=torch.complex64, candidates: Sequence[int]
     return best, res
 
 
-_ = time  # re-exported for callers timing on the host
+
+# ---------------------------------------------------------------- batched schedule
+TUNED_DIR = Path(__file__).resolve().parent / "tuned"
+SCHEDULE_FIELDS = ("res8_max", "res4_max", "res2_max", "res1_max", "wave_t", "wave_hbits", "wave_budget",
+                   "wave_lanes", "wave_max_ops", "wave_adj_stage_bits")
+
+
+def _gpu_tag(device=None) -> str:
+    name = torch.cuda.get_device_name(device) if torch.cuda.is_available() else "cpu"
+    return "".join(c if c.isalnum() else "_" for c in name).strip("_").lower()
+
+
+def schedule_path(device=None) -> Path:
+    env = os.environ.get("TYXONQ_GB300_SCHEDULE")
+    return Path(env) if env else TUNED_DIR / f"{_gpu_tag(device)}.json"
+
+
+def load_schedule(dtype, device=None) -> dict | None:
+    """Tuned schedule fields for dtype on this GPU, or None."""
+    p = schedule_path(device)
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    ent = d.get("c64" if dtype == torch.complex64 else "c128")
+    if not ent:
+        return None
+    return {k: int(v) for k, v in ent["schedule"].items() if k in SCHEDULE_FIELDS}
+
+
+def save_schedule(dtype, fields: dict, table: list, workload: str, device=None, path: Path | None = None) -> Path:
+    p = Path(path or schedule_path(device))
+    p.parent.mkdir(parents=True, exist_ok=True)
+    d = json.loads(p.read_text()) if p.exists() else {}
+    d["gpu"] = torch.cuda.get_device_name(device)
+    d["c64" if dtype == torch.complex64 else "c128"] = {
+        "schedule": {k: int(fields[k]) for k in SCHEDULE_FIELDS}, "workload": workload,
+        "tuned_at": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
+        "candidates_ms": table}
+    p.write_text(json.dumps(d, indent=1))
+    return p
+
+
+def _candidates(field: str, cur: dict, dtype) -> list:
+    c64 = dtype == torch.complex64
+    top = 13 if c64 else 12
+    if field == "res1_max":
+        return [top - 1, top]
+    if field == "res2_max":
+        return [v for v in (top - 2, top - 1) if v <= cur["res1_max"]]
+    if field == "res4_max":
+        return [v for v in (top - 3, top - 2) if v <= cur["res2_max"]]
+    if field == "res8_max":
+        return [v for v in (top - 4, top - 3) if v <= cur["res4_max"]]
+    if field == "wave_t":
+        return [11, 12, 13] if c64 else [11, 12]
+    if field == "wave_budget":
+        return [32 << 20, 48 << 20, 64 << 20, 96 << 20]
+    if field == "wave_lanes":
+        return [1, 2, 3]
+    if field == "wave_adj_stage_bits":
+        return [3, 4]
+    if field == "wave_max_ops":
+        return [128, 256]
+    return [cur[field]]
+
+
+def time_batched(instances, schedule, dtype=torch.complex64, steps: int = 3, flush=None) -> float:
+    """Median ms of one graph-replayed evaluation of the instances under `schedule`
+    (an L2-sized buffer written before every timed step)."""
+    import numpy as np
+
+    from .batch import BatchedVQE
+
+    bv = BatchedVQE(instances, dtype=dtype, schedule=schedule)
+    bv.set_theta(np.concatenate([i.theta for i in instances]))
+    bv.capture()
+    if flush is None:
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=bv.device)
+    bv.run()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        bv.run()
+        b.record()
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    del bv
+    ts.sort()
+    return ts[len(ts) // 2]
+
+
+def tune_batched(instances, dtype=torch.complex64, steps: int = 3, order: Sequence[str] | None = None,
+                 log: Callable[[str], None] | None = None):
+    """Coordinate descent over the batched schedule from the current default;
+    returns (Schedule, [(fields, ms)] of every candidate timed)."""
+    from dataclasses import asdict, replace
+
+    from .batch import Schedule
+
+    best = Schedule.builtin(dtype)
+    cur = asdict(best)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    table = []
+    best_ms = time_batched(instances, best, dtype, steps, flush)
+    table.append(({k: cur[k] for k in SCHEDULE_FIELDS}, best_ms))
+    if log:
+        log(f"start {best_ms:.2f} ms")
+    for field in order or ("wave_lanes", "wave_budget", "wave_adj_stage_bits", "wave_t", "wave_max_ops",
+                           "res1_max", "res2_max", "res4_max", "res8_max"):
+        for v in _candidates(field, cur, dtype):
+            if v == cur[field]:
+                continue
+            trial = dict(cur)
+            trial[field] = v
+            if field == "wave_t":
+                trial["wave_hbits"] = v
+            try:
+                ms = time_batched(instances, replace(best, **{k: trial[k] for k in SCHEDULE_FIELDS}), dtype, steps,
+                                  flush)
+            except Exception as e:  # a candidate that does not fit (shared memory, L2) is skipped
+                if log:
+                    log(f"{field}={v}: skipped ({e})")
+                continue
+            table.append(({k: trial[k] for k in SCHEDULE_FIELDS}, ms))
+            if log:
+                log(f"{field}={v}: {ms:.2f} ms (best {best_ms:.2f})")
+            if ms < best_ms:
+                best_ms, cur = ms, trial
+                best = replace(best, **{k: trial[k] for k in SCHEDULE_FIELDS})
+    return best, table
+
+
+def main() -> None:
+    import argparse
+
+    from .workloads import batched_vqe
+
+    ap = argparse.ArgumentParser(description="tune the batched VQE schedule on this GPU")
+    ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--out", default=None)
+    args = ap.parse_args()
+    insts = batched_vqe(args.count, seed=3)
+    sched, table = tune_batched(insts, steps=args.steps, log=lambda m: print(m, flush=True))
+    from dataclasses import asdict
+
+    p = save_schedule(torch.complex64, asdict(sched), [[f, ms] for f, ms in table],
+                      f"batched_vqe({args.count}, seed=3)", path=args.out)
+    print(json.dumps({"schedule": {k: asdict(sched)[k] for k in SCHEDULE_FIELDS}, "file": str(p)}))
+
+
+if __name__ == "__main__":
+    main()

@@ -15,8 +15,10 @@ energies and gradients with a few persistent launches of
 (complex64; complex128 shifts every boundary down by one qubit).  Angles live
 on the device (ops read theta[pidx]), so a new parameter vector costs one
 H2D copy; the whole step (memsets + launches) can be captured in a CUDA graph
-(``capture``) and replayed.  The class boundaries, group counts and tile
-widths are the schedule the autotuner (tyxonq_gb300.autotune) searches.
+(``capture``) and replayed.  The class boundaries, wave tile width, L2 budget,
+lanes and stage widths are the schedule the autotuner
+(tyxonq_gb300.autotune.tune_batched) searches; ``Schedule.default`` is the
+tuned one for the current GPU when it was saved.
 """
 from __future__ import annotations
 
@@ -64,10 +66,23 @@ class Schedule:
     wave_adj_stage_bits: int = 4  # register bits per adjoint stage (3: 8 amplitudes of psi and of lam per thread)
 
     @classmethod
-    def default(cls, dtype) -> "Schedule":
+    def builtin(cls, dtype) -> "Schedule":
+        """The untuned schedule (shared-memory capacity rules)."""
         if dtype == torch.complex128:
             return cls(res8_max=9, res4_max=10, res2_max=11, res1_max=12, t_fwd=12, t_adj=11)
         return cls()
+
+    @classmethod
+    def default(cls, dtype, device=None) -> "Schedule":
+        """The autotuned schedule for this GPU when one was saved
+        (tyxonq_gb300.autotune), else the builtin one."""
+        from dataclasses import replace
+
+        from .autotune import load_schedule
+
+        base = cls.builtin(dtype)
+        tuned = load_schedule(dtype, device)
+        return replace(base, **tuned) if tuned else base
 
     def class_of(self, n: int) -> tuple[str, int, int]:
         """(class name, groups per CTA, threads per CTA)."""
@@ -383,14 +398,7 @@ def _to_dev(arr: np.ndarray, device) -> torch.Tensor:
 
 
 # ---------------------------------------------------------------- plain engine comparison
-def plain_energy_and_grad(inst, dtype=torch.complex64, device="cuda") -> tuple[float, np.ndarray]:
-    """The plain single-circuit GPU engine on one instance: one kernel launch per
-    gate forward, H psi, <psi|H psi>, then per gate in reverse one generator
-    reduction (tq_sv_generator_im) and two inverse-gate launches."""
-    from .engine import execute_plain
-    from .program import _generator
-
-    n = int(inst.n)
+def _plain_gates(inst):
     theta = np.asarray(inst.theta, dtype=np.float64)
     gates, params = [], []
     for name, qs, p in inst.structure():
@@ -401,28 +409,88 @@ def plain_energy_and_grad(inst, dtype=torch.complex64, device="cuda") -> tuple[f
         else:
             gates.append(_rot_gate(name, qs, float(theta[p])))
             params.append(int(p))
-    psi = K.init_statevector(n, dtype=dtype, device=device, basis_index=int(getattr(inst, "basis", 0)))
-    execute_plain(psi, gates)
-    lam = K.apply_pauli_sum(psi, inst.H)
-    e = K.inner_re(psi, lam)
-    lib = nat.load()
-    outs = []
-    loc = {q: n - 1 - q for q in range(n)}
-    buf = torch.empty(len(gates), dtype=torch.float64, device=device)
-    for gi in range(len(gates) - 1, -1, -1):
-        g = gates[gi]
-        if params[gi] is not None:
-            gx, gz, gc, _, coef = _generator(g, loc)
-            p_ws, cap = K._ws(lib.tq_sv_inner_workspace_bytes(n), device)
-            nat.call("tq_sv_generator_im", ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), n,
-                     K.dtype_tag(psi), gx, gz, gc, ctypes.c_void_p(buf.data_ptr() + 8 * gi), p_ws, cap,
-                     K.stream_ptr(device))
-            outs.append((gi, params[gi], coef))
-        inv = g if g.kind in ("cx", "cz", "swap") else Gate(g.kind, g.qubits, np.conj(g.mat).T)
-        execute_plain(psi, [inv])
-        execute_plain(lam, [inv])
-    vals = buf.cpu().numpy()
-    grad = np.zeros(int(inst.n_params))
-    for gi, p, coef in outs:
-        grad[p] += coef * vals[gi]
-    return float(e.item()), grad
+    return gates, params
+
+
+class PlainEngine:
+    """The plain single-circuit GPU engine on one instance: one kernel launch per
+    gate forward, H psi, <psi|H psi>, then per gate in reverse one generator
+    reduction (tq_sv_generator_im) and two inverse-gate launches.  Buffers are
+    allocated once; ``capture`` records the whole evaluation in a CUDA graph so
+    that replays are bound by the GPU, not by the host loop that issues the
+    launches."""
+
+    def __init__(self, inst, dtype=torch.complex64, device="cuda"):
+        from .program import _generator
+
+        self.inst = inst
+        self.n = n = int(inst.n)
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self.gates, self.params = _plain_gates(inst)
+        self.psi = torch.empty(1 << n, dtype=dtype, device=self.device)
+        self.lam = torch.empty_like(self.psi)
+        self.buf = torch.zeros(max(len(self.gates), 1), dtype=torch.float64, device=self.device)
+        self.energy = torch.zeros(1, dtype=torch.float64, device=self.device)
+        loc = {q: n - 1 - q for q in range(n)}
+        self.outs = []
+        self.gen = {}
+        for gi, g in enumerate(self.gates):
+            if self.params[gi] is not None:
+                gx, gz, gc, _, coef = _generator(g, loc)
+                self.gen[gi] = (gx, gz, gc)
+                self.outs.append((gi, self.params[gi], coef))
+        self.inv = [g if g.kind in ("cx", "cz", "swap") else Gate(g.kind, g.qubits, np.conj(g.mat).T)
+                    for g in self.gates]
+        self.graph = None
+
+    def launch(self) -> None:
+        from .engine import execute_plain
+
+        lib = nat.load()
+        n, dev = self.n, self.device
+        st = K.stream_ptr(dev)
+        nat.call("tq_sv_init_basis", ctypes.c_void_p(self.psi.data_ptr()), n, K.dtype_tag(self.psi),
+                 int(getattr(self.inst, "basis", 0)), st)
+        execute_plain(self.psi, self.gates)
+        K.apply_pauli_sum(self.psi, self.inst.H, out=self.lam)
+        p_ws, cap = K._ws(lib.tq_sv_inner_workspace_bytes(n), dev)
+        nat.call("tq_sv_inner_re", ctypes.c_void_p(self.psi.data_ptr()), ctypes.c_void_p(self.lam.data_ptr()), n,
+                 K.dtype_tag(self.psi), ctypes.c_void_p(self.energy.data_ptr()), p_ws, cap, st)
+        for gi in range(len(self.gates) - 1, -1, -1):
+            if gi in self.gen:
+                gx, gz, gc = self.gen[gi]
+                nat.call("tq_sv_generator_im", ctypes.c_void_p(self.psi.data_ptr()),
+                         ctypes.c_void_p(self.lam.data_ptr()), n, K.dtype_tag(self.psi), gx, gz, gc,
+                         ctypes.c_void_p(self.buf.data_ptr() + 8 * gi), p_ws, cap, st)
+            execute_plain(self.psi, [self.inv[gi]])
+            execute_plain(self.lam, [self.inv[gi]])
+
+    def capture(self) -> None:
+        self.launch()  # warm-up: device tables and workspaces exist before capture
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch()
+        self.graph = g
+
+    def run(self) -> None:
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.launch()
+
+    def result(self) -> tuple[float, np.ndarray]:
+        vals = self.buf.cpu().numpy()
+        grad = np.zeros(int(self.inst.n_params))
+        for gi, p, coef in self.outs:
+            grad[p] += coef * vals[gi]
+        return float(self.energy.item()), grad
+
+
+def plain_energy_and_grad(inst, dtype=torch.complex64, device="cuda") -> tuple[float, np.ndarray]:
+    """One evaluation of the plain single-circuit engine (launches issued from
+    the host, no graph)."""
+    eng = PlainEngine(inst, dtype, device)
+    eng.launch()
+    return eng.result()

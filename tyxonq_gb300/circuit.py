@@ -3,7 +3,8 @@ not installed.
 
 Mirrors tyxonq/core/ir/circuit.py: op tuples (name, qubits..., angle) in
 ``ops`` (:49-182), gate builders (:1042-1633), ``compile()`` / ``device()`` /
-``run()`` / ``state()`` (:191-214, :427-583, :828-981).  ``run`` applies the
+``run()`` / ``state()`` (:191-214, :427-583, :828-981), ``expectation`` of
+gate products (:1634-1787).  ``run`` applies the
 native compile pipeline's two rewrites that change results (auto
 ``measure_z`` on every qubit when none is present, auto_measure.py:23-35, and
 ``x`` -> ``rx(pi)``, gates_transform.py:31-32), honours the reference quirk
@@ -187,3 +188,11 @@ class Circuit:
 
     def expectation_ps(self, hamiltonian, **kw) -> float:
         return self._engine(**kw).expval(self, hamiltonian)
+
+    def expectation(self, *pauli_ops: Any) -> float:
+        """<psi|O|psi> for a product of (gate, qubits) factors (circuit.py:1634-1737)."""
+        return self._engine().expectation_product(self, pauli_ops)
+
+    def expval(self, *pauli_ops: Any) -> float:
+        """Alias of expectation (circuit.py:1720-1737)."""
+        return self.expectation(*pauli_ops)

@@ -211,6 +211,40 @@ class GpuStatevectorEngine:
         psi, _ = self.simulate(circuit, mode="state")
         return float(K.pauli_expectation(psi, obs, n).item())
 
+    def expectation_product(self, circuit, pauli_ops) -> float:
+        """Re <O psi|psi> for a product O of one- and two-qubit gate matrices
+        given as (gate, qubits) pairs, as Circuit._expectation_statevector does
+        (core/ir/circuit.py:1739-1787): the circuit's state, a copy with every
+        factor applied in order, and the real part of their inner product."""
+        n = int(getattr(circuit, "num_qubits", 0))
+        psi, _ = self.simulate(circuit, mode="state")
+        phi = psi.clone()
+        for spec in pauli_ops:
+            if not isinstance(spec, (tuple, list)) or len(spec) != 2:
+                raise ValueError(f"Each Pauli operator must be (gate, qubits), got {spec}")
+            gate, qubits = spec
+            if hasattr(gate, "tensor"):
+                m = gate.tensor
+            elif callable(gate):
+                m = gate()
+            else:
+                m = gate
+            m = np.asarray(m.detach().cpu().numpy() if hasattr(m, "detach") else m, dtype=np.complex128)
+            if not isinstance(qubits, (list, tuple)):
+                qubits = [qubits]
+            qs = [int(q) for q in qubits]
+            for q in qs:
+                if q < 0 or q >= n:
+                    raise ValueError(f"qubit index {q} out of range for {n} qubits")
+            if len(qs) == 1:
+                K.apply_1q(phi, m.reshape(2, 2), qs[0])
+            elif len(qs) == 2:
+                if qs[0] != qs[1]:  # the reference's 2q kernel leaves psi unchanged for q0 == q1
+                    K.apply_2q(phi, m.reshape(4, 4), qs[0], qs[1])
+            else:
+                raise NotImplementedError(f"Pauli products on {len(qs)} qubits not yet supported")
+        return float(K.inner_re(phi, psi).item())
+
     # ------------------------------------------------------------ extras
     def energy(self, circuit, hamiltonian) -> float:
         """Re <psi|H|psi> for a Pauli-sum H, FP64 accumulation."""

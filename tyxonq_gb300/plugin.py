@@ -6,7 +6,8 @@ imports ``StatevectorEngine`` from ``devices/simulators/statevector/engine``
 at call time (core/ir/circuit.py:491-494).  ``install`` wraps the former so
 ``device="statevector_gpu"`` (and, with ``replace_statevector``, plain
 ``"statevector"``) returns GpuStatevectorEngine, and rebinds the latter so
-``Circuit.state()`` runs on the GPU.  The chain API
+``Circuit.state()`` runs on the GPU; ``Circuit.expectation`` of gate products
+on a statevector device (circuit.py:1739-1787) runs on the GPU too.  The chain API
 ``c.compile().device(provider="simulator", device="statevector").run()`` then
 reaches the GPU engine unchanged.  ``uninstall`` restores both.
 """
@@ -38,7 +39,22 @@ def install(replace_statevector: bool = True, alias: str = "statevector_gpu"):
     drv._select_engine = _select_engine
     if replace_statevector:
         sv_mod.StatevectorEngine = GpuStatevectorEngine
+        _route_expectation(GpuStatevectorEngine)
     return GpuStatevectorEngine
+
+
+def _route_expectation(engine_cls) -> None:
+    """Circuit.expectation on a statevector device (core/ir/circuit.py:1739-1787)
+    runs the state and the operator product on the GPU."""
+    from tyxonq.core.ir.circuit import Circuit  # type: ignore
+
+    if "sv_expect" not in _saved:
+        _saved["sv_expect"] = Circuit._expectation_statevector
+
+    def _expectation_statevector(self, pauli_ops, nb, n):
+        return engine_cls().expectation_product(self, pauli_ops)
+
+    Circuit._expectation_statevector = _expectation_statevector
 
 
 def uninstall():
@@ -49,3 +65,7 @@ def uninstall():
 
     drv._select_engine = _saved["select"]
     sv_mod.StatevectorEngine = _saved["sv_cls"]
+    if "sv_expect" in _saved:
+        from tyxonq.core.ir.circuit import Circuit  # type: ignore
+
+        Circuit._expectation_statevector = _saved.pop("sv_expect")
