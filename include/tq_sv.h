@@ -400,6 +400,16 @@ TQ_API int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_ite
                        const tq_tile_op* ops, const tq_pauli_group* groups, const tq_pauli_term* terms,
                        const double* theta, void* pool, double* partials, int max_pass_ops, void* stream);
 
+/* One launch of a wave phase (kind 0 forward, 2 adjoint with 4-bit stages)
+ * with a circuit-specialised kernel (tq_jit_load of a wave source written by
+ * tyxonq_gb300/jit.py): every item of items[0..n_items) must use a pass whose
+ * body the kernel was generated for.  Arguments and shared memory as
+ * tq_wave_run, whose interpreting kernels it replaces pass body by pass body;
+ * both stand in for the reference's per-instance loop (devices/base.py:378-381). */
+TQ_API int tq_jit_wave_run(void* kernel, int kind, int dtype, const tq_wave_item* items, int n_items, int t,
+                           const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
+                           const double* theta, void* pool, double* partials, int max_ops, void* stream);
+
 /* H psi and / or <psi|H|psi> of one state (n >= 12) through the wave H psi
  * kernel: output tiles of 4096 amplitudes, 16 per thread, each group's terms
  * summed per class of the bits that tell a thread's amplitudes apart, then a

@@ -73,7 +73,8 @@ def test_chain_api_mirror_end_to_end():
     r = Circuit(1).x(0).run(shots=0)[0]["result_meta"]
     np.testing.assert_allclose(r["statevector"], [0, -1j], atol=1e-6)
     psi = Circuit(1).x(0).state()  # state() does not compile
-    np.testing.assert_allclose(psi.cpu().numpy(), [0, 1], atol=1e-6)
+    psi = psi.cpu().numpy() if hasattr(psi, "cpu") else np.asarray(psi)  # numpy backend when TyxonQ is importable
+    np.testing.assert_allclose(psi, [0, 1], atol=1e-6)
 
 
 @pytest.mark.gpu

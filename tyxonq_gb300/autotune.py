@@ -120,7 +120,7 @@ def tune_forward(gates, n: int, dtype=torch.complex64, candidates: Sequence[int]
 # ---------------------------------------------------------------- batched schedule
 TUNED_DIR = Path(__file__).resolve().parent / "tuned"
 SCHEDULE_FIELDS = ("res8_max", "res4_max", "res2_max", "res1_max", "wave_t", "wave_hbits", "wave_budget",
-                   "wave_lanes", "wave_max_ops", "wave_adj_stage_bits")
+                   "wave_lanes", "wave_max_ops", "wave_adj_stage_bits", "wave_jit")
 
 
 def _gpu_tag(device=None) -> str:

@@ -64,6 +64,7 @@ class Schedule:
     wave_lanes: int = 2  # waves in flight at once, each lane on its own stream
     wave_max_ops: int = 256
     wave_adj_stage_bits: int = 4  # register bits per adjoint stage (3: 8 amplitudes of psi and of lam per thread)
+    wave_jit: int = 1  # circuit-specialised wave kernels (runtime-compiled per distinct pass body)
 
     @classmethod
     def builtin(cls, dtype) -> "Schedule":
@@ -95,6 +96,13 @@ class Schedule:
         if n <= self.res1_max:
             return "res1", 1, 1024
         return "streamed", 1, 1024
+
+
+def _jit_enabled() -> bool:
+    """Circuit-specialised kernels are on unless TYXONQ_GB300_JIT=0."""
+    import os
+
+    return os.environ.get("TYXONQ_GB300_JIT", "1") != "0"
 
 
 def structure_gates(structure) -> tuple[list[Gate], dict]:
@@ -248,7 +256,7 @@ class BatchedVQE:
             sc = self.sched
             self.waves = WavePlan(wave_entries, dtype, dev, t=sc.wave_t, hbits=sc.wave_hbits, budget=sc.wave_budget,
                                   lanes=sc.wave_lanes, adj_stage_bits=sc.wave_adj_stage_bits,
-                                  max_ops=sc.wave_max_ops)
+                                  max_ops=sc.wave_max_ops, jit=bool(sc.wave_jit) and _jit_enabled())
             self.n_structures += self.waves.n_structures
         lib = nat.load()
         order = ["streamed", "res1", "res2", "res4", "res8"]
@@ -362,7 +370,11 @@ class BatchedVQE:
         wave reductions)."""
         n = len(self.launch_order)
         if self.waves is not None:
-            n += sum(1 for L in self.waves.launches if L[0] != "run" or L[3] > 0)
+            for li, L in enumerate(self.waves.launches):
+                if li in self.waves.jit_sub:
+                    n += len(self.waves.jit_sub[li])
+                elif L[0] != "run" or L[3] > 0:
+                    n += 1
         return n
 
     def capture(self) -> None:

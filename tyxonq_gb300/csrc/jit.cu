@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "staged_io.cuh"
+#include "wave_io.cuh"
 
 namespace tq {
 
@@ -212,3 +213,37 @@ extern "C" int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dty
   }
   return TQ_OK;
 }
+
+extern "C" int tq_jit_wave_run(void* kernel, int kind, int dtype, const tq_wave_item* items, int n_items, int t,
+                               const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
+                               const double* theta, void* pool, double* partials, int max_ops, void* stream) {
+  if (!kernel || !items || !passes || !stages || !ops || !pool || (kind == 2 && !partials))
+    return fail(TQ_ERR_ARG, "tq_jit_wave_run: NULL argument");
+  if (kind != 0 && kind != 2) return fail(TQ_ERR_ARG, "tq_jit_wave_run: kind %d (0 forward, 2 adjoint)", kind);
+  if (dtype != TQ_C64 && dtype != TQ_C128) return fail(TQ_ERR_ARG, "tq_jit_wave_run: dtype tag %d", dtype);
+  if (t < 9 || t > (dtype == TQ_C64 ? 13 : 12)) return fail(TQ_ERR_ARG, "tq_jit_wave_run: t=%d", t);
+  if (max_ops < 1 || max_ops > 4096) return fail(TQ_ERR_ARG, "tq_jit_wave_run: max_ops %d", max_ops);
+  if (n_items <= 0) return TQ_OK;
+  const size_t S = dtype == TQ_C64 ? sizeof(cplx<float>) : sizeof(cplx<double>);
+  const size_t rop = dtype == TQ_C64 ? sizeof(ROp<float>) : sizeof(ROp<double>);
+  const size_t R = dtype == TQ_C64 ? sizeof(float) : sizeof(double);
+  const int threads = 1 << (t - kRB);
+  size_t smem = (kind == 0 ? 1 : 2) * padded_len(t) * S + w_hoff_bytes(t) + (size_t)max_ops * rop;
+  if (kind == 2) smem += R * (size_t)max_ops * (threads / 32);
+  if (smem > 227 * 1024) return fail(TQ_ERR_ARG, "tq_jit_wave_run: %zu bytes of shared memory", smem);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "tq_jit_wave_run: device");
+  cudaKernel_t k = static_cast<JitKernel*>(kernel)->kernel;
+  e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem, dev);
+  if (e != cudaSuccess) return cuda_status(e, "tq_jit_wave_run: shared memory attribute");
+  void* args_f[] = {(void*)&items, &n_items, (void*)&passes, (void*)&stages, (void*)&ops, (void*)&theta, &pool,
+                    &max_ops};
+  void* args_a[] = {(void*)&items, &n_items, (void*)&passes, (void*)&stages, (void*)&ops, (void*)&theta, &pool,
+                    (void*)&partials, &max_ops};
+  e = cudaLaunchKernel((const void*)k, dim3((unsigned)n_items), dim3(threads), kind == 0 ? args_f : args_a, smem,
+                       (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "tq_jit_wave_run: launch");
+  return TQ_OK;
+}
+

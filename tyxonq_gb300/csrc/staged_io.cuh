@@ -32,12 +32,6 @@ __device__ __forceinline__ int64_t tile_base(int64_t g, const PassArgs& P) {
   return x;
 }
 
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // Issue (without waiting) the async copy of one tile into a padded buffer.
 template <typename R>
 __device__ __forceinline__ void staged_issue_load(cplx<R>* s, const typename C2<R>::T* g, int64_t base,

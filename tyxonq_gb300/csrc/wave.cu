@@ -16,80 +16,9 @@
 //           partials[part_off + k] per op k of the pass.
 // Gradient and energy partials are summed by tq_wave_reduce in a fixed order.
 #include "stage.cuh"
+#include "wave_io.cuh"
 
 namespace tq {
-
-struct WPass {
-  int t, nlow, op_begin, op_end;
-  int pos[TQ_TILE_MAX_BITS];
-};
-
-__device__ __forceinline__ WPass wload_pass(const tq_tile_pass* p) {
-  WPass s;
-  s.t = p->t;
-  s.nlow = p->nlow;
-  s.op_begin = p->op_begin;
-  s.op_end = p->op_end;
-#pragma unroll
-  for (int i = 0; i < TQ_TILE_MAX_BITS; ++i) s.pos[i] = p->pos[i];
-  return s;
-}
-
-__device__ __forceinline__ void w_hoff(int64_t* hoff, const WPass& P) {
-  const int nh = 1 << (P.t - P.nlow);
-  for (int h = threadIdx.x; h < nh; h += blockDim.x) {
-    int64_t off = 0;
-    for (int k = 0; k < P.t - P.nlow; ++k)
-      if ((h >> k) & 1) off |= int64_t(1) << P.pos[P.nlow + k];
-    hoff[h] = off;
-  }
-}
-
-// Passes of a wave keep at least kWaveMinNlow contiguous low bits, so the
-// offset table has at most 2^(t - kWaveMinNlow) entries.
-constexpr int kWaveMinNlow = 4;
-__host__ __device__ __forceinline__ size_t w_hoff_bytes(int t) { return sizeof(int64_t) << (t - kWaveMinNlow); }
-
-__device__ __forceinline__ int64_t w_base(int64_t g, const WPass& P) {
-  int64_t x = g << P.nlow;
-  for (int k = P.nlow; k < P.t; ++k) x = insert_zero(x, P.pos[k]);
-  return x;
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-__device__ __forceinline__ void w_commit_wait() {
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-}
-
-template <typename R>
-__device__ __forceinline__ void w_load(cplx<R>* s, const typename C2<R>::T* g, int64_t base, const int64_t* hoff,
-                                       const WPass& P) {
-  constexpr int A = 16 / sizeof(cplx<R>);
-  const int nc = (1 << P.t) / A;
-  const int lm = (1 << P.nlow) - 1;
-  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-    const int j = c * A;
-    cp_async16(&s[pphys(j)], &g[base + hoff[j >> P.nlow] + (j & lm)]);
-  }
-}
-
-template <typename R>
-__device__ __forceinline__ void w_store(const cplx<R>* s, typename C2<R>::T* g, int64_t base, const int64_t* hoff,
-                                        const WPass& P) {
-  constexpr int A = 16 / sizeof(cplx<R>);
-  const int nc = (1 << P.t) / A;
-  const int lm = (1 << P.nlow) - 1;
-  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-    const int j = c * A;
-    *reinterpret_cast<float4*>(&g[base + hoff[j >> P.nlow] + (j & lm)]) =
-        *reinterpret_cast<const float4*>(&s[pphys(j)]);
-  }
-}
 
 // ------------------------------------------------------------------ forward
 // Shared memory: padded tile | offset table (8 << (t - kWaveMinNlow) bytes) |

@@ -199,6 +199,172 @@ def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool) -> list[str
     return lines
 
 
+def _grad_code(o) -> tuple:
+    """Gradient routine of an adjoint record with a slot (rop_build, grad)."""
+    gx, gz, gc = int(o["gxm"]), int(o["gzm"]), int(o["gcm"])
+    if gc == 0 and _one_bit(gx) and gx < 16 and (gz & ~gx) == 0:
+        return "pair", _ffs(gx)
+    if gx == 0 and gc == 0 and _one_bit(gz) and gz < 16:
+        return "diag", _ffs(gz)
+    if gx == 0 and gz == 0 and _one_bit(gc) and gc < 16:
+        return "diag", _ffs(gc)
+    return "gen", (gx & 15, gz & 15, gc)
+
+
+def _emit_adj_op(lines: list, k_rel: int, o, double: bool) -> None:
+    """One adjoint op on psi (x) and lam (y) registers: the gradient term
+    Im <lam|G|psi> first (when the op has a slot), then the un-apply."""
+    routine, arg = _op_code(o, double)
+    if routine == "u2":
+        routine = "u2adj"
+    has_grad = int(o["slot"]) >= 0
+    signed = bool(int(o["zo"]) or int(o["zg"]))
+    body = [f"const ROp<R>& r = rops[{k_rel}];"]
+    if signed:
+        body.append("const R sg = rop_sign<R>(r, gbase, b);")
+    s = "sg * " if signed else ""
+    if has_grad:
+        gk, garg = _grad_code(o)
+        if gk == "pair":
+            g = f"g_pair<R, kNR, {garg}>(x, y, r.gph, r.gw0)"
+        elif gk == "diag":
+            g = f"g_diag<R, kNR, {garg}>(x, y, r.gph, r.gw0, r.gw1)"
+        else:
+            g = f"j_grad<R, {garg[0]}, {garg[1]}, {garg[2]}>(x, y, r.gph)"
+        body.append(f"const R part = {s}{g};")
+    for arr in ("x", "y"):
+        if routine == "u1":
+            body.append(f"r_u1<R, kNR, {arg}>({arr}, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y), "
+                        f"cplx<R>({s}r.m[2].x, {s}r.m[2].y), r.m[3]);")
+        elif routine == "rr":
+            body.append(f"r_rr<R, kNR, {arg}>({arr}, r.m[0].x, {s}r.m[1].x, {s}r.m[2].x);")
+        elif routine == "ri":
+            body.append(f"r_ri<R, kNR, {arg}>({arr}, r.m[0].x, {s}r.m[1].y, {s}r.m[2].y);")
+        elif routine == "d":
+            if signed:
+                body.append(f"r_d1<R, kNR, {arg}>({arr}, sg < R(0) ? r.m[1] : r.m[0], sg < R(0) ? r.m[0] : r.m[1]);")
+            else:
+                body.append(f"r_d1<R, kNR, {arg}>({arr}, r.m[0], r.m[1]);")
+        elif routine == "dh":
+            body.append(f"r_dh<R, kNR, {arg}>({arr}, r.m[1]);")
+        elif routine == "perm":
+            mode, a, b = arg
+            body.append(f"r_perm<R, kNR, {mode}, {a}, {b}>({arr});")
+        elif routine == "u2adj":
+            A, B = arg
+            body.append(f"j_u2_adj<R, {A}, {B}>({arr}, ops[r.op]);")
+        elif routine == "prot":
+            xm, zm, cm = arg
+            body.append(f"j_prot<R, {xm}, {zm}, {cm}>({arr}, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y));")
+    if has_grad:
+        body.append(f"j_part<R>(part, wpart, {k_rel}, nwarps, warp, lane);")
+    lines.append("    { " + " ".join(body) + " }")
+
+
+def _adj_body(stages: np.ndarray, ops: np.ndarray, p, double: bool, max_ops: int) -> list[str] | None:
+    """Body lines of one adjoint pass (4-bit stages), or None (library kernel)."""
+    sb, se = int(p[2]), int(p[3])
+    if se <= sb:
+        return None
+    op0 = int(stages[sb]["op_begin"])
+    nops = int(stages[se - 1]["op_end"]) - op0
+    if nops <= 0 or nops > max_ops:
+        return None
+    lines = []
+    for si in range(sb, se):
+        st = stages[si]
+        bits = [int(v) for v in st["bits"]]
+        if any(v < 0 for v in bits) or sorted(bits) != bits:
+            return None
+        lines.append(f"  {{  // stage bits {bits}")
+        lines.append("    int b = tid;")
+        for bb in bits:
+            lines.append("    " + _insz("b", bb))
+        lines.append("    const int p0 = b + ((b >> 4) << 1);")
+        offs = []
+        for i in range(16):
+            j = 0
+            for k in range(4):
+                if (i >> k) & 1:
+                    j |= 1 << bits[k]
+            offs.append(_pphys(j))
+        lines.append("    " + " ".join(f"x[{i}] = sp[p0 + {offs[i]}]; y[{i}] = sl[p0 + {offs[i]}];"
+                                       for i in range(16)))
+        for k in range(int(st["op_begin"]), int(st["op_end"])):
+            _emit_adj_op(lines, k - op0, ops[k], double)
+        lines.append("    " + " ".join(f"sp[p0 + {offs[i]}] = x[{i}]; sl[p0 + {offs[i]}] = y[{i}];"
+                                       for i in range(16)))
+        lines.append("    __syncthreads();")
+        lines.append("  }")
+    return lines
+
+
+WAVE_FWD_KERNEL = "tq_jit_wave_forward"
+WAVE_ADJ_KERNEL = "tq_jit_wave_adjoint"
+
+
+def wave_source(kind: int, t: int, body: str, double: bool) -> str:
+    """Source of one wave kernel: kind 0 forward (body over s), 2 adjoint
+    (body over sp, sl)."""
+    R = "double" if double else "float"
+    threads = 1 << (t - 4)
+    head = ['#include "jit_wave.cuh"', "", "namespace tq {", "template <typename R>"]
+    if kind == 0:
+        head.append("__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ s, const ROp<R>* __restrict__ rops, "
+                    "const tq_tile_op* __restrict__ ops, uint64_t gbase) {")
+        head += ["  const int tid = threadIdx.x;", "  cplx<R> x[kNR];"]
+    else:
+        head.append("__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ sp, cplx<R>* __restrict__ sl, "
+                    "const ROp<R>* __restrict__ rops, const tq_tile_op* __restrict__ ops, R* __restrict__ wpart, "
+                    "uint64_t gbase, int nwarps, int warp, int lane) {")
+        head += ["  const int tid = threadIdx.x;", "  cplx<R> x[kNR], y[kNR];"]
+    src = head + [body, "}", "}  // namespace tq", ""]
+    common = ("const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes, "
+              "const tq_tile_stage* __restrict__ stages, const tq_tile_op* __restrict__ ops, "
+              "const double* __restrict__ theta, void* pool")
+    if kind == 0:
+        src.append(f'extern "C" __global__ void __launch_bounds__({threads}) {WAVE_FWD_KERNEL}({common}, int max_ops) {{')
+        src.append(f"  tq::jit_wave_forward<{R}>(items, n_items, passes, stages, ops, theta, pool, max_ops, "
+                   f"[&](tq::cplx<{R}>* s, const tq::ROp<{R}>* rops, uint64_t gbase) "
+                   f"{{ tq::jit_body<{R}>(s, rops, ops, gbase); }});")
+    else:
+        minb = 2 if threads <= 256 else 1
+        src.append(f'extern "C" __global__ void __launch_bounds__({threads}, {minb}) {WAVE_ADJ_KERNEL}({common}, '
+                   "double* partials, int max_ops) {")
+        src.append(f"  tq::jit_wave_adjoint<{R}>(items, n_items, passes, stages, ops, theta, pool, partials, max_ops, "
+                   f"[&](tq::cplx<{R}>* sp, tq::cplx<{R}>* sl, const tq::ROp<{R}>* rops, {R}* wpart, uint64_t gbase, "
+                   f"int nwarps, int warp, int lane) "
+                   f"{{ tq::jit_body<{R}>(sp, sl, rops, ops, wpart, gbase, nwarps, warp, lane); }});")
+    src.append("}")
+    return "\n".join(src) + "\n"
+
+
+def wave_kernels(kind: int, t: int, stages: np.ndarray, ops: np.ndarray, pass_rows: dict, double: bool,
+                 max_ops: int, device) -> dict:
+    """{pass id: kernel handle} for the given wave passes (pass id -> (t, nlow,
+    op_begin, op_end, pos) rows); passes without a body are left out."""
+    srcs = {}
+    for pid, row in pass_rows.items():
+        if kind == 0:
+            class _P:
+                pass
+            pp = _P()
+            pp.op_begin, pp.op_end, pp.t = row[2], row[3], row[0]
+            lines = _pass_body(stages, ops, pp, double)
+            if lines is not None:
+                nops = int(stages[row[3] - 1]["op_end"]) - int(stages[row[2]]["op_begin"])
+                if nops > max_ops:
+                    lines = None
+        else:
+            lines = _adj_body(stages, ops, row, double, max_ops)
+        if lines is not None:
+            srcs[pid] = wave_source(kind, t, "\n".join(lines), double)
+    uniq = list(dict.fromkeys(srcs.values()))
+    handles = dict(zip(uniq, kernels_for(uniq, device, names=[WAVE_FWD_KERNEL if kind == 0 else WAVE_ADJ_KERNEL]
+                                         * len(uniq))))
+    return {pid: handles[src] for pid, src in srcs.items()}
+
+
 @dataclass
 class JitStaged:
     """Specialised kernels of one staged segment: per pass a kernel handle
@@ -273,9 +439,11 @@ def _build_cubin(source: str) -> bytes:
         lib.tq_jit_free_host(out)
 
 
-def kernels_for(sources: list[str], device) -> list[int]:
+def kernels_for(sources: list[str], device, names: list[str] | None = None) -> list[int]:
     """Kernel handles for the given sources on `device` (built in parallel,
-    cubins cached on disk by source and header digest)."""
+    cubins cached on disk by source and header digest); names: the kernel of
+    each source (default the staged pass kernel)."""
+    names = names or [KERNEL_NAME] * len(sources)
     dev = torch.device(device)
     digest = _headers_digest()
     keys = [hashlib.sha256((digest + "\0" + src).encode()).hexdigest() for src in sources]
@@ -307,7 +475,7 @@ def kernels_for(sources: list[str], device) -> list[int]:
                 continue
             h = ctypes.c_void_p()
             blob = blobs[i]
-            nat.check(lib.tq_jit_load(blob, len(blob), KERNEL_NAME.encode(), ctypes.byref(h)))
+            nat.check(lib.tq_jit_load(blob, len(blob), names[i].encode(), ctypes.byref(h)))
             _kernels[(keys[i], dev.index)] = h.value
         return [_kernels[(k, dev.index)] for k in keys]
 

@@ -57,7 +57,7 @@ def _dev(arr: np.ndarray, device) -> torch.Tensor:
 
 class WavePlan:
     def __init__(self, entries, dtype, device, t: int = 12, hbits: int = 12, budget: int = 48 << 20,
-                 max_ops: int = 256, lanes: int = 1, adj_stage_bits: int = 4):
+                 max_ops: int = 256, lanes: int = 1, adj_stage_bits: int = 4, jit: bool = False):
         """entries: list of dicts with keys idx (instance index), n, gates,
         params, key (structure key), theta_off, grad_offset, basis,
         group_begin, group_count.  Waves are dealt round-robin to `lanes`
@@ -167,6 +167,11 @@ class WavePlan:
             self.launch_lanes += [lane] * (len(launches) - n_launch0)
         self.launches = launches
         self.n_items = len(items)
+        # circuit-specialised kernels: one per distinct pass body; the items of each
+        # forward / adjoint launch are grouped by body, one sub-launch per group
+        self.jit_sub: dict = {}
+        if jit and items:
+            self._specialise(items, device)
         pool_base = np.concatenate([[0], np.cumsum(lane_pool)]).astype(np.int64)
         part_base = np.concatenate([[0], np.cumsum(lane_part)]).astype(np.int64)
         pool_need, part_need = int(pool_base[-1]), int(part_base[-1])
@@ -197,6 +202,41 @@ class WavePlan:
         self.pool = torch.empty(max(pool_need, 2), dtype=dtype, device=device)
         self.partials = torch.zeros(max(part_need, 1), dtype=torch.float64, device=device)
         self.pool_bytes = self.pool.numel() * S
+
+    def _specialise(self, items: list, device) -> None:
+        from . import jit as J
+
+        st = np.concatenate(self.stages) if self.stages else np.zeros(0, STAGE_DTYPE)
+        ops = np.concatenate(self.ops) if self.ops else np.zeros(0, TILE_OP_DTYPE)
+        double = self.dt == 1
+        used = {0: {}, 2: {}}
+        for L in self.launches:
+            if L[0] == "run" and L[1] in (0, 2) and L[3] > 0:
+                for row in items[L[2]:L[2] + L[3]]:
+                    used[L[1]][row[2]] = self.passes[row[2]]
+        kern = {0: J.wave_kernels(0, self.t, st, ops, used[0], double, self.fwd_max_ops, device)}
+        if self.adj_rb == 4:
+            kern[2] = J.wave_kernels(2, self.t, st, ops, used[2], double, self.adj_max_ops, device)
+        else:
+            kern[2] = {}
+        self.jit_kernels = kern
+        for li, L in enumerate(self.launches):
+            if L[0] != "run" or L[1] not in (0, 2) or L[3] == 0:
+                continue
+            kind, b, c = L[1], L[2], L[3]
+            block = items[b:b + c]
+            key = [kern[kind].get(row[2], 0) for row in block]
+            order = sorted(range(c), key=lambda i: key[i])
+            items[b:b + c] = [block[i] for i in order]
+            subs, i = [], 0
+            while i < c:
+                j = i
+                while j < c and key[order[j]] == key[order[i]]:
+                    j += 1
+                subs.append((b + i, j - i, key[order[i]]))
+                i = j
+            self.jit_sub[li] = subs
+        self.jit_bodies = len({h for d in kern.values() for h in d.values()})
 
     # ------------------------------------------------------------ encoding
     def _add_staged(self, enc) -> list[int]:
@@ -258,13 +298,28 @@ class WavePlan:
         gradient reductions)."""
         P = ctypes.c_void_p
         isz = WAVE_ITEM_DTYPE.itemsize
-        for L, lane in zip(self.launches, self.launch_lanes):
+        for li, (L, lane) in enumerate(zip(self.launches, self.launch_lanes)):
             if lane_streams is not None:
                 stream = lane_streams[lane]
             phase = L[1] if L[0] == "run" else (1 if L[0] == "reduce_e" else 2)
             if phase not in kinds:
                 continue
-            if L[0] == "run":
+            if L[0] == "run" and li in self.jit_sub:
+                kind = L[1]
+                for b0, c0, k in self.jit_sub[li]:
+                    if k:
+                        nat.call("tq_jit_wave_run", P(k), kind, self.dt, P(self.items_dev.data_ptr() + isz * b0), c0,
+                                 self.t, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
+                                 P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.pool.data_ptr()),
+                                 P(self.partials.data_ptr()), self.fwd_max_ops if kind == 0 else self.adj_max_ops,
+                                 stream)
+                    else:
+                        nat.call("tq_wave_run", kind, self.dt, P(self.items_dev.data_ptr() + isz * b0), c0, self.t,
+                                 self.hbits, self.adj_rb if kind == 2 else 4, P(self.passes_dev.data_ptr()),
+                                 P(self.stages_dev.data_ptr()), P(self.ops_dev.data_ptr()), None, None,
+                                 P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()),
+                                 self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
+            elif L[0] == "run":
                 _, kind, b, c = L
                 if c == 0:
                     continue
