@@ -145,3 +145,29 @@ def test_plain_engine_graph_replay_matches_oracle():
             e_ref, g_ref = _oracle(inst)
             assert abs(e - e_ref) < 1e-10
             np.testing.assert_allclose(g, g_ref, atol=1e-10)
+
+
+@pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
+def test_specialised_wave_kernels_match_interpreter_and_oracle(dtype):
+    """Wave passes through the circuit-specialised kernels against the library's
+    interpreting wave kernels and the oracle (14-16 qubits: every instance in waves)."""
+    from dataclasses import replace
+
+    from tyxonq_gb300.batch import BatchedVQE, Schedule
+
+    insts = _instances(10, 41, (14, 16), depth_range=(1, 4), terms_range=(20, 80))
+    theta = np.concatenate([i.theta for i in insts])
+    base = Schedule.builtin(dtype)
+    res = {}
+    for jit in (1, 0):
+        bv = BatchedVQE(insts, dtype=dtype, schedule=replace(base, wave_jit=jit))
+        assert bv.waves is not None and (len(bv.waves.jit_sub) > 0) == bool(jit)
+        e, g = bv.run(theta)
+        res[jit] = (e.cpu().numpy().copy(), bv.split_grads(g.cpu().numpy()))
+    tol_e = 1e-10 if dtype == torch.complex128 else 1e-5
+    tol_g = 1e-10 if dtype == torch.complex128 else 1e-4
+    for k, inst in enumerate(insts):
+        e_ref, g_ref = _oracle(inst)
+        for jit in (1, 0):
+            assert abs(res[jit][0][k] - e_ref) < tol_e, (jit, k)
+            np.testing.assert_allclose(res[jit][1][k], g_ref, atol=tol_g)
