@@ -295,13 +295,14 @@ TQ_API int tq_jit_unload(void* kernel);
 TQ_API size_t tq_jit_rops_bytes(int dtype, int n_ops);
 
 /* Staged forward passes with specialised kernels: pass p runs kernels[p]
- * (a tq_jit_load handle), or the library's interpreting kernel where
- * kernels[p] is NULL.  Tables as tq_sv_run_staged (ops holds n_ops records;
+ * (a tq_jit_load handle; CTAs of 2^(t - stage_bits) threads, stage_bits 4 or
+ * 5), or the library's interpreting kernel where kernels[p] is NULL (4-bit
+ * stages only).  Tables as tq_sv_run_staged (ops holds n_ops records;
  * stages_host is a host copy of `stages`, for launch sizes); at most 256 ops
  * per specialised pass; ws: tq_jit_rops_bytes(dtype, n_ops) bytes, 16-byte
  * aligned. */
-TQ_API int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dtype, const tq_tile_pass* passes,
-                             int n_passes, const tq_tile_stage* stages_host, const tq_tile_stage* stages,
+TQ_API int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi, int n, int dtype,
+                             const tq_tile_pass* passes, int n_passes, const tq_tile_stage* stages_host, const tq_tile_stage* stages,
                              const tq_tile_op* ops, int n_ops, const double* theta, void* ws, size_t ws_bytes,
                              void* stream);
 

@@ -50,14 +50,17 @@ def test_specialised_passes_match_oracle_and_interpreter(n, dtype):
     ops = _extended_ops(n, 16, seed=n)
     gates, _ = lower_ops(_C(n, ops), mode="state")
     ref = csv.run_ops(n, ops, allowed=sv.STATE_OPS)
+    tol = 1e-12 if dtype == C128 else 2e-6 * math.sqrt(len(ops))
     prog = compile_forward(gates, n, dtype)
     a = prog.run(K.init_statevector(n, dtype=dtype)).cpu().numpy()
-    assert prog.specialise(dtype) == prog.n_passes > 0
-    b = prog.run(K.init_statevector(n, dtype=dtype)).cpu().numpy()
-    tol = 1e-12 if dtype == C128 else 2e-6 * math.sqrt(len(ops))
     np.testing.assert_allclose(a, ref, atol=tol, rtol=0)
-    np.testing.assert_allclose(b, ref, atol=tol, rtol=0)
-    np.testing.assert_allclose(b, a, atol=tol, rtol=0)
+    for bits in (4, 5):  # 4-bit stages (the library kernel's layout) and 5-bit stages
+        prog = compile_forward(gates, n, dtype)
+        assert prog.specialise(dtype, stage_bits=bits) == prog.n_passes > 0
+        assert {obj.rb for kind, obj in prog.segments if kind == "staged"} == {bits}
+        b = prog.run(K.init_statevector(n, dtype=dtype)).cpu().numpy()
+        np.testing.assert_allclose(b, ref, atol=tol, rtol=0, err_msg=f"{bits}-bit stages")
+        np.testing.assert_allclose(b, a, atol=tol, rtol=0)
 
 
 def _prot_oracle(psi, n, pauli, a):

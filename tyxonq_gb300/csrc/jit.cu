@@ -139,7 +139,8 @@ extern "C" int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass*
                                 const tq_tile_stage* stages, const tq_tile_op* ops, const double* theta,
                                 void* stream);
 
-extern "C" int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dtype, const tq_tile_pass* passes,
+extern "C" int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi, int n, int dtype,
+                                 const tq_tile_pass* passes,
                                  int n_passes, const tq_tile_stage* stages_host, const tq_tile_stage* stages,
                                  const tq_tile_op* ops, int n_ops, const double* theta, void* ws, size_t ws_bytes,
                                  void* stream) {
@@ -149,6 +150,8 @@ extern "C" int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dty
   if (!kernels || !passes || !stages_host || !stages || !ops || !psi)
     return fail(TQ_ERR_ARG, "tq_jit_run_staged: NULL argument");
   if (n_ops <= 0) return fail(TQ_ERR_ARG, "tq_jit_run_staged: empty op table");
+  if (stage_bits != 4 && stage_bits != 5)
+    return fail(TQ_ERR_ARG, "tq_jit_run_staged: %d register bits per stage (4 or 5)", stage_bits);
   const size_t need = tq_jit_rops_bytes(dtype, n_ops);
   if (!ws || ws_bytes < need)
     return fail(TQ_ERR_WORKSPACE, "tq_jit_run_staged: workspace of %zu bytes, %zu needed", ws_bytes, need);
@@ -156,8 +159,13 @@ extern "C" int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dty
   const int tmax = dtype == TQ_C64 ? 13 : 12;
   for (int p = 0; p < n_passes; ++p) {
     const tq_tile_pass& tp = passes[p];
-    if (tp.op_end == tp.op_begin || !kernels[p]) continue;
-    if (tp.t < 9 || tp.t > tmax || tp.t > n || tp.nlow < 1 || tp.nlow > tp.t)
+    if (tp.op_end == tp.op_begin) continue;
+    if (!kernels[p]) {
+      if (stage_bits != 4)
+        return fail(TQ_ERR_ARG, "tq_jit_run_staged: pass %d has no kernel and %d-bit stages", p, stage_bits);
+      continue;
+    }
+    if (tp.t < 9 || tp.t > tmax || tp.t > n || tp.nlow < 1 || tp.nlow > tp.t || tp.t - stage_bits < 5)
       return fail(TQ_ERR_ARG, "tq_jit_run_staged: pass %d has t=%d nlow=%d (n=%d)", p, tp.t, tp.nlow, n);
     const int op0 = stages_host[tp.op_begin].op_begin, op1 = stages_host[tp.op_end - 1].op_end;
     if (op0 < 0 || op1 > n_ops || op1 - op0 <= 0 || op1 - op0 > kStagedRopCap)
@@ -188,7 +196,7 @@ extern "C" int tq_jit_run_staged(void* const* kernels, void* psi, int n, int dty
     P.op_end = tp.op_end;
     for (int i = 0; i < TQ_TILE_MAX_BITS; ++i) P.pos[i] = tp.pos[i];
     const int nops = stages_host[tp.op_end - 1].op_end - stages_host[tp.op_begin].op_begin;
-    const int threads = 1 << (tp.t - kRB);
+    const int threads = 1 << (tp.t - stage_bits);
     const int64_t ntiles = int64_t(1) << (n - tp.t);
     cudaKernel_t k = static_cast<JitKernel*>(kernels[p])->kernel;
     // occupancy with double buffering sets the grid; one buffer when every CTA owns one tile

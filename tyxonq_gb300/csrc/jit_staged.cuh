@@ -18,14 +18,15 @@
 
 namespace tq {
 
-// In-place dense 4x4 on register bits (A = matrix high bit, B = low bit).
-template <typename R, int A, int B>
+// In-place dense 4x4 on register bits (A = matrix high bit, B = low bit) of
+// NR registers.
+template <typename R, int NR, int A, int B>
 __device__ __forceinline__ void j_u2(cplx<R>* x, const tq_tile_op& o) {
   cplx<R> u[16];
 #pragma unroll
   for (int e = 0; e < 16; ++e) u[e] = op_m<R>(o, e);
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if (((i >> A) & 1) || ((i >> B) & 1)) continue;
     const int id[4] = {i, i | (1 << B), i | (1 << A), i | (1 << A) | (1 << B)};
     const cplx<R> v[4] = {x[id[0]], x[id[1]], x[id[2]], x[id[3]]};
@@ -43,19 +44,19 @@ __device__ __forceinline__ void j_u2(cplx<R>* x, const tq_tile_op& o) {
 // In-place Pauli rotation exp(-i a/2 P) on register bits: X/Y bits XM, Z/Y bits
 // ZM, control bits CM (all compile-time), coefficients c = m0 (real part used,
 // as the library's t_prot) and w = sign * m1.
-template <typename R, int XM, int ZM, int CM>
+template <typename R, int NR, int XM, int ZM, int CM>
 __device__ __forceinline__ void j_prot(cplx<R>* x, cplx<R> c, cplx<R> w) {
   if constexpr (XM == 0) {
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) {
+    for (int i = 0; i < NR; ++i) {
       if ((i & CM) != CM) continue;
       const R sg = (__popc(i & ZM) & 1) ? R(-1) : R(1);
       x[i] = cmul(cplx<R>(c.x + sg * w.x, sg * w.y), x[i]);
     }
   } else {
-    constexpr int H = (XM & 8) ? 3 : (XM & 4) ? 2 : (XM & 2) ? 1 : 0;
+    constexpr int H = (XM & 16) ? 4 : (XM & 8) ? 3 : (XM & 4) ? 2 : (XM & 2) ? 1 : 0;
 #pragma unroll
-    for (int i = 0; i < kNR; ++i) {
+    for (int i = 0; i < NR; ++i) {
       if ((i >> H) & 1) continue;
       if ((i & CM) != CM) continue;
       const int j = i ^ XM;
@@ -66,19 +67,6 @@ __device__ __forceinline__ void j_prot(cplx<R>* x, cplx<R> c, cplx<R> w) {
       x[j] = cfma(cplx<R>(w.x * si, w.y * si), a, cplx<R>(c.x * b.x, c.x * b.y));
     }
   }
-}
-
-// Load / store the 16 registers of a stage: off[i] = padded offset of register
-// pattern i (compile-time), p0 = padded address of the thread's base index.
-template <typename R>
-__device__ __forceinline__ void j_load(cplx<R>* x, const cplx<R>* s, int p0, const int (&off)[kNR]) {
-#pragma unroll
-  for (int i = 0; i < kNR; ++i) x[i] = s[p0 + off[i]];
-}
-template <typename R>
-__device__ __forceinline__ void j_store(const cplx<R>* x, cplx<R>* s, int p0, const int (&off)[kNR]) {
-#pragma unroll
-  for (int i = 0; i < kNR; ++i) s[p0 + off[i]] = x[i];
 }
 
 // The tile loop of one forward pass (same memory schedule as k_staged_forward:

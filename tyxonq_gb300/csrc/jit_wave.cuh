@@ -16,7 +16,7 @@
 namespace tq {
 
 // In-place adjoint of a dense 4x4 on register bits (A high, B low): U^dagger.
-template <typename R, int A, int B>
+template <typename R, int NR, int A, int B>
 __device__ __forceinline__ void j_u2_adj(cplx<R>* x, const tq_tile_op& o) {
   cplx<R> u[16];
 #pragma unroll
@@ -27,7 +27,7 @@ __device__ __forceinline__ void j_u2_adj(cplx<R>* x, const tq_tile_op& o) {
       u[4 * r + c] = cplx<R>(v.x, -v.y);
     }
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if (((i >> A) & 1) || ((i >> B) & 1)) continue;
     const int id[4] = {i, i | (1 << B), i | (1 << A), i | (1 << A) | (1 << B)};
     const cplx<R> v[4] = {x[id[0]], x[id[1]], x[id[2]], x[id[3]]};
@@ -46,11 +46,11 @@ __device__ __forceinline__ void j_u2_adj(cplx<R>* x, const tq_tile_op& o) {
 // Im <y|G|x> over the thread's registers for a general generator
 // G|i> = [i & CM == CM] ph (-1)^{popc(i & ZM)} |i ^ XM> (register bits; the
 // caller applies the sign of Z factors outside the registers).
-template <typename R, int XM, int ZM, int CM>
+template <typename R, int NR, int XM, int ZM, int CM>
 __device__ __forceinline__ R j_grad(const cplx<R>* x, const cplx<R>* y, cplx<R> ph) {
   R acc = 0;
 #pragma unroll
-  for (int i = 0; i < kNR; ++i) {
+  for (int i = 0; i < NR; ++i) {
     if ((i & CM) != CM) continue;
     const R sg = (__popc(i & ZM) & 1) ? R(-1) : R(1);
     const cplx<R> v = cmul(ph, x[i]);

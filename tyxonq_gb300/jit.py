@@ -61,9 +61,9 @@ def _mat(o, e: int, double: bool) -> complex:
 
 def _op_code(o, double: bool) -> tuple:
     """(routine, args) the device compiles op record o into (rop_build, forward,
-    not fused); routine None = no-op."""
+    not fused); routine None = no-op.  Register bits as encoded (0..rb-1)."""
     kind = int(o["kind"])
-    a, b = int(o["a"]) & 3, int(o["b"]) & 3
+    a, b = int(o["a"]), int(o["b"])
     if kind == TOP_U1:
         return "u1", a
     if kind == TOP_D1:
@@ -103,7 +103,7 @@ def _single_bit(o) -> int | None:
         return None
     kind = int(o["kind"])
     if kind in (TOP_U1, TOP_D1):
-        return int(o["a"]) & 3
+        return int(o["a"])
     if kind == TOP_PROT:
         xm, zm, cm = int(o["xm"]) & 15, int(o["zm"]) & 15, int(o["cm"]) & 15
         if cm:
@@ -120,37 +120,40 @@ def _emit_op(lines: list, k_rel: int, o, routine: str, arg, signed: bool) -> Non
     s = "sg * " if signed else ""
     pre = f"const ROp<R>& r = {r}; " + ("const R sg = rop_sign<R>(r, gbase, b); " if signed else "")
     if routine == "u1":
-        call = (f"r_u1<R, kNR, {arg}>(x, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y), "
+        call = (f"r_u1<R, NR, {arg}>(x, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y), "
                 f"cplx<R>({s}r.m[2].x, {s}r.m[2].y), r.m[3]);")
     elif routine == "rr":
-        call = f"r_rr<R, kNR, {arg}>(x, r.m[0].x, {s}r.m[1].x, {s}r.m[2].x);"
+        call = f"r_rr<R, NR, {arg}>(x, r.m[0].x, {s}r.m[1].x, {s}r.m[2].x);"
     elif routine == "ri":
-        call = f"r_ri<R, kNR, {arg}>(x, r.m[0].x, {s}r.m[1].y, {s}r.m[2].y);"
+        call = f"r_ri<R, NR, {arg}>(x, r.m[0].x, {s}r.m[1].y, {s}r.m[2].y);"
     elif routine == "d":
         if signed:
-            call = f"r_d1<R, kNR, {arg}>(x, sg < R(0) ? r.m[1] : r.m[0], sg < R(0) ? r.m[0] : r.m[1]);"
+            call = f"r_d1<R, NR, {arg}>(x, sg < R(0) ? r.m[1] : r.m[0], sg < R(0) ? r.m[0] : r.m[1]);"
         else:
-            call = f"r_d1<R, kNR, {arg}>(x, r.m[0], r.m[1]);"
+            call = f"r_d1<R, NR, {arg}>(x, r.m[0], r.m[1]);"
     elif routine == "dh":
-        call = f"r_dh<R, kNR, {arg}>(x, r.m[1]);"
+        call = f"r_dh<R, NR, {arg}>(x, r.m[1]);"
     elif routine == "perm":
         mode, a, b = arg
-        call = f"r_perm<R, kNR, {mode}, {a}, {b}>(x);"
+        call = f"r_perm<R, NR, {mode}, {a}, {b}>(x);"
         pre = ""
     elif routine == "u2":
         A, B = arg
-        call = f"j_u2<R, {A}, {B}>(x, ops[r.op]);"
+        call = f"j_u2<R, NR, {A}, {B}>(x, ops[r.op]);"
     elif routine == "prot":
         xm, zm, cm = arg
-        call = f"j_prot<R, {xm}, {zm}, {cm}>(x, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y));"
+        call = f"j_prot<R, NR, {xm}, {zm}, {cm}>(x, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y));"
     else:
         return
     lines.append(f"    {{ {pre}{call} }}")
 
 
-def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool) -> list[str] | None:
-    """Body lines of one pass (stages[p.op_begin:p.op_end]), or None if the
+def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool, stage_bits: list | None = None,
+               rb: int = 4) -> list[str] | None:
+    """Body lines of one pass (stages[p.op_begin:p.op_end]) with rb-bit register
+    stages (stage_bits: every stage's bits, needed for rb > 4), or None if the
     interpreter must run it."""
+    NR = 1 << rb
     sb, se = int(p.op_begin), int(p.op_end)
     if se <= sb:
         return None
@@ -161,8 +164,8 @@ def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool) -> list[str
     lines = []
     for si in range(sb, se):
         st = stages[si]
-        bits = [int(v) for v in st["bits"]]
-        if any(v < 0 for v in bits) or sorted(bits) != bits:
+        bits = [int(v) for v in (stage_bits[si] if stage_bits is not None else st["bits"])]
+        if len(bits) != rb or any(v < 0 for v in bits) or sorted(bits) != bits:
             return None
         lines.append(f"  {{  // stage bits {bits}")
         lines.append("    int b = tid;")
@@ -170,13 +173,13 @@ def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool) -> list[str
             lines.append("    " + _insz("b", bb))
         lines.append("    const int p0 = b + ((b >> 4) << 1);")
         offs = []
-        for i in range(16):
+        for i in range(NR):
             j = 0
-            for k in range(4):
+            for k in range(rb):
                 if (i >> k) & 1:
                     j |= 1 << bits[k]
             offs.append(_pphys(j))
-        lines.append("    " + " ".join(f"x[{i}] = s[p0 + {offs[i]}];" for i in range(16)))
+        lines.append("    " + " ".join(f"x[{i}] = s[p0 + {offs[i]}];" for i in range(NR)))
         k, k1 = int(st["op_begin"]), int(st["op_end"])
         while k < k1:
             o = ops[k]
@@ -193,7 +196,7 @@ def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool) -> list[str
             signed = bool(int(o["zo"]) or int(o["zg"]))
             _emit_op(lines, k - op0, o, routine, arg, signed)
             k += 1
-        lines.append("    " + " ".join(f"s[p0 + {offs[i]}] = x[{i}];" for i in range(16)))
+        lines.append("    " + " ".join(f"s[p0 + {offs[i]}] = x[{i}];" for i in range(NR)))
         lines.append("    __syncthreads();")
         lines.append("  }")
     return lines
@@ -226,36 +229,36 @@ def _emit_adj_op(lines: list, k_rel: int, o, double: bool) -> None:
     if has_grad:
         gk, garg = _grad_code(o)
         if gk == "pair":
-            g = f"g_pair<R, kNR, {garg}>(x, y, r.gph, r.gw0)"
+            g = f"g_pair<R, NR, {garg}>(x, y, r.gph, r.gw0)"
         elif gk == "diag":
-            g = f"g_diag<R, kNR, {garg}>(x, y, r.gph, r.gw0, r.gw1)"
+            g = f"g_diag<R, NR, {garg}>(x, y, r.gph, r.gw0, r.gw1)"
         else:
-            g = f"j_grad<R, {garg[0]}, {garg[1]}, {garg[2]}>(x, y, r.gph)"
+            g = f"j_grad<R, NR, {garg[0]}, {garg[1]}, {garg[2]}>(x, y, r.gph)"
         body.append(f"const R part = {s}{g};")
     for arr in ("x", "y"):
         if routine == "u1":
-            body.append(f"r_u1<R, kNR, {arg}>({arr}, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y), "
+            body.append(f"r_u1<R, NR, {arg}>({arr}, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y), "
                         f"cplx<R>({s}r.m[2].x, {s}r.m[2].y), r.m[3]);")
         elif routine == "rr":
-            body.append(f"r_rr<R, kNR, {arg}>({arr}, r.m[0].x, {s}r.m[1].x, {s}r.m[2].x);")
+            body.append(f"r_rr<R, NR, {arg}>({arr}, r.m[0].x, {s}r.m[1].x, {s}r.m[2].x);")
         elif routine == "ri":
-            body.append(f"r_ri<R, kNR, {arg}>({arr}, r.m[0].x, {s}r.m[1].y, {s}r.m[2].y);")
+            body.append(f"r_ri<R, NR, {arg}>({arr}, r.m[0].x, {s}r.m[1].y, {s}r.m[2].y);")
         elif routine == "d":
             if signed:
-                body.append(f"r_d1<R, kNR, {arg}>({arr}, sg < R(0) ? r.m[1] : r.m[0], sg < R(0) ? r.m[0] : r.m[1]);")
+                body.append(f"r_d1<R, NR, {arg}>({arr}, sg < R(0) ? r.m[1] : r.m[0], sg < R(0) ? r.m[0] : r.m[1]);")
             else:
-                body.append(f"r_d1<R, kNR, {arg}>({arr}, r.m[0], r.m[1]);")
+                body.append(f"r_d1<R, NR, {arg}>({arr}, r.m[0], r.m[1]);")
         elif routine == "dh":
-            body.append(f"r_dh<R, kNR, {arg}>({arr}, r.m[1]);")
+            body.append(f"r_dh<R, NR, {arg}>({arr}, r.m[1]);")
         elif routine == "perm":
             mode, a, b = arg
-            body.append(f"r_perm<R, kNR, {mode}, {a}, {b}>({arr});")
+            body.append(f"r_perm<R, NR, {mode}, {a}, {b}>({arr});")
         elif routine == "u2adj":
             A, B = arg
-            body.append(f"j_u2_adj<R, {A}, {B}>({arr}, ops[r.op]);")
+            body.append(f"j_u2_adj<R, NR, {A}, {B}>({arr}, ops[r.op]);")
         elif routine == "prot":
             xm, zm, cm = arg
-            body.append(f"j_prot<R, {xm}, {zm}, {cm}>({arr}, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y));")
+            body.append(f"j_prot<R, NR, {xm}, {zm}, {cm}>({arr}, r.m[0], cplx<R>({s}r.m[1].x, {s}r.m[1].y));")
     if has_grad:
         body.append(f"j_part<R>(part, wpart, {k_rel}, nwarps, warp, lane);")
     lines.append("    { " + " ".join(body) + " }")
@@ -312,12 +315,12 @@ def wave_source(kind: int, t: int, body: str, double: bool) -> str:
     if kind == 0:
         head.append("__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ s, const ROp<R>* __restrict__ rops, "
                     "const tq_tile_op* __restrict__ ops, uint64_t gbase) {")
-        head += ["  const int tid = threadIdx.x;", "  cplx<R> x[kNR];"]
+        head += ["  const int tid = threadIdx.x;", "  constexpr int NR = 16;", "  cplx<R> x[NR];"]
     else:
         head.append("__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ sp, cplx<R>* __restrict__ sl, "
                     "const ROp<R>* __restrict__ rops, const tq_tile_op* __restrict__ ops, R* __restrict__ wpart, "
                     "uint64_t gbase, int nwarps, int warp, int lane) {")
-        head += ["  const int tid = threadIdx.x;", "  cplx<R> x[kNR], y[kNR];"]
+        head += ["  const int tid = threadIdx.x;", "  constexpr int NR = 16;", "  cplx<R> x[NR], y[NR];"]
     src = head + [body, "}", "}  // namespace tq", ""]
     common = ("const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes, "
               "const tq_tile_stage* __restrict__ stages, const tq_tile_op* __restrict__ ops, "
@@ -373,6 +376,7 @@ class JitStaged:
     kernels: ctypes.Array
     n_kernels: int
     ws: torch.Tensor | None = None
+    rb: int = 4
 
 
 _kernels: dict = {}  # (source hash, device) -> kernel handle
@@ -385,7 +389,7 @@ def cache_dir() -> Path:
     return Path(d) if d else Path.home() / ".cache" / "tyxonq_gb300" / "jit"
 
 
-def pass_source(t: int, body: str, double: bool) -> str:
+def pass_source(t: int, body: str, double: bool, rb: int = 4) -> str:
     R = "double" if double else "float"
     T2 = "double2" if double else "float2"
     return "\n".join([
@@ -396,12 +400,13 @@ def pass_source(t: int, body: str, double: bool) -> str:
         "__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ s, const ROp<R>* __restrict__ rops, "
         "const tq_tile_op* __restrict__ ops, uint64_t gbase) {",
         "  const int tid = threadIdx.x;",
-        "  cplx<R> x[kNR];",
+        f"  constexpr int NR = {1 << rb};",
+        "  cplx<R> x[NR];",
         body,
         "}",
         "}  // namespace tq",
         "",
-        f'extern "C" __global__ void __launch_bounds__({1 << (t - 4)}, 1) {KERNEL_NAME}({T2}* psi, int n, '
+        f'extern "C" __global__ void __launch_bounds__({1 << (t - rb)}, 1) {KERNEL_NAME}({T2}* psi, int n, '
         "const tq::PassArgs P, const tq_tile_stage* __restrict__ stages, "
         f"const tq_tile_op* __restrict__ ops, const tq::ROp<{R}>* __restrict__ rops_g, int dbuf) {{",
         f"  tq::jit_staged_forward<{R}>(psi, n, P, stages, rops_g, dbuf, "
@@ -482,27 +487,53 @@ def kernels_for(sources: list[str], device, names: list[str] | None = None) -> l
 
 def specialise(enc, dtype, device="cuda") -> JitStaged | None:
     """Specialised kernels for the passes of an EncodedStaged program; None
-    when no pass qualifies."""
+    when no pass qualifies (with stages wider than 4 bits: None unless every
+    pass qualifies, since the library kernel takes at most 4)."""
     double = dtype == torch.complex128
     tmax = 12 if double else 13
+    rb = int(getattr(enc, "rb", 4))
     srcs, where = [], []
     for pi in range(enc.n_passes):
         p = enc.passes[pi]
-        if not (9 <= int(p.t) <= tmax):
+        if not (9 <= int(p.t) <= tmax) or int(p.t) - rb < 5:
             continue
-        lines = _pass_body(enc.stages_host, enc.ops_host, p, double)
+        lines = _pass_body(enc.stages_host, enc.ops_host, p, double, enc.stage_bits, rb)
         if lines is None:
             continue
-        srcs.append(pass_source(int(p.t), "\n".join(lines), double))
+        srcs.append(pass_source(int(p.t), "\n".join(lines), double, rb))
         where.append(pi)
-    if not srcs:
+    if not srcs or (rb > 4 and len(srcs) < sum(1 for pi in range(enc.n_passes)
+                                               if enc.passes[pi].op_end > enc.passes[pi].op_begin)):
         return None
     uniq = list(dict.fromkeys(srcs))
     handles = dict(zip(uniq, kernels_for(uniq, device)))
     arr = (ctypes.c_void_p * max(enc.n_passes, 1))()
     for pi, src in zip(where, srcs):
         arr[pi] = handles[src]
-    return JitStaged(arr, len(where))
+    return JitStaged(arr, len(where), rb=rb)
+
+
+def specialise_wide(enc, dtype, device="cuda"):
+    """The segment re-encoded with 5-bit register stages and specialised kernels
+    for every pass, or None (an op the 5-bit records cannot express: Pauli
+    rotations with register masks above bit 3, or a pass without a kernel)."""
+    from .program import encode_staged
+
+    if enc.source is None:
+        return None
+    plans, gates, params, slots, n = enc.source
+    if slots is not None:
+        return None
+    wide = encode_staged(n, plans, gates, params=params, rb=5)
+    ops = wide.ops_host
+    prot = ops[ops["kind"] == TOP_PROT]
+    if len(prot) and int(((prot["xm"] | prot["zm"] | prot["cm"]) >= 16).sum()):
+        return None
+    js = specialise(wide, dtype, device)
+    if js is None:
+        return None
+    wide.jit = js
+    return wide
 
 
 def run_staged(js: JitStaged, enc, psi: torch.Tensor, n: int, dtag: int, theta_ptr, stream) -> None:
@@ -514,6 +545,6 @@ def run_staged(js: JitStaged, enc, psi: torch.Tensor, n: int, dtag: int, theta_p
     if js.ws is None or js.ws.numel() < need or js.ws.device != psi.device:
         js.ws = torch.empty(max(need, 16), dtype=torch.uint8, device=psi.device)
     P = ctypes.c_void_p
-    nat.call("tq_jit_run_staged", js.kernels, P(psi.data_ptr()), n, dtag, enc.passes, enc.n_passes,
+    nat.call("tq_jit_run_staged", js.kernels, js.rb, P(psi.data_ptr()), n, dtag, enc.passes, enc.n_passes,
              enc.stages_host.ctypes.data_as(P), P(st_d.data_ptr()), P(ops_d.data_ptr()), n_ops, theta_ptr,
              P(js.ws.data_ptr()), js.ws.numel(), stream)

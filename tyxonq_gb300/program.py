@@ -490,6 +490,8 @@ class ForwardProgram:
                 from . import jit
 
                 jit.run_staged(obj.jit, obj, psi, self.n, dt, th, K.stream_ptr(psi.device))
+            elif kind == "staged" and obj.rb > STAGE_BITS:  # pragma: no cover - never built without kernels
+                raise RuntimeError("a 5-bit staged segment needs its specialised kernels")
             elif kind == "staged":
                 st, ops = obj.device_tables(psi.device)
                 nat.call("tq_sv_run_staged", ctypes.c_void_p(psi.data_ptr()), self.n, dt, obj.passes, obj.n_passes,
@@ -501,17 +503,27 @@ class ForwardProgram:
                          ctypes.c_void_p(ops.data_ptr()), th, K.stream_ptr(psi.device))
         return psi
 
-    def specialise(self, dtype, device="cuda") -> int:
+    def specialise(self, dtype, device="cuda", stage_bits: int = 5) -> int:
         """Compile circuit-specialised kernels (runtime CUDA compilation, cached
         per structure) for every register-staged segment; returns the number of
-        passes that run them."""
+        passes that run them.  stage_bits=5: segments re-encoded with 5-bit
+        register stages (32 amplitudes per thread: fewer shared-memory sweeps
+        per pass) where every pass takes a specialised kernel; 4-bit stages
+        otherwise."""
         from . import jit
 
         count = 0
-        for kind, obj in self.segments:
-            if kind == "staged" and obj.jit is None:
+        for si, (kind, obj) in enumerate(self.segments):
+            if kind != "staged":
+                continue
+            if obj.jit is None and stage_bits == 5 and obj.rb == STAGE_BITS:
+                wide = jit.specialise_wide(obj, dtype, device)
+                if wide is not None:
+                    self.segments[si] = (kind, wide)
+                    obj = wide
+            if obj.jit is None and obj.rb == STAGE_BITS:
                 obj.jit = jit.specialise(obj, dtype, device)
-            if kind == "staged" and obj.jit is not None:
+            if obj.jit is not None:
                 count += obj.jit.n_kernels
         return count
 
@@ -620,6 +632,9 @@ class EncodedStaged:
     ops_host: np.ndarray
     _dev: tuple | None = None
     jit: object | None = None  # jit.JitStaged: circuit-specialised kernels for these passes
+    rb: int = STAGE_BITS  # register bits per stage
+    stage_bits: list | None = None  # every stage's register bits (host; the device table holds at most 4)
+    source: tuple | None = None  # (plans, gates, params, slots) it was encoded from
 
     def device_tables(self, device):
         if self._dev is None or self._dev[0].device != torch.device(device):
@@ -689,9 +704,14 @@ def encode_staged(n: int, plans: Sequence[PassPlan], gates: Sequence[Gate], para
         passes.append(p)
     st = np.zeros(len(stage_rows), dtype=STAGE_DTYPE)
     for i, (bits, b, e) in enumerate(stage_rows):
-        st[i] = (list(bits) + [-1] * (STAGE_BITS - len(bits)), b, e)
+        bl = list(bits)[:STAGE_BITS]
+        st[i] = (bl + [-1] * (STAGE_BITS - len(bl)), b, e)
     arr = (TilePass * max(len(passes), 1))(*passes)
-    return EncodedStaged(arr, len(passes), st, pack_ops(fields))
+    enc = EncodedStaged(arr, len(passes), st, pack_ops(fields))
+    enc.rb = rb
+    enc.stage_bits = [list(bits) for bits, _, _ in stage_rows]
+    enc.source = (list(plans), gates, params, slots, n)
+    return enc
 
 
 def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int | None = None,
