@@ -101,7 +101,9 @@ def test_circuit_expectation_known_answers_on_gpu(dtype, monkeypatch):
     e += sum(c.expectation((gate_z(), [i]), (gate_z(), [i + 1])) for i in range(n - 1))
     assert abs(e + 3.0) < tol
     # callables and two-qubit factors, as the reference accepts them
-    assert abs(bell.expectation((gate_x, [0]), (np.kron(gate_x(), gate_x()), [0, 1])) - 1.0) < tol
+    assert abs(bell.expectation((gate_x, [0]), (gate_x(), [1])) - 1.0) < tol
+    assert abs(bell.expectation((np.kron(gate_z(), gate_z()), [0, 1])) - 1.0) < tol
+    assert abs(bell.expectation((np.kron(gate_x(), gate_x()), [0, 1]), (gate_x, [1])) - 0.0) < tol  # <X_0> = 0
     with pytest.raises(NotImplementedError):
         bell.expectation((np.eye(8), [0, 1, 1]))
 

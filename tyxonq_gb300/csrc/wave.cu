@@ -66,6 +66,34 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
 }
 
 // ------------------------------------------------------------------ H psi
+// acc[k] += (-1)^popc(k & C) sw * pv[k] (IM: times i) for the one-term groups.
+template <typename R, int PER, int C, bool IM>
+__device__ __forceinline__ void hpsi_one_term_c(cplx<R>* acc, const cplx<R>* pv, R sw) {
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const R s = (__builtin_popcount(k & C) & 1) ? -sw : sw;
+    if (IM) {
+      acc[k].x = fma(-s, pv[k].y, acc[k].x);
+      acc[k].y = fma(s, pv[k].x, acc[k].y);
+    } else {
+      acc[k].x = fma(s, pv[k].x, acc[k].x);
+      acc[k].y = fma(s, pv[k].y, acc[k].y);
+    }
+  }
+}
+
+template <typename R, int PER, bool IM>
+__device__ __forceinline__ void hpsi_one_term(cplx<R>* acc, const cplx<R>* pv, R sw, int c) {
+  switch (c) {
+#define TQ_HC(C_) \
+  case C_: if constexpr (C_ < PER) hpsi_one_term_c<R, PER, C_, IM>(acc, pv, sw); break;
+    TQ_HC(0) TQ_HC(1) TQ_HC(2) TQ_HC(3) TQ_HC(4) TQ_HC(5) TQ_HC(6) TQ_HC(7)
+    TQ_HC(8) TQ_HC(9) TQ_HC(10) TQ_HC(11) TQ_HC(12) TQ_HC(13) TQ_HC(14) TQ_HC(15)
+#undef TQ_HC
+    default: break;
+  }
+}
+
 // Item = output tile of HN = 2^hb amplitudes (256 threads x PER).  The partner
 // of output i under a group with flip m is psi[i ^ m]: it lies in source tile
 // (tile ^ (m >> hb)) at offset (i ^ m) mod HN.  Groups are visited in the order
@@ -135,26 +163,17 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
         if (cnt == 1 && (w1.x == R(0) || w1.y == R(0))) {
           // one term (most groups of a random Pauli sum) with a real or imaginary
           // weight (c * i^ny for real c): each amplitude takes two FMAs with a
-          // signed weight.  A general complex weight takes the path below.
+          // signed weight.  The sign of amplitude k is (-1)^(p0 + popc(k & c)):
+          // p0 per thread, c = the term's Z/Y bits among the k bits (the same for
+          // every thread), so one uniform switch over c selects code whose
+          // per-k signs are constants.  A general complex weight takes the path below.
           const uint64_t zy = __ldg(&terms[first].zy);
-          const cplx<R> w = w1;
           const int p0 = __popcll(sbase & zy) & 1;
           const int c = (int)(zy >> 8) & (PER - 1);
-          if (w.y == R(0)) {
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-              const R sw = ((p0 ^ __popc(k & c)) & 1) ? -w.x : w.x;
-              acc[k].x = fma(sw, pv[k].x, acc[k].x);
-              acc[k].y = fma(sw, pv[k].y, acc[k].y);
-            }
-          } else {
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-              const R sw = ((p0 ^ __popc(k & c)) & 1) ? -w.y : w.y;
-              acc[k].x = fma(-sw, pv[k].y, acc[k].x);
-              acc[k].y = fma(sw, pv[k].x, acc[k].y);
-            }
-          }
+          if (w1.y == R(0))
+            hpsi_one_term<R, PER, false>(acc, pv, p0 ? -w1.x : w1.x, c);
+          else
+            hpsi_one_term<R, PER, true>(acc, pv, p0 ? -w1.y : w1.y, c);
           continue;
         }
 #pragma unroll
