@@ -399,7 +399,20 @@ typedef struct {
 TQ_API int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
                        int stage_bits, const tq_tile_pass* passes, const tq_tile_stage* stages,
                        const tq_tile_op* ops, const tq_pauli_group* groups, const tq_pauli_term* terms,
-                       const double* theta, void* pool, double* partials, int max_pass_ops, void* stream);
+                       const double* theta, void* pool, double* partials, double* norm_partials,
+                       int max_pass_ops, void* stream);
+
+/* Divide energies and gradients by <psi|psi> (summed in order from the H psi
+ * items' norm_partials of tq_wave_run kind 1): row r scales energies[inst[r]]
+ * by 1 / sum(norm_partials[first[r] .. first[r] + count[r])) and
+ * grads[goff[r] .. goff[r] + gcount[r]) likewise.  For exact unitary circuits
+ * <psi|psi> = 1 and nothing changes; for complex64 states it removes the norm
+ * drift of rounded rotation coefficients (E = <psi|H|psi> / <psi|psi>), the
+ * largest part of the complex64 energy error against the reference's
+ * complex128 dynamics.expectation (dynamics.py:117-126). */
+TQ_API int tq_wave_normalize(const double* norm_partials, const int32_t* first, const int32_t* count,
+                             const int32_t* inst, const int32_t* goff, const int32_t* gcount, int n_rows,
+                             double* energies, double* grads, void* stream);
 
 /* One launch of a wave phase (kind 0 forward, 2 adjoint with 4-bit stages)
  * with a circuit-specialised kernel (tq_jit_load of a wave source written by

@@ -81,3 +81,27 @@ def test_bench_workload_matches_oracle_at_full_size():
     for de, dg, i in rows:
         assert de < E_TOL, (i, insts[i].n, insts[i].depth, insts[i].H.n_terms, de)
         assert dg < G_TOL, (i, insts[i].n, insts[i].depth, insts[i].H.n_terms, dg)
+
+
+@pytest.mark.parametrize("n,depth,terms", [(22, 6, 800), (24, 4, 500), (26, 2, 200)])
+def test_serving_size_energies_match_c_oracle(n, depth, terms):
+    """Serving-size requests (HEA, complex64, one state through the session
+    estimator) against the C complex128 oracle: 1e-5 absolute on the energy."""
+    from oracle import csv
+    from tyxonq_gb300.serving import VqeRequest, default_estimator_factory
+    from tyxonq_gb300.hamiltonian import random_pauli_sum
+    from tyxonq_gb300.workloads import hea_rz_ops_params
+
+    rng = np.random.default_rng(n)
+    H = random_pauli_sum(n, terms, rng)
+    struct = hea_rz_ops_params(n, depth)
+    npar = 2 * n * depth
+    theta = rng.uniform(0, 2 * np.pi, npar)
+    req = VqeRequest("s", n, struct, npar, H, theta)
+    est = default_estimator_factory(req, torch.complex64, torch.device("cuda"))
+    e = est.energy(theta)
+    ops = [(nm, *qs) if p is None else (nm, *qs, float(theta[p])) for nm, qs, p in struct]
+    psi = csv.run_ops(n, ops)
+    e_ref = csv.pauli_expectation(psi, H.codes, H.coeffs)
+    print(f"\nn={n}: |dE| = {abs(e - e_ref):.3e}")
+    assert abs(e - e_ref) < E_TOL

@@ -107,7 +107,9 @@ SIGNATURES: dict[str, tuple] = {
     "tq_ci_energy_grad": (c_int, [c_int64, c_int64, c_int, _P, _P, c_int64, _P, c_int64, _P, _P, _P, _P, c_int, c_int,
                                   _P, _P, _P, c_size_t, _P]),
     "tq_batch_smem_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
-    "tq_wave_run": (c_int, [c_int, c_int, _P, c_int, c_int, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, _P, c_int, _P]),
+    "tq_wave_run": (c_int, [c_int, c_int, _P, c_int, c_int, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, c_int,
+                            _P]),
+    "tq_wave_normalize": (c_int, [_P, _P, _P, _P, _P, _P, c_int, _P, _P, _P]),
     "tq_wave_reduce": (c_int, [_P, _P, _P, _P, _P, _P, c_int, _P, c_int, _P]),
     "tq_batch_run": (c_int, [c_int, _P, _P, c_int, c_int, c_int, c_int, c_int, c_size_t, _P, _P, _P, _P, _P, _P,
                              _P, _P, _P, _P]),

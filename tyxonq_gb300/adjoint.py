@@ -273,7 +273,7 @@ class _StagedReverse:
             nat.call("tq_wave_run", 2, self.dt, P(self.items_dev.data_ptr() + isz * first), count, self.t, 12,
                      self.rb, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
                      P(self.ops_dev.data_ptr()), None, None, P(theta.data_ptr()), P(self.pool.data_ptr()),
-                     P(self.partials.data_ptr()), self.max_ops, st)
+                     P(self.partials.data_ptr()), None, self.max_ops, st)
         for b, c in self.layers:
             nat.call("tq_wave_reduce", P(self.partials.data_ptr()), P(self.r_first.data_ptr() + 4 * b),
                      P(self.r_count.data_ptr() + 4 * b), P(self.r_stride.data_ptr() + 4 * b),
@@ -352,23 +352,27 @@ class ParametricEstimator:
         return self.prog.forward.run(self.psi, self.theta)
 
     def energy_async(self, theta) -> torch.Tensor:
-        """Enqueue an energy evaluation on the current stream; returns a device scalar."""
+        """Enqueue an energy evaluation on the current stream; returns a device
+        scalar <psi|H|psi> / <psi|psi> (the circuit is unitary, so the division
+        only removes the norm drift of rounded complex64 rotations)."""
         psi = self._forward(theta)
-        return K.pauli_expectation(psi, self.H)
+        return K.pauli_expectation(psi, self.H) / K.norm2(psi)
 
     def energy_and_grad_async(self, theta) -> tuple[torch.Tensor, torch.Tensor]:
         """Enqueue energy + adjoint gradient; returns (device energy, device
-        slot values -- per-parameter gradients on the staged path)."""
+        slot values -- per-parameter gradients on the staged path), both divided
+        by <psi|psi> as in energy_async."""
         self._ensure_staged()
         psi = self._forward(theta)
         if self.lam is None:
             self.lam = torch.empty_like(self.psi)
         K.apply_pauli_sum(psi, self.H, out=self.lam)
-        e = K.inner_re(psi, self.lam)
+        q = K.norm2(psi)
+        e = K.inner_re(psi, self.lam) / q
         if self._staged is not None:
-            return e, self._staged.run(self.theta)
+            return e, self._staged.run(self.theta) / q
         sv = reverse_sweep(self.prog, psi, self.lam, self.theta)
-        return e, sv
+        return e, sv / q
 
     def grad_from_slots(self, slot_vals: np.ndarray) -> np.ndarray:
         if self._staged is not None:

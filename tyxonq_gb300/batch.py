@@ -184,7 +184,7 @@ class BatchedVQE:
                 wave_entries.append({"idx": i, "n": n, "gates": gates, "params": params, "key": (n, skey),
                                      "theta_offset": theta_off, "theta_off": theta_off, "grad_offset": theta_off,
                                      "basis": int(getattr(inst, "basis", 0)), "group_begin": n_groups_total,
-                                     "group_count": len(g)})
+                                     "group_count": len(g), "n_params": int(inst.n_params)})
                 insts[i]["n"] = n
                 insts[i]["streamed"] = 2
                 theta_off += int(inst.n_params)

@@ -70,7 +70,7 @@ __device__ void eval_resident(const BatchArgs& A, const tq_batch_inst& I, int in
   }
   // lam = H psi, and E = Re <psi|lam>.  Thread owns j = gtid + k * gsize (k < N / gsize
   // <= 8 for every size class); the term sign parity splits as in k_wave_hpsi.
-  R eloc = 0;
+  R eloc = 0, nloc = 0;
   const int lg = 31 - __clz(gsize);
   const int per = N >> lg;
   if (per >= 1 && per <= 8 && (gsize << lg) != 0) {
@@ -108,6 +108,7 @@ __device__ void eval_resident(const BatchArgs& A, const tq_batch_inst& I, int in
         const int j = gtid + (k << lg);
         lam[j] = acc[k];
         eloc += psi[j].x * acc[k].x + psi[j].y * acc[k].y;
+        nloc += psi[j].x * psi[j].x + psi[j].y * psi[j].y;
       }
   } else {
     for (int j = gtid; j < N; j += gsize) {
@@ -120,9 +121,15 @@ __device__ void eval_resident(const BatchArgs& A, const tq_batch_inst& I, int in
       }
       lam[j] = acc;
       eloc += psi[j].x * acc.x + psi[j].y * acc.y;
+      nloc += psi[j].x * psi[j].x + psi[j].y * psi[j].y;
     }
   }
-  const double E = group_sum((double)eloc, red, gtid, gsize, bar);
+  // E = <psi|H|psi> / <psi|psi>: exact for unitary circuits, and for complex64
+  // states it removes the norm drift of rounded rotation coefficients; the
+  // gradient terms are divided by the same norm
+  const double Q = group_sum((double)nloc, red, gtid, gsize, bar);
+  const double inv = Q > 0 ? 1.0 / Q : 1.0;
+  const double E = group_sum((double)eloc, red, gtid, gsize, bar) * inv;
   // reverse sweep
   double* grad = A.grads + I.grad_offset;
   for (int k = I.adj_begin; k < I.adj_begin + I.adj_count; ++k) {
@@ -130,7 +137,7 @@ __device__ void eval_resident(const BatchArgs& A, const tq_batch_inst& I, int in
     if (o.slot >= 0) {
       const R part = tile_grad_partial<R>(psi, lam, n, o.gxm, o.gzm, o.gcm, gen_phase<R>(o.gny), gtid, gsize);
       const double s = group_sum((double)part, red, gtid, gsize, bar);
-      if (gtid == 0) grad[o.slot] += o.gcoef * s;
+      if (gtid == 0) grad[o.slot] += o.gcoef * s * inv;
     }
     tile_apply<R>(psi, n, o, gtid, gsize, true, th);
     tile_apply<R>(lam, n, o, gtid, gsize, true, th);
@@ -242,6 +249,7 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
   const int tid = threadIdx.x, nt = blockDim.x;
   double* red = reinterpret_cast<double*>(smem);
   unsigned char* work = smem + 32 * sizeof(double);
+  __shared__ double norm_inv;
   for (int64_t i = tid; i < N; i += nt) {
     T2 v;
     v.x = (i == I.basis) ? R(1) : R(0);
@@ -275,7 +283,7 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
   {
     cplx<R>* ps = reinterpret_cast<cplx<R>*>(work);
     cplx<R>* ls = ps + HN;
-    R eloc = 0;
+    R eloc = 0, nloc = 0;
     const int64_t ntile = N >> hb;
     for (int64_t T = 0; T < ntile; ++T) {
       for (int j = tid; j < HN; j += nt) ls[j] = cplx<R>(0, 0);
@@ -305,6 +313,7 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
       for (int j = tid; j < HN; j += nt) {
         const cplx<R> a = ps[j], l = ls[j];
         eloc += a.x * l.x + a.y * l.y;
+        nloc += a.x * a.x + a.y * a.y;
         T2 v;
         v.x = l.x;
         v.y = l.y;
@@ -312,7 +321,8 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
       }
       __syncthreads();
     }
-    // block sum of eloc
+    // block sums of eloc and of <psi|psi> (the energy and the gradient terms are
+    // divided by the norm: see eval_resident)
     double v = (double)eloc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -322,6 +332,19 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
       double s = 0;
       for (int w = 0; w < (nt >> 5); ++w) s += red[w];
       A.energies[inst_id] = s;
+    }
+    __syncthreads();
+    v = (double)nloc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) red[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+      double q = 0;
+      for (int w = 0; w < (nt >> 5); ++w) q += red[w];
+      const double inv = q > 0 ? 1.0 / q : 1.0;
+      A.energies[inst_id] *= inv;
+      norm_inv = inv;
     }
     __syncthreads();
   }
@@ -372,7 +395,7 @@ __device__ void eval_streamed(const BatchArgs& A, const tq_batch_inst& I, int in
     if (tid == 0)
       for (int k = 0; k < nops; ++k) {
         const tq_tile_op& o = A.ops[P.op_begin + k];
-        if (o.slot >= 0) grad[o.slot] += o.gcoef * acc[k];
+        if (o.slot >= 0) grad[o.slot] += o.gcoef * acc[k] * norm_inv;
       }
     __syncthreads();
   }

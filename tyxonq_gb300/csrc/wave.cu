@@ -104,7 +104,7 @@ template <typename R, int PER>
 __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restrict__ items, int n_items, int hbits,
                                                    const tq_pauli_group* __restrict__ groups,
                                                    const tq_pauli_term* __restrict__ terms, void* pool,
-                                                   void* lam_pool, double* partials) {
+                                                   void* lam_pool, double* partials, double* norm_partials) {
   typedef typename C2<R>::T T2;
   extern __shared__ __align__(16) unsigned char smem[];
   cplx<R>* src = reinterpret_cast<cplx<R>*>(smem);
@@ -235,29 +235,42 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
       buf ^= 1;
     }
     cp_async_wait_group<0>();
-    R eloc = 0;
+    R eloc = 0, nloc = 0;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       const int j = threadIdx.x + k * blockDim.x;
       if (j < HN) {
         const T2 a = psi[t0 + j];
         eloc += a.x * acc[k].x + a.y * acc[k].y;
+        nloc += a.x * a.x + a.y * a.y;
         T2 o;
         o.x = acc[k].x;
         o.y = acc[k].y;
         if (lam) lam[t0 + j] = o;
       }
     }
-    double v = (double)eloc;
+    double v = (double)eloc, nv = (double)nloc;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_down_sync(0xffffffffu, v, o);
+      nv += __shfl_down_sync(0xffffffffu, nv, o);
+    }
     __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    if ((threadIdx.x & 31) == 0) {
+      red[threadIdx.x >> 5] = v;
+      red[16 + (threadIdx.x >> 5)] = nv;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-      double s = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+      double s = 0, q = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        s += red[w];
+        q += red[16 + w];
+      }
       partials[I.part_off] = s;
+      // <psi|psi> of the tile: the energy of a complex64 state is divided by it
+      // (tq_wave_normalize), which removes the norm drift of rounded rotations
+      if (norm_partials) norm_partials[I.part_off] = q;
     }
   }
 }
@@ -399,7 +412,7 @@ template <typename R>
 static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, int hbits, int rb,
                        const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
                        const tq_pauli_group* groups, const tq_pauli_term* terms, const double* theta, void* pool,
-                       double* partials, int max_ops, cudaStream_t s) {
+                       double* partials, double* norm_partials, int max_ops, cudaStream_t s) {
   if (kind == 1) {
     if (hbits < 8 || hbits > 12) return fail(TQ_ERR_ARG, "tq_wave_run: hbits %d outside [8, 12]", hbits);
     const int grid = n_items;
@@ -408,7 +421,8 @@ static int wave_launch(int kind, const tq_wave_item* items, int n_items, int t, 
 #define TQ_HPSI(PER_)                                                                                          \
   e = cudaFuncSetAttribute(k_wave_hpsi<R, PER_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);        \
   if (e != cudaSuccess) return cuda_status(e, "tq_wave_run: smem attribute");                                  \
-  k_wave_hpsi<R, PER_><<<grid, 256, sm, s>>>(items, n_items, hbits, groups, terms, pool, pool, partials);
+  k_wave_hpsi<R, PER_><<<grid, 256, sm, s>>>(items, n_items, hbits, groups, terms, pool, pool, partials,       \
+                                             norm_partials);
     switch (hbits) {
       case 8: TQ_HPSI(1) break;
       case 9: TQ_HPSI(2) break;
@@ -575,14 +589,14 @@ extern "C" int tq_sv_pauli_sum_tiled(const void* psi, void* out, int n, int dtyp
     e = cudaFuncSetAttribute(k_wave_hpsi<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_status(e, "tq_sv_pauli_sum_tiled: smem attribute");
     k_wave_hpsi<float, 16><<<items, 256, sm, s>>>(it, items, kTiledHb, groups, terms, const_cast<void*>(psi), buf,
-                                                  part);
+                                                  part, nullptr);
     if (out && buf != out)
       k_slice_sum<float><<<grid_for(N, 256), 256, 0, s>>>((const float2*)buf, slices, N, (float2*)out);
   } else {
     e = cudaFuncSetAttribute(k_wave_hpsi<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_status(e, "tq_sv_pauli_sum_tiled: smem attribute");
     k_wave_hpsi<double, 16><<<items, 256, sm, s>>>(it, items, kTiledHb, groups, terms, const_cast<void*>(psi), buf,
-                                                   part);
+                                                   part, nullptr);
     if (out && buf != out)
       k_slice_sum<double><<<grid_for(N, 256), 256, 0, s>>>((const double2*)buf, slices, N, (double2*)out);
   }
@@ -594,7 +608,8 @@ extern "C" int tq_sv_pauli_sum_tiled(const void* psi, void* out, int n, int dtyp
 extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n_items, int t, int hbits,
                            int stage_bits, const tq_tile_pass* passes, const tq_tile_stage* stages,
                            const tq_tile_op* ops, const tq_pauli_group* groups, const tq_pauli_term* terms,
-                           const double* theta, void* pool, double* partials, int max_pass_ops, void* stream) {
+                           const double* theta, void* pool, double* partials, double* norm_partials,
+                           int max_pass_ops, void* stream) {
   if (dtype != TQ_C64 && dtype != TQ_C128) return fail(TQ_ERR_ARG, "tq_wave_run: bad dtype %d", dtype);
   if (kind < 0 || kind > 2) return fail(TQ_ERR_ARG, "tq_wave_run: bad kind %d", kind);
   if (n_items < 0) return fail(TQ_ERR_ARG, "tq_wave_run: negative item count");
@@ -606,9 +621,39 @@ extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n
   if (kind != 1 && max_pass_ops < 1) return fail(TQ_ERR_ARG, "tq_wave_run: max_pass_ops %d < 1", max_pass_ops);
   cudaStream_t s = (cudaStream_t)stream;
   return dtype == TQ_C64 ? wave_launch<float>(kind, items, n_items, t, hbits, stage_bits, passes, stages, ops, groups,
-                                              terms, theta, pool, partials, max_pass_ops, s)
+                                              terms, theta, pool, partials, norm_partials, max_pass_ops, s)
                          : wave_launch<double>(kind, items, n_items, t, hbits, stage_bits, passes, stages, ops,
-                                               groups, terms, theta, pool, partials, max_pass_ops, s);
+                                               groups, terms, theta, pool, partials, norm_partials, max_pass_ops, s);
+}
+
+// Energies and gradients of complex64 / complex128 states divided by <psi|psi>:
+// row r covers instance inst[r], whose norm partials are
+// norm_partials[first[r] .. first[r] + count[r]) (summed in order) and whose
+// gradient entries are grads[goff[r] .. goff[r] + gcount[r]).
+__global__ void k_wave_normalize(const double* __restrict__ norm_partials, const int32_t* __restrict__ first,
+                                 const int32_t* __restrict__ count, const int32_t* __restrict__ inst,
+                                 const int32_t* __restrict__ goff, const int32_t* __restrict__ gcount, int n_rows,
+                                 double* energies, double* grads) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+    double q = 0;
+    for (int j = 0; j < count[r]; ++j) q += norm_partials[first[r] + j];
+    const double inv = q > 0 ? 1.0 / q : 1.0;
+    energies[inst[r]] *= inv;
+    for (int j = 0; j < gcount[r]; ++j) grads[goff[r] + j] *= inv;
+  }
+}
+
+extern "C" int tq_wave_normalize(const double* norm_partials, const int32_t* first, const int32_t* count,
+                                 const int32_t* inst, const int32_t* goff, const int32_t* gcount, int n_rows,
+                                 double* energies, double* grads, void* stream) {
+  if (n_rows < 0) return fail(TQ_ERR_ARG, "tq_wave_normalize: negative count");
+  if (n_rows == 0) return TQ_OK;
+  if (!norm_partials || !first || !count || !inst || !goff || !gcount || !energies || !grads)
+    return fail(TQ_ERR_ARG, "tq_wave_normalize: NULL pointer");
+  k_wave_normalize<<<(n_rows + 127) / 128, 128, 0, (cudaStream_t)stream>>>(norm_partials, first, count, inst, goff,
+                                                                            gcount, n_rows, energies, grads);
+  TQ_CHECK_LAUNCH("tq_wave_normalize");
+  return TQ_OK;
 }
 
 extern "C" int tq_wave_reduce(const double* partials, const int32_t* first, const int32_t* count,

@@ -95,6 +95,7 @@ class WavePlan:
             waves.append(cur)
         self.waves = waves
         items, launches, rows = [], [], []
+        norm_rows, norm_lane = [], []
         item_lane, row_lane, self.launch_lanes = [], [], []
         lane_pool = [0] * self.lanes
         lane_part = [0] * self.lanes
@@ -162,6 +163,12 @@ class WavePlan:
                 rb = len(rows)
                 rows += layers[lay]
                 launches.append(("reduce_g", rb, len(layers[lay])))
+            # energies and gradients divided by <psi|psi> (norm partials of the H psi items)
+            nb = len(norm_rows)
+            norm_rows += [(e["epart"], 1 << (e["n"] - min(hbits, e["n"])), e["idx"], e["grad_offset"],
+                           int(e.get("n_params", 0))) for e in wv]
+            norm_lane += [lane] * len(wv)
+            launches.append(("normalize", nb, len(wv)))
             item_lane += [lane] * (len(items) - n_items0)
             row_lane += [lane] * (len(rows) - n_rows0)
             self.launch_lanes += [lane] * (len(launches) - n_launch0)
@@ -185,6 +192,12 @@ class WavePlan:
             it["lam_off"] += pool_base[il]
             it["part_off"] += part_base[il].astype(np.int32)
         rows = [(r[0] + int(part_base[l]),) + tuple(r[1:]) for r, l in zip(rows, row_lane)]
+        norm_rows = [(r[0] + int(part_base[l]),) + tuple(r[1:]) for r, l in zip(norm_rows, norm_lane)]
+        self.n_first = torch.tensor([x[0] for x in norm_rows] or [0], dtype=torch.int32, device=device)
+        self.n_count = torch.tensor([x[1] for x in norm_rows] or [0], dtype=torch.int32, device=device)
+        self.n_inst = torch.tensor([x[2] for x in norm_rows] or [0], dtype=torch.int32, device=device)
+        self.n_goff = torch.tensor([x[3] for x in norm_rows] or [0], dtype=torch.int32, device=device)
+        self.n_gcount = torch.tensor([x[4] for x in norm_rows] or [0], dtype=torch.int32, device=device)
         self.items_dev = _dev(it, device)
         r = np.array(rows, dtype=object) if rows else np.zeros((0, 5))
         self.r_first = torch.tensor([x[0] for x in rows] or [0], dtype=torch.int32, device=device)
@@ -201,6 +214,7 @@ class WavePlan:
         self.ops_dev = _dev(np.concatenate(self.ops) if self.ops else np.zeros(1, TILE_OP_DTYPE), device)
         self.pool = torch.empty(max(pool_need, 2), dtype=dtype, device=device)
         self.partials = torch.zeros(max(part_need, 1), dtype=torch.float64, device=device)
+        self.norm_partials = torch.zeros(max(part_need, 1), dtype=torch.float64, device=device)
         self.pool_bytes = self.pool.numel() * S
 
     def _specialise(self, items: list, device) -> None:
@@ -301,7 +315,7 @@ class WavePlan:
         for li, (L, lane) in enumerate(zip(self.launches, self.launch_lanes)):
             if lane_streams is not None:
                 stream = lane_streams[lane]
-            phase = L[1] if L[0] == "run" else (1 if L[0] == "reduce_e" else 2)
+            phase = L[1] if L[0] == "run" else (1 if L[0] in ("reduce_e", "normalize") else 2)
             if phase not in kinds:
                 continue
             if L[0] == "run" and li in self.jit_sub:
@@ -317,7 +331,7 @@ class WavePlan:
                         nat.call("tq_wave_run", kind, self.dt, P(self.items_dev.data_ptr() + isz * b0), c0, self.t,
                                  self.hbits, self.adj_rb if kind == 2 else 4, P(self.passes_dev.data_ptr()),
                                  P(self.stages_dev.data_ptr()), P(self.ops_dev.data_ptr()), None, None,
-                                 P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()),
+                                 P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()), None,
                                  self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
             elif L[0] == "run":
                 _, kind, b, c = L
@@ -328,7 +342,14 @@ class WavePlan:
                          P(self.stages_dev.data_ptr()),
                          P(self.ops_dev.data_ptr()), P(groups_dev.data_ptr()), P(terms_dev.data_ptr()),
                          P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()),
+                         P(self.norm_partials.data_ptr()) if kind == 1 else None,
                          self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
+            elif L[0] == "normalize":
+                _, b, c = L
+                nat.call("tq_wave_normalize", P(self.norm_partials.data_ptr()), P(self.n_first.data_ptr() + 4 * b),
+                         P(self.n_count.data_ptr() + 4 * b), P(self.n_inst.data_ptr() + 4 * b),
+                         P(self.n_goff.data_ptr() + 4 * b), P(self.n_gcount.data_ptr() + 4 * b), c,
+                         P(energies.data_ptr()), P(grads.data_ptr()), stream)
             else:
                 kind, b, c = L
                 out = energies if kind == "reduce_e" else grads
