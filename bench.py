@@ -330,6 +330,33 @@ def bench_fused_28q(args) -> dict:
             "pass_gbs": 2 * (1 << n2) * 8 / (m / prog.n_passes * 1e-3) / 1e9}
 
 
+def bench_serving(args) -> list:
+    """Serving sweep: for each arrival rate, a Poisson trace of
+    args.serving_requests requests (sessions of two optimizer steps, HEA
+    n ~ U{10..26}, depth ~ U{2..10}, 20-1000 Pauli terms, 30% energy+gradient,
+    complex64) replayed in real time; p50 / p99 latency and served throughput."""
+    import torch
+
+    from tyxonq_gb300.serving import VqeServer, make_trace, replay
+
+    serving = []
+    # warm-up trace (not reported): first use of every kernel and of the per-request streams
+    warm = make_trace(16, rate=80.0, seed=99, n_range=(10, 26), depth_range=(2, 10), terms_range=(20, 1000),
+                      grad_fraction=0.5, iterations=2)
+    replay(VqeServer(max_inflight=8), warm)
+    torch.cuda.empty_cache()
+    for rate in args.serving_rates:
+        trace = make_trace(args.serving_requests, rate=rate, seed=int(rate), n_range=(10, 26), depth_range=(2, 10),
+                           terms_range=(20, 1000), grad_fraction=0.3, iterations=2)
+        srv = VqeServer(max_inflight=8)
+        st = replay(srv, trace)
+        st["rate_rps"] = rate
+        serving.append(st)
+        del srv
+        torch.cuda.empty_cache()
+    return serving
+
+
 def bench_small_configs(reps: int = 10) -> dict:
     """Per-call times, host parameters in and host results out, of
     * the 12-qubit HEA (4 layers of [RY on every qubit; CX ladder]) with the
@@ -479,6 +506,9 @@ def run_case(args):
     if args.case == "fused":
         print(json.dumps({"case": "fused", **bench_fused_28q(args)}))
         return
+    if args.case == "serving":
+        print(json.dumps({"case": "serving", "sweep": bench_serving(args)}))
+        return
     if args.case == "civector":
         from tyxonq_gb300 import chem
         from tyxonq_gb300.vqe import UCCSD
@@ -517,10 +547,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--serving-requests", type=int, default=1000, help="requests per arrival rate")
+    ap.add_argument("--serving-rates", type=float, nargs="+", default=[25.0, 50.0, 100.0, 200.0])
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="weak: every rank evaluates its own --count instances; strong: one --count workload "
                          "split over the ranks by estimated cost")
-    ap.add_argument("--case", default="full", choices=["full", "gates", "fused", "batched", "small", "civector"],
+    ap.add_argument("--case", default="full",
+                    choices=["full", "gates", "fused", "batched", "small", "civector", "serving"],
                     help="gates / fused (28-qubit circuit, specialised passes only) / batched / small / civector "
                          "(16-qubit UCCSD in CI space): run only that part "
                          "(profiling captures); full: the benchmark line")
@@ -650,23 +683,7 @@ def main():
     small = bench_small_configs()
 
     # ---------------- serving: Poisson arrivals, 70% energy / 30% energy+gradient, 10-26 qubits
-    from tyxonq_gb300.serving import VqeServer, make_trace, replay
-
-    serving = []
-    # warm-up trace (not reported): first use of every kernel and of the per-request streams
-    warm = make_trace(16, rate=80.0, seed=99, n_range=(10, 26), depth_range=(2, 10), terms_range=(20, 1000),
-                      grad_fraction=0.5, iterations=2)
-    replay(VqeServer(max_inflight=8), warm)
-    torch.cuda.empty_cache()
-    for rate in (20.0, 80.0):
-        trace = make_trace(48, rate=rate, seed=int(rate), n_range=(10, 26), depth_range=(2, 10),
-                           terms_range=(20, 1000), grad_fraction=0.3, iterations=2)
-        srv = VqeServer(max_inflight=8)
-        st = replay(srv, trace)
-        st["rate_rps"] = rate
-        serving.append(st)
-        del srv
-        torch.cuda.empty_cache()
+    serving = bench_serving(args)
 
     # ---------------- CPU baseline: oracle port, one instance of every size, one core
     cpu = None
@@ -702,9 +719,11 @@ def main():
                                 "of one launch per gate",
                       "speedup_batched": value / world / plain_evals, "max_energy_diff_abs": worst},
         "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "latency": {"p50_ms": serving[-1]["p50_ms"], "p99_ms": serving[-1]["p99_ms"], "sweep": serving,
-                    "workload": "Poisson arrivals, 24 sessions x 2 optimizer steps, HEA n~U{10..26} depth~U{2..10}, "
-                                "20-1000 Pauli terms, 30% energy+gradient, complex64"},
+        "latency": {"p50_ms": serving[0]["p50_ms"], "p99_ms": serving[0]["p99_ms"],
+                    "at_rate_rps": serving[0]["rate_rps"], "sweep": serving,
+                    "workload": f"Poisson arrivals, {args.serving_requests // 2} sessions x 2 optimizer steps per "
+                                "rate, HEA n~U{10..26} depth~U{2..10}, 20-1000 Pauli terms, 30% energy+gradient, "
+                                "complex64"},
         "gate_kernels_28q": gk,
         "small_configs": small,
         "roofline": {"kernel": "tq_jit_staged_pass (circuit-specialised fused pass of the 28-qubit complex64 "

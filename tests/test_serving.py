@@ -21,7 +21,9 @@ class _FakeServer(VqeServer):
     """Device work replaced by tickets that complete after `delay` polls."""
 
     def __init__(self, delay=2, **kw):
-        super().__init__(device="cpu", estimator_factory=lambda r, d, dev: _FakeEst(r.n), **kw)
+        kw.setdefault("compile_workers", 0)
+        kw.setdefault("estimator_factory", lambda r, d, dev: _FakeEst(r.n))
+        super().__init__(device="cpu", **kw)
         self.delay = delay
         self.max_concurrent = 0
 
@@ -146,4 +148,32 @@ def test_footprint_counts_tables_workspace_and_partials():
     srv = VqeServer(device="cpu", hbm_budget=1 << 40, streams=[None])
     req = VqeRequest("s", n, struct, n_param, H, np.zeros(n_param), True)
     assert srv._footprint(req) == g
+
+
+def test_slow_estimator_builds_do_not_block_other_requests():
+    """A new session's estimator is built on the compile worker: a request of a
+    resident session admitted meanwhile completes before the slow build ends."""
+    import threading
+
+    gate = threading.Event()
+
+    def factory(req, dtype, device):
+        if req.session == "slow":
+            gate.wait(5)
+        return _FakeEst(req.n)
+
+    srv = _FakeServer(hbm_budget=1 << 30, streams=[None] * 4, compile_workers=1, estimator_factory=factory)
+    srv.submit(_req("fast", 8))
+    srv.drain()  # "fast" is resident now
+    slow, fast = _req("slow", 8), _req("fast", 8)
+    srv.submit(slow)
+    srv.submit(fast)
+    for _ in range(200):
+        srv.step()
+        if fast.done is not None:
+            break
+    assert fast.done is not None and slow.done is None  # not blocked by the build
+    gate.set()
+    srv.drain()
+    assert slow.error is None and slow.energy == 8.0
 

@@ -307,7 +307,10 @@ class ParametricEstimator:
     call takes a parameter vector (host array or float64 device tensor)."""
 
     def __init__(self, n: int, pgates: Sequence[ParamGate], n_params: int, hamiltonian, dtype=torch.complex64,
-                 device="cuda", init_basis: int = 0):
+                 device="cuda", init_basis: int = 0, prog: AdjointProgram | None = None):
+        """prog: a program already compiled for this structure (build_parametric
+        of the same pgates, n, n_params and dtype); its tables are read-only and
+        may be shared by estimators on one device."""
         self.n = int(n)
         self.n_params = int(n_params)
         self.H = as_pauli_sum(hamiltonian, self.n)
@@ -315,7 +318,7 @@ class ParametricEstimator:
         self.device = torch.device(device)
         self.init_basis = int(init_basis)
         self._pgates = list(pgates)
-        self.prog = build_parametric(pgates, self.n, self.n_params, dtype)
+        self.prog = prog if prog is not None else build_parametric(pgates, self.n, self.n_params, dtype)
         self.theta = torch.zeros(max(self.n_params, 1), dtype=torch.float64, device=self.device)
         self._staged = None
         cold = sum(_cold_in_staged_adjoint(_canon(p.gate)) for p in pgates) / max(len(pgates), 1)

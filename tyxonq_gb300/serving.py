@@ -9,7 +9,10 @@ over time.  The server
     budget -- evicting idle sessions least-recently-used first;
   * keeps each session's statevectors and compiled circuit resident across
     its optimizer iterations (angles are read on the device, so a new
-    parameter vector costs one small copy, no re-planning);
+    parameter vector costs one small copy, no re-planning); a new session's
+    estimator is built on a worker thread (the loop keeps admitting and
+    polling), and sessions with the same circuit structure share one compiled
+    program;
   * enqueues every admitted request on its own CUDA stream, so the work of
     requests that arrive while others run overlaps on the device, and
     completes requests by polling their events;
@@ -21,8 +24,10 @@ of waiting forever.  The reference has no serving layer; this is new.
 """
 from __future__ import annotations
 
+import threading
 import time
 from collections import OrderedDict, deque
+from concurrent.futures import Future, ThreadPoolExecutor
 from dataclasses import dataclass, field
 from typing import Callable, Sequence
 
@@ -52,13 +57,33 @@ class VqeRequest:
         return None if self.done is None else self.done - self.arrival
 
 
+_PROGRAMS: "OrderedDict" = OrderedDict()  # structure key -> (param gates, compiled program)
+_PROGRAMS_LOCK = threading.Lock()
+_PROGRAMS_MAX = 256
+
+
 def default_estimator_factory(req: VqeRequest, dtype, device):
-    from .adjoint import ParamGate, ParametricEstimator
+    """A session estimator; sessions with the same circuit structure share one
+    compiled program (structure-keyed cache: only angles and H differ)."""
+    from .adjoint import ParamGate, ParametricEstimator, build_parametric
     from .batch import structure_gates
 
-    gates, params = structure_gates(req.structure)
-    pg = [ParamGate(g, params[i][0] if i in params else None) for i, g in enumerate(gates)]
-    return ParametricEstimator(req.n, pg, req.n_params, req.H, dtype=dtype, device=device)
+    key = (int(req.n), tuple((nm, tuple(int(q) for q in qs), p) for nm, qs, p in req.structure),
+           int(req.n_params), str(dtype), str(device))
+    with _PROGRAMS_LOCK:
+        hit = _PROGRAMS.get(key)
+        if hit is not None:
+            _PROGRAMS.move_to_end(key)
+    if hit is None:
+        gates, params = structure_gates(req.structure)
+        pg = [ParamGate(g, params[i][0] if i in params else None) for i, g in enumerate(gates)]
+        hit = (pg, build_parametric(pg, req.n, req.n_params, dtype))
+        with _PROGRAMS_LOCK:
+            _PROGRAMS[key] = hit
+            while len(_PROGRAMS) > _PROGRAMS_MAX:
+                _PROGRAMS.popitem(last=False)
+    pg, prog = hit
+    return ParametricEstimator(req.n, pg, req.n_params, req.H, dtype=dtype, device=device, prog=prog)
 
 
 @dataclass
@@ -67,11 +92,15 @@ class _Session:
     bytes: int
     busy: bool = False
     pending: deque = field(default_factory=deque)
+    building: Future | None = None  # estimator under construction on the compile worker
 
 
 class VqeServer:
     def __init__(self, device="cuda", dtype=torch.complex64, hbm_budget: int | None = None, max_inflight: int = 8,
-                 estimator_factory: Callable | None = None, streams: Sequence | None = None):
+                 estimator_factory: Callable | None = None, streams: Sequence | None = None,
+                 compile_workers: int = 1):
+        """compile_workers > 0: new sessions' estimators are built on a worker
+        thread while the loop keeps admitting and polling other requests."""
         self.device = torch.device(device)
         self.dtype = dtype
         if hbm_budget is None:
@@ -87,6 +116,7 @@ class VqeServer:
         self.inflight: list = []
         self.used = 0
         self.completed: list[VqeRequest] = []
+        self.pool = ThreadPoolExecutor(compile_workers) if compile_workers > 0 else None
 
     # ------------------------------------------------------------ memory
     def _footprint(self, req: VqeRequest) -> int:
@@ -164,6 +194,11 @@ class VqeServer:
         self.sessions.move_to_end(req.session)
         sess.busy = True
         req.admitted = time.perf_counter()
+        if sess.est is None and self.pool is not None:
+            # build off the loop; launched by _poll once the estimator exists
+            sess.building = self.pool.submit(self.factory, req, self.dtype, self.device)
+            self.inflight.append((req, si, None, None, None, sess))
+            return
         ev, e_h, sv_h = self._launch(sess, req, si)
         self.inflight.append((req, si, ev, e_h, sv_h, sess))
 
@@ -197,6 +232,25 @@ class VqeServer:
         still = []
         for item in self.inflight:
             req, si, ev, e_h, sv_h, sess = item
+            if ev is None:  # estimator still being built
+                if not sess.building.done():
+                    still.append(item)
+                    continue
+                try:
+                    sess.est = sess.building.result()
+                except Exception as exc:  # a session that cannot be built fails its request
+                    sess.building = None
+                    req.error = f"{type(exc).__name__}: {exc}"
+                    req.done = time.perf_counter()
+                    sess.busy = False
+                    self.free_streams.append(si)
+                    self.completed.append(req)
+                    done += 1
+                    continue
+                sess.building = None
+                ev, e_h, sv_h = self._launch(sess, req, si)
+                still.append((req, si, ev, e_h, sv_h, sess))
+                continue
             if not self._ready(ev):
                 still.append(item)
                 continue
