@@ -32,6 +32,9 @@ METRIC = "VQE energy+grad evals/s batched vs plain GPU; p50/p99 latency; gate HB
 # DRAM bytes read + written by one k_staged_forward launch of the 28-qubit pass,
 # from the ncu capture summarised in profiles/k_staged_forward_28q_c64.txt
 STAGED_PASS_DRAM_BYTES = 4.2654e9
+# DRAM bytes per item of the wave adjoint kernel (L2-resident states): from the
+# ncu capture of tq_jit_wave_adjoint; None until captured
+WAVE_ADJ_DRAM_BYTES_PER_ITEM = None
 
 
 def _peaks():
@@ -330,6 +333,29 @@ def bench_fused_28q(args) -> dict:
             "pass_gbs": 2 * (1 << n2) * 8 / (m / prog.n_passes * 1e-3) / 1e9}
 
 
+def measure_l2_copy_gbs(mib: int = 24, reps: int = 50) -> float:
+    """Bandwidth of a copy whose source and destination stay in L2 together
+    (2 x `mib` MiB < 126 MiB): read + write bytes / device time, best of 3."""
+    import torch
+
+    a = torch.empty(mib << 20, dtype=torch.uint8, device="cuda").fill_(1)
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        x, y = _events()
+        x.record()
+        for _ in range(reps):
+            b.copy_(a)
+        y.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * a.numel() * reps / (x.elapsed_time(y) * 1e-3) / 1e9)
+    del a, b
+    return best
+
+
 def bench_serving(args) -> list:
     """Serving sweep: for each arrival rate, a Poisson trace of
     args.serving_requests requests (sessions of two optimizer steps, HEA
@@ -624,6 +650,16 @@ def main():
         ms = float(t.item())
     value = job_count / (ms * 1e-3)
 
+    # ---------------- per-phase device time of the wave kernels (one evaluation, serialised on
+    # one stream, CUDA events around every launch) against the measured L2 copy bandwidth
+    waves_prof = bv.profile_waves()
+    torch.cuda.synchronize()
+    l2_gbs = measure_l2_copy_gbs()
+    for ph in waves_prof.values():
+        ph["gbs"] = ph["alg_bytes"] / (ph["ms"] * 1e-3) / 1e9
+        ph["frac_of_l2_copy"] = ph["gbs"] / l2_gbs
+        ph["avg_launch_ms"] = ph["ms"] / ph["launches"]
+
     # ---------------- e2e: host theta -> device, evaluate, energies + gradients -> host
     e_host = torch.empty(bv.count, dtype=torch.float64).pin_memory()
     g_host = torch.empty(bv.grads.numel(), dtype=torch.float64).pin_memory()
@@ -726,10 +762,18 @@ def main():
                                 "complex64"},
         "gate_kernels_28q": gk,
         "small_configs": small,
-        "roofline": {"kernel": "tq_jit_staged_pass (circuit-specialised fused pass of the 28-qubit complex64 "
-                               "depth-40 random circuit, 2*N*8 B per launch)", "bound": "hbm",
-                     "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,
-                     "traffic": STAGED_PASS_DRAM_BYTES, "peak_kind": peak_kind},
+        "roofline": {"kernel": "tq_jit_wave_adjoint (circuit-specialised adjoint pass of the L2-resident waves, "
+                               "the largest share of the batched step; 4 * 2^12 * 8 B per item: psi and lam tiles "
+                               "read and written once)",
+                     "bound": "l2", "achieved": waves_prof["adjoint"]["gbs"], "peak": l2_gbs, "unit": "GB/s",
+                     "frac": waves_prof["adjoint"]["frac_of_l2_copy"], "traffic": WAVE_ADJ_DRAM_BYTES_PER_ITEM,
+                     "traffic_unit": "DRAM bytes per item (ncu)",
+                     "peak_kind": "measured in this run: L2-resident copy (2 x 24 MiB)"},
+        "roofline_c2": {"kernel": "tq_jit_staged_pass (circuit-specialised fused pass of the 28-qubit complex64 "
+                                  "depth-40 random circuit, 2*N*8 B per launch)", "bound": "hbm",
+                        "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,
+                        "traffic": STAGED_PASS_DRAM_BYTES, "peak_kind": peak_kind},
+        "wave_kernels": {"phases": waves_prof, "l2_copy_gbs": l2_gbs},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches_per_step * args.steps,

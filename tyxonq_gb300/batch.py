@@ -184,7 +184,9 @@ class BatchedVQE:
                 wave_entries.append({"idx": i, "n": n, "gates": gates, "params": params, "key": (n, skey),
                                      "theta_offset": theta_off, "theta_off": theta_off, "grad_offset": theta_off,
                                      "basis": int(getattr(inst, "basis", 0)), "group_begin": n_groups_total,
-                                     "group_count": len(g), "n_params": int(inst.n_params)})
+                                     "group_count": len(g), "n_params": int(inst.n_params),
+                                     "partner_tiles": int(len(np.unique(g["flip"] >> np.uint64(
+                                         min(self.sched.wave_hbits, n))))) if len(g) else 0})
                 insts[i]["n"] = n
                 insts[i]["streamed"] = 2
                 theta_off += int(inst.n_params)
@@ -376,6 +378,48 @@ class BatchedVQE:
                 elif L[0] != "run" or L[3] > 0:
                     n += 1
         return n
+
+    def profile_waves(self) -> dict:
+        """One evaluation of the wave launches alone, serialised on the current
+        stream with CUDA events around every kernel: per phase (forward, hpsi,
+        adjoint) the launches, items, total device ms and the algorithmic bytes
+        moved (forward 2 * 2^t * S per item, adjoint 4 * 2^t * S -- psi and lam
+        tiles read and written once -- and H psi (1 + partner tiles) * 2^hb * S
+        read plus 2^hb * S written per item)."""
+        if self.waves is None:
+            return {}
+        main = torch.cuda.current_stream(self.device)
+        marks = []
+
+        def cb(when, kind, items, jit):
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(main)
+            marks.append((when, kind, items, jit, ev))
+
+        self.grads.zero_()
+        self.launch_waves_only(main, cb)
+        torch.cuda.synchronize(self.device)
+        out: dict = {}
+        names = {0: "forward", 1: "hpsi", 2: "adjoint"}
+        S = 8 if self.dtype == torch.complex64 else 16
+        for (w0, kind, items, jit, a), (w1, _, _, _, b) in zip(marks[0::2], marks[1::2]):
+            d = out.setdefault(names[kind], {"launches": 0, "items": 0, "ms": 0.0, "specialised_launches": 0})
+            d["launches"] += 1
+            d["items"] += items
+            d["ms"] += a.elapsed_time(b)
+            d["specialised_launches"] += int(jit)
+        t = self.waves.t
+        if "forward" in out:
+            out["forward"]["alg_bytes"] = out["forward"]["items"] * 2 * (S << t)
+        if "adjoint" in out:
+            out["adjoint"]["alg_bytes"] = out["adjoint"]["items"] * 4 * (S << t)
+        if "hpsi" in out:
+            out["hpsi"]["alg_bytes"] = int(self.waves.hpsi_alg_bytes)
+        return out
+
+    def launch_waves_only(self, stream, on_launch=None) -> None:
+        self.waves.launch(self.groups_dev, self.terms_dev, self.theta, self.energies, self.grads,
+                          ctypes.c_void_p(stream.cuda_stream), None, on_launch=on_launch)
 
     def capture(self) -> None:
         """Capture launch() into a CUDA graph (replayed by run())."""

@@ -96,6 +96,7 @@ class WavePlan:
         self.waves = waves
         items, launches, rows = [], [], []
         norm_rows, norm_lane = [], []
+        self.hpsi_alg_bytes = 0
         item_lane, row_lane, self.launch_lanes = [], [], []
         lane_pool = [0] * self.lanes
         lane_part = [0] * self.lanes
@@ -127,6 +128,7 @@ class WavePlan:
             b = len(items)
             for e in wv:
                 hb = min(hbits, e["n"])
+                self.hpsi_alg_bytes += (1 << (e["n"] - hb)) * (int(e.get("partner_tiles", 1)) + 1) * (S << hb)
                 for tile in range(1 << (e["n"] - hb)):
                     items.append((e["psi_off"], e["lam_off"], 0, tile, e["theta_off"], e["epart"] + tile, e["n"],
                                   e["group_begin"], e["group_count"], -1))
@@ -306,12 +308,14 @@ class WavePlan:
 
     # ------------------------------------------------------------ execution
     def launch(self, groups_dev, terms_dev, theta, energies, grads, stream, lane_streams=None,
-               kinds=(0, 1, 2)) -> None:
+               kinds=(0, 1, 2), on_launch=None) -> None:
         """Enqueue every launch; lane l's on lane_streams[l] when given, else all on `stream`.
         kinds: the phases to run (0 forward, 1 H psi + energy reduction, 2 adjoint +
-        gradient reductions)."""
+        gradient reductions).  on_launch(when, kind, n_items, jit): called before
+        ("start") and after ("end") each kernel launch (profiling on one stream)."""
         P = ctypes.c_void_p
         isz = WAVE_ITEM_DTYPE.itemsize
+        cb = on_launch or (lambda *a: None)
         for li, (L, lane) in enumerate(zip(self.launches, self.launch_lanes)):
             if lane_streams is not None:
                 stream = lane_streams[lane]
@@ -321,6 +325,7 @@ class WavePlan:
             if L[0] == "run" and li in self.jit_sub:
                 kind = L[1]
                 for b0, c0, k in self.jit_sub[li]:
+                    cb("start", kind, c0, bool(k))
                     if k:
                         nat.call("tq_jit_wave_run", P(k), kind, self.dt, P(self.items_dev.data_ptr() + isz * b0), c0,
                                  self.t, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
@@ -333,10 +338,12 @@ class WavePlan:
                                  P(self.stages_dev.data_ptr()), P(self.ops_dev.data_ptr()), None, None,
                                  P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()), None,
                                  self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
+                    cb("end", kind, c0, bool(k))
             elif L[0] == "run":
                 _, kind, b, c = L
                 if c == 0:
                     continue
+                cb("start", kind, c, False)
                 nat.call("tq_wave_run", kind, self.dt, P(self.items_dev.data_ptr() + isz * b), c, self.t,
                          self.hbits, self.adj_rb if kind == 2 else 4, P(self.passes_dev.data_ptr()),
                          P(self.stages_dev.data_ptr()),
@@ -344,6 +351,7 @@ class WavePlan:
                          P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()),
                          P(self.norm_partials.data_ptr()) if kind == 1 else None,
                          self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
+                cb("end", kind, c, False)
             elif L[0] == "normalize":
                 _, b, c = L
                 nat.call("tq_wave_normalize", P(self.norm_partials.data_ptr()), P(self.n_first.data_ptr() + 4 * b),
