@@ -60,3 +60,42 @@ def test_basis_change_restores_state():
     H = as_pauli_sum(_tfim(n), n)
     shot_energy(psi, H, 1000, 1)
     np.testing.assert_allclose(psi.cpu().numpy(), v, atol=1e-13)
+
+
+def test_reference_basis_mapping_matches_its_exact_observable():
+    """basis_map='reference' rotates circuit qubit n-1-q for Hamiltonian index q
+    and reads parities at q (hea_device_runtime.py:282-284): the estimate
+    converges to the exact value of that measured observable."""
+    from tyxonq_gb300 import kernels as K
+    from tyxonq_gb300.shots import group_by_basis, shot_energy
+
+    n = 6
+    rng = np.random.default_rng(9)
+    v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    v /= np.linalg.norm(v)
+    terms = [(0.7, [("X", 0), ("Z", 2)]), (-0.4, [("Y", 1)]), (0.9, [("Z", 3), ("Z", 5)]), (0.5, [("X", 4)])]
+    psi = K.from_array(v, dtype=torch.complex128)
+    shots = 40000
+    est = shot_energy(psi, terms, shots, seed=2, basis_map="reference")
+    h = np.array([[1, 1], [1, -1]]) / math.sqrt(2)
+    to_z = {"X": h, "Y": h @ np.diag([1.0, -1j])}
+    const, groups = group_by_basis(terms, n)
+    exact = const
+    for bases, items in groups.items():
+        w = v.copy()
+        for q, p in enumerate(bases):
+            if p in to_z:
+                w = sv.apply_1q(w, to_z[p], n - 1 - q, n)
+        prob = np.abs(w) ** 2
+        idx = np.arange(1 << n)
+        for term, c in items:
+            mask = 0
+            for q, _ in term:
+                mask |= 1 << (n - 1 - q)
+            par = np.array([bin(i & mask).count("1") & 1 for i in idx])
+            exact += c * float(np.sum(prob * (1 - 2 * par)))
+    sigma = math.sqrt(sum(c * c for c, t in terms) / shots)
+    assert abs(est - exact) < 5 * sigma
+    same = shot_energy(psi, terms, shots, seed=2)
+    exact_same = float(np.real(np.vdot(v, sv.apply_pauli_sum(v, *sv.terms_to_codes(n, terms)))))
+    assert abs(same - exact_same) < 5 * sigma

@@ -453,6 +453,35 @@ class AdjointEnergy(torch.autograd.Function):
         return gout * g, None
 
 
+class PauliEnergyFn(torch.autograd.Function):
+    """E = Re <psi|H|psi> of a device state for a Pauli-sum H, differentiable in
+    psi (backward: dE/dpsi = 2 H psi in torch's complex-gradient convention, the
+    input _StateFn's adjoint backward takes).  Replaces dynamics.expectation
+    with a dense H (dynamics.py:117-126) without forming the 2^n x 2^n matrix."""
+
+    @staticmethod
+    def forward(ctx, psi: torch.Tensor, H):
+        ctx.save_for_backward(psi)
+        ctx.H = H
+        return K.pauli_expectation(psi.detach().contiguous(), H).reshape(())
+
+    @staticmethod
+    def backward(ctx, gout):
+        (psi,) = ctx.saved_tensors
+        hpsi = K.apply_pauli_sum(psi.detach().contiguous(), ctx.H)
+        scale = (2.0 * gout).to(hpsi.real.dtype)
+        return scale * hpsi, None
+
+
+def pauli_energy(psi, H):
+    """Differentiable <psi|H|psi> of a device state (torch) or a host state (numpy: float)."""
+    if isinstance(psi, torch.Tensor) and psi.is_cuda:
+        return PauliEnergyFn.apply(psi, H)
+    arr = psi.detach().cpu().numpy() if isinstance(psi, torch.Tensor) else np.asarray(psi)
+    dev = K.from_array(arr, dtype=torch.complex128 if arr.dtype == np.complex128 else torch.complex64)
+    return float(K.pauli_expectation(dev, H).item())
+
+
 # ---------------------------------------------------------------- circuit-level autograd
 def _angle_leaves(circuit) -> tuple[list, list]:
     """(angle tensors requiring grad, (op index, arg position) for each)."""

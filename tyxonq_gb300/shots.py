@@ -14,7 +14,9 @@ Here the state is prepared once per parameter vector on the GPU, each group's
 basis change is applied in place with the 1q kernel, shots are drawn with the
 device sampler (sorted basis indices, counter-based RNG), the change is undone,
 and the parities are reduced from the sampled indices.  A term's qubit q is
-the circuit's qubit q (bit n-1-q of the basis index).
+the circuit's qubit q (bit n-1-q of the basis index); basis_map="reference"
+reproduces the reference runtime's mapping instead (rotation on circuit qubit
+n-1-q for Hamiltonian index q).
 """
 from __future__ import annotations
 
@@ -65,14 +67,23 @@ def parity_expectations(indices: np.ndarray, terms: Sequence, n: int) -> np.ndar
     return out
 
 
-def shot_energy(psi: torch.Tensor, H, shots: int, seed: int, grouping: tuple | None = None) -> float:
+def shot_energy(psi: torch.Tensor, H, shots: int, seed: int, grouping: tuple | None = None,
+                basis_map: str = "same") -> float:
     """Estimate <psi|H|psi> from `shots` samples per basis group.  psi is
-    restored (up to rounding) on return."""
+    restored (up to rounding) on return.
+
+    basis_map: "same" rotates circuit qubit q for the term's qubit q (the
+    estimate of <H>); "reference" reproduces hea_device_runtime.py:
+    _prefix_ops_for_bases (:282-284), which rotates circuit qubit n-1-q for
+    Hamiltonian index q while the parities are read at position q, so that
+    results equal that runtime's on the same counts."""
     n = K._check_state(psi)
+    if basis_map not in ("same", "reference"):
+        raise ValueError("basis_map must be 'same' or 'reference'")
     const, groups = grouping if grouping is not None else group_by_basis(H, n)
     e = const
     for gi, (bases, items) in enumerate(groups.items()):
-        rot = [(q, p) for q, p in enumerate(bases) if p in _TO_Z]
+        rot = [((n - 1 - q) if basis_map == "reference" else q, p) for q, p in enumerate(bases) if p in _TO_Z]
         for q, p in rot:
             K.apply_1q(psi, _TO_Z[p], q)
         idx = K.sample(psi, shots, (int(seed) * 1000003 + gi) & ((1 << 63) - 1)).cpu().numpy()
@@ -89,18 +100,19 @@ class ShotEstimator:
     program): every shifted parameter vector is one forward run plus one
     sampling round per basis group."""
 
-    def __init__(self, est, H, shots: int = 1024, seed: int = 0):
+    def __init__(self, est, H, shots: int = 1024, seed: int = 0, basis_map: str = "same"):
         self.est = est
         self.n = est.n
         self.shots = int(shots)
         self.seed = int(seed)
         self.grouping = group_by_basis(H, self.n)
+        self.basis_map = basis_map
         self._calls = 0
 
     def energy(self, theta) -> float:
         psi = self.est._forward(np.asarray(theta, dtype=np.float64))
         self._calls += 1
-        return shot_energy(psi, None, self.shots, self.seed + self._calls, self.grouping)
+        return shot_energy(psi, None, self.shots, self.seed + self._calls, self.grouping, self.basis_map)
 
     def energy_and_grad(self, theta) -> tuple[float, np.ndarray]:
         th = np.asarray(theta, dtype=np.float64)
