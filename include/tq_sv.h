@@ -269,6 +269,22 @@ typedef struct {
 TQ_API int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
                             const tq_tile_stage* stages, const tq_tile_op* ops, const double* theta, void* stream);
 
+/* ------------------------------------------------------------ Kraus trajectory batches */
+
+/* One Kraus channel on `qubit` of n_traj trajectories of an n-qubit circuit,
+ * stored as n_traj consecutive states of 2^n amplitudes: per trajectory the
+ * qubit's reduced density matrix, the Born weights p_i = Tr(K_i rho K_i^dagger)
+ * of the n_ops (<= 16) operators in kraus_dev (device, 8 doubles each,
+ * row-major (re, im)), the first operator whose cumulative normalised weight
+ * reaches status_dev[t] (and whose weight is positive), and psi_t <-
+ * K_i psi_t / sqrt(p_i); chosen_dev[t] = i.  Fixed-order sums, no host round
+ * trip.  Replaces the per-run unravelling of apply_kraus_statevector
+ * (tyxonq/libs/quantum_library/kernels/statevector.py:132-218, engine.py:145-155),
+ * one trajectory per call there, for a whole batch of trajectories here. */
+TQ_API size_t tq_traj_kraus_workspace_bytes(int n, int n_traj);
+TQ_API int tq_traj_kraus(void* psi, int n, int n_traj, int dtype, int qubit, const double* kraus_dev, int n_ops,
+                         const double* status_dev, int32_t* chosen_dev, void* ws, size_t ws_bytes, void* stream);
+
 /* ------------------------------------------------------------ circuit-specialised passes */
 
 /* Runtime compilation (NVRTC, sm_103a) of staged forward pass kernels whose op

@@ -88,3 +88,48 @@ def test_noisy_sampling_distribution(noise):
     psi, _ = sv.run_ops(n, ops, mode="run")
     p = sv.noisy_probabilities(psi, n, noise)
     assert sv.chi2_pvalue(out["result"], p) > 1e-4
+
+
+@pytest.mark.parametrize("dtype,tol", [(C128, 1e-12), (C64, 1e-5)])
+def test_kraus_trajectory_batch_matches_oracle_per_trajectory(dtype, tol):
+    """64 trajectories of a noisy circuit in one batch (run_trajectories):
+    every trajectory's <Z_q> equals the oracle's single-trajectory unravelling
+    (apply_kraus_statevector restated) with the same statuses, and the mean
+    equals their average."""
+    sets = golden_data.kraus_sets()
+    n, T = 7, 64
+    rng = np.random.default_rng(4)
+    ops = []
+    kc = {"ad": sets["amp_damp"], "pd": sets["phase_damp"], "dp": sets["depol"]}
+    for layer in range(3):
+        for q in range(n):
+            ops.append(("ry", q, float(rng.uniform(0, 2 * np.pi))))
+        for q in range(n - 1):
+            ops.append(("cx", q, q + 1))
+        for q in range(0, n, 2):
+            ops.append(("kraus", q, ["ad", "pd", "dp"][(q + layer) % 3]))
+    ops.append(("kraus", 1, "ad", 0.5))  # an explicit status: the same for every trajectory
+    ops += [("measure_z", q) for q in range(n)]
+    eng = _engine(dtype)
+    out = eng.run_trajectories(_C(n, ops, kc), T, seed=21, per_trajectory=True)
+    assert out["trajectories"] == T
+    per = out["per_trajectory"]
+    stat = out["statuses"]
+    for t in range(T):
+        j, ops_t = 0, []
+        for op in ops:
+            if op[0] == "kraus" and len(op) == 3:
+                ops_t.append(("kraus", op[1], op[2], float(stat[j][t])))
+                j += 1
+            elif op[0] == "kraus":
+                ops_t.append(op)
+                j += 1
+            else:
+                ops_t.append(op)
+        psi, meas = sv.run_ops(n, ops_t, mode="run", kraus_cache=kc)
+        z = [sv.expect_z(psi, q, n) for q in meas]
+        np.testing.assert_allclose(per[t], z, atol=tol, rtol=0, err_msg=f"trajectory {t}")
+    mean = [out["expectations"][f"Z{q}"] for q in range(n)]
+    np.testing.assert_allclose(mean, per.mean(axis=0), atol=tol, rtol=0)
+    # distinct trajectories actually took different branches
+    assert np.unique(np.round(per[:, 0], 6)).size > 1

@@ -77,6 +77,8 @@ SIGNATURES: dict[str, tuple] = {
     "tq_sv_tile_max_bits": (c_int, [c_int]),
     "tq_sv_run_staged": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P, _P, _P]),
     "tq_sv_run_tiles": (c_int, [_P, c_int, c_int, _P, c_int, _P, _P, _P]),
+    "tq_traj_kraus_workspace_bytes": (c_size_t, [c_int, c_int]),
+    "tq_traj_kraus": (c_int, [_P, c_int, c_int, c_int, c_int, _P, c_int, _P, _P, _P, c_size_t, _P]),
     "tq_jit_build": (c_int, [ctypes.c_char_p, _P, c_int, _P, _P, ctypes.c_char_p, c_size_t]),
     "tq_jit_free_host": (None, [_P]),
     "tq_jit_load": (c_int, [_P, c_size_t, ctypes.c_char_p, _P]),

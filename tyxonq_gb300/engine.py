@@ -245,6 +245,61 @@ class GpuStatevectorEngine:
                 raise NotImplementedError(f"Pauli products on {len(qs)} qubits not yet supported")
         return float(K.inner_re(phi, psi).item())
 
+    def run_trajectories(self, circuit, trajectories: int, seed: int | None = None,
+                         per_trajectory: bool = False) -> Dict[str, Any]:
+        """<Z_q> of the measured qubits over a batch of Kraus trajectories.
+
+        The reference unravels one trajectory per run() (each Kraus op draws a
+        status, engine.py:145-155; statevector.py:132-218).  Here
+        `trajectories` (rounded up to a power of two, T) run together: T states
+        of the circuit back to back form one state of n + log2 T qubits, so
+        every unitary segment between channels is one fused program over all
+        of them, and each channel is one device step in which every trajectory
+        picks its operator from its own status (tq_traj_kraus).  Statuses of a
+        Kraus op without an explicit status are drawn, op by op, as
+        numpy.random.default_rng(seed).random(T).  Returns {"expectations":
+        {"Z{q}": mean over trajectories}, "trajectories": T, "statuses": [per
+        channel array], and "per_trajectory": T x len(measured) array when
+        asked}."""
+        from dataclasses import replace
+
+        n = int(getattr(circuit, "num_qubits", 0))
+        T = 1 << max(0, int(trajectories - 1).bit_length()) if trajectories > 1 else 1
+        b = T.bit_length() - 1
+        gates, measures = lower_ops(circuit, mode="run", extended=self.extended_gates)
+        init = self._initial(circuit)
+        psi = init.reshape(1, -1).expand(T, -1).contiguous().reshape(-1)
+        rng = np.random.default_rng(seed)
+        statuses = []
+        seg: list[Gate] = []
+
+        def flush():
+            if seg:
+                self._execute_unitary(psi, seg)
+                seg.clear()
+
+        for g in gates:
+            if g.kind == "kraus":
+                flush()
+                st = np.full(T, float(g.status)) if g.status is not None else rng.random(T)
+                statuses.append(st)
+                K.kraus_trajectories(psi, n, T, g.kraus, g.qubits[0], torch.from_numpy(st))
+            else:
+                seg.append(replace(g, qubits=tuple(q + b for q in g.qubits),
+                                   pauli=tuple((q + b, pp) for q, pp in g.pauli) if g.pauli else g.pauli))
+        flush()
+        out: Dict[str, Any] = {"trajectories": T, "statuses": statuses}
+        z = K.expect_z_all(psi).cpu().numpy() if n + b > 0 else np.zeros(0)
+        out["expectations"] = {f"Z{q}": float(z[q + b]) / T for q in measures}
+        if per_trajectory:
+            per = np.zeros((T, len(measures)))
+            view = psi.reshape(T, -1)
+            for t in range(T):
+                zt = K.expect_z_all(view[t]).cpu().numpy() if n > 0 else np.zeros(0)
+                per[t] = [zt[q] for q in measures]
+            out["per_trajectory"] = per
+        return out
+
     # ------------------------------------------------------------ extras
     def energy(self, circuit, hamiltonian) -> float:
         """Re <psi|H|psi> for a Pauli-sum H, FP64 accumulation."""

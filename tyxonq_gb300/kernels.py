@@ -268,6 +268,23 @@ def apply_kraus(psi: torch.Tensor, ops, qubit: int, status: float) -> int:
     return sel
 
 
+def kraus_trajectories(psi: torch.Tensor, n: int, n_traj: int, ops, qubit: int, status: torch.Tensor) -> torch.Tensor:
+    """One Kraus channel on every trajectory of a batch (psi: n_traj states of
+    2^n amplitudes, back to back): each trajectory picks its operator from its
+    own status on the device (tq_traj_kraus).  Returns the chosen operator
+    index per trajectory (int32 device tensor)."""
+    mats = np.stack([np.asarray(k.detach().cpu().numpy() if hasattr(k, "detach") else k,
+                                dtype=np.complex128).reshape(2, 2) for k in ops])
+    kd = torch.from_numpy(np.stack([mats.real, mats.imag], axis=-1).reshape(len(ops), 8).copy()).to(psi.device)
+    st = status.to(device=psi.device, dtype=torch.float64).contiguous()
+    chosen = torch.empty(n_traj, dtype=torch.int32, device=psi.device)
+    lib = nat.load()
+    p, cap = _ws(lib.tq_traj_kraus_workspace_bytes(int(n), int(n_traj)), psi.device)
+    nat.call("tq_traj_kraus", _ptr(psi), int(n), int(n_traj), dtype_tag(psi), int(qubit), _ptr(kd), len(ops), _ptr(st),
+             _ptr(chosen), p, cap, stream_ptr(psi.device))
+    return chosen
+
+
 def inner_re(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     n = _check_state(a)
     _check_state(b, n)
