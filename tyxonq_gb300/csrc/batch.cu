@@ -447,6 +447,7 @@ extern "C" int tq_batch_run(int dtype, const tq_batch_inst* insts, const int32_t
                             const tq_tile_pass* passes, const tq_tile_op* ops, const tq_pauli_group* groups,
                             const tq_pauli_term* terms, const double* theta, void* pool, double* energies,
                             double* grads, int32_t* counter, void* stream) {
+  TQ_RANGE("tq_batch_run");
   if (dtype != TQ_C64 && dtype != TQ_C128) return fail(TQ_ERR_ARG, "tq_batch_run: bad dtype %d", dtype);
   if (n_work < 0) return fail(TQ_ERR_ARG, "tq_batch_run: negative work count");
   if (n_work == 0) return TQ_OK;

@@ -533,6 +533,7 @@ extern "C" int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const 
                                  int64_t n_partials, const double* sin_omc, const int64_t* row_ptr, const int32_t* col,
                                  const double* val, int grad, int threads, double* ket_out, double* out, void* ws,
                                  size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_ci_energy_grad");
   if (D < 1 || n_ex < 0 || init_index < 0 || init_index >= D || max_pairs < 0 || n_partials < 1)
     return fail(TQ_ERR_ARG, "tq_ci_energy_grad: D=%lld, n_ex=%d, init=%lld, max_pairs=%lld, n_partials=%lld",
                 (long long)D, n_ex, (long long)init_index, (long long)max_pairs, (long long)n_partials);
@@ -588,6 +589,7 @@ extern "C" int tq_ci_energy_grad(int64_t D, int64_t init_index, int n_ex, const 
 
 extern "C" int tq_sv_apply_excitations(void* psi, int n, int dtype, const tq_excitation* exc, int n_ex,
                                        const double* sincos, int reverse, void* stream) {
+  TQ_RANGE("tq_sv_apply_excitations");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_ex < 0 || n < 2) return fail(TQ_ERR_ARG, "tq_sv_apply_excitations: n=%d, n_ex=%d", n, n_ex);
@@ -613,6 +615,7 @@ extern "C" size_t tq_sv_excitation_adjoint_workspace_bytes(int n, int n_ex) {
 
 extern "C" int tq_sv_excitation_adjoint(void* psi, void* lam, int n, int dtype, const tq_excitation* exc, int n_ex,
                                         const double* sincos, double* grads, void* ws, size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_excitation_adjoint");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_ex < 0 || n < 2) return fail(TQ_ERR_ARG, "tq_sv_excitation_adjoint: n=%d, n_ex=%d", n, n_ex);

@@ -91,6 +91,20 @@ __host__ __device__ __forceinline__ int64_t insert_zero2(int64_t i, int plo, int
 }
 
 #ifndef __CUDACC_RTC__
+// ----------------------------------------------------------------- tracing
+// One NVTX range per entry point (kernel class): header-only NVTX v3, a no-op
+// unless a tool (nsys, ncu) is attached.
+}  // namespace tq
+#include <nvtx3/nvToolsExt.h>
+namespace tq {
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define TQ_RANGE(name) ::tq::NvtxRange tq_nvtx_range_(name)
+
 // ----------------------------------------------------------------- errors
 // Host-side error reporting: each failing entry point records a message that
 // tq_last_error() returns (thread-local, like errno).

@@ -351,6 +351,7 @@ extern "C" int tq_sv_init_basis(void* psi, int n, int dtype, int64_t basis, void
 }
 
 extern "C" int tq_sv_apply_1q(void* psi, int n, int dtype, int qubit, const double* u, void* stream) {
+  TQ_RANGE("tq_sv_apply_1q");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if ((rc = check_qubit(n, qubit))) return rc;
@@ -373,6 +374,7 @@ extern "C" int tq_sv_apply_1q(void* psi, int n, int dtype, int qubit, const doub
 }
 
 extern "C" int tq_sv_apply_diag1(void* psi, int n, int dtype, int qubit, const double* d, void* stream) {
+  TQ_RANGE("tq_sv_apply_diag1");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if ((rc = check_qubit(n, qubit))) return rc;
@@ -399,6 +401,7 @@ extern "C" int tq_sv_apply_diag1(void* psi, int n, int dtype, int qubit, const d
 }
 
 extern "C" int tq_sv_apply_2q(void* psi, int n, int dtype, int q0, int q1, const double* u, void* stream) {
+  TQ_RANGE("tq_sv_apply_2q");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if ((rc = check_qubit(n, q0)) || (rc = check_qubit(n, q1))) return rc;
@@ -448,17 +451,21 @@ static int perm2(void* psi, int n, int dtype, int q0, int q1, void* stream, cons
 }
 
 extern "C" int tq_sv_apply_cx(void* psi, int n, int dtype, int control, int target, void* stream) {
+  TQ_RANGE("tq_sv_apply_cx");
   return perm2<0>(psi, n, dtype, control, target, stream, "tq_sv_apply_cx");
 }
 extern "C" int tq_sv_apply_swap(void* psi, int n, int dtype, int q0, int q1, void* stream) {
+  TQ_RANGE("tq_sv_apply_swap");
   return perm2<1>(psi, n, dtype, q0, q1, stream, "tq_sv_apply_swap");
 }
 extern "C" int tq_sv_apply_cz(void* psi, int n, int dtype, int q0, int q1, void* stream) {
+  TQ_RANGE("tq_sv_apply_cz");
   return perm2<2>(psi, n, dtype, q0, q1, stream, "tq_sv_apply_cz");
 }
 
 extern "C" int tq_sv_apply_kq(void* psi, int n, int dtype, const int* qubits, int k, const double* u,
                               void* stream) {
+  TQ_RANGE("tq_sv_apply_kq");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (!psi || !qubits || !u) return fail(TQ_ERR_ARG, "NULL pointer");
@@ -494,6 +501,7 @@ extern "C" int tq_sv_apply_kq(void* psi, int n, int dtype, const int* qubits, in
 
 extern "C" int tq_sv_apply_pauli_rotation(void* psi, int n, int dtype, uint64_t x_mask, uint64_t z_mask,
                                           double theta, void* stream) {
+  TQ_RANGE("tq_sv_apply_pauli_rotation");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (!psi) return fail(TQ_ERR_ARG, "psi is NULL");

@@ -52,6 +52,7 @@ using namespace tq;
 
 extern "C" int tq_jit_build(const char* source, const char* const* include_dirs, int n_include_dirs, void** cubin,
                             size_t* cubin_size, char* log, size_t log_cap) {
+  TQ_RANGE("tq_jit_build");
   if (!source || !cubin || !cubin_size) return fail(TQ_ERR_ARG, "tq_jit_build: NULL argument");
   *cubin = nullptr;
   *cubin_size = 0;
@@ -144,6 +145,7 @@ extern "C" int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi
                                  int n_passes, const tq_tile_stage* stages_host, const tq_tile_stage* stages,
                                  const tq_tile_op* ops, int n_ops, const double* theta, void* ws, size_t ws_bytes,
                                  void* stream) {
+  TQ_RANGE("tq_jit_run_staged");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_passes <= 0) return TQ_OK;
@@ -225,6 +227,7 @@ extern "C" int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi
 extern "C" int tq_jit_wave_run(void* kernel, int kind, int dtype, const tq_wave_item* items, int n_items, int t,
                                const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
                                const double* theta, void* pool, double* partials, int max_ops, void* stream) {
+  TQ_RANGE("tq_jit_wave_run");
   if (!kernel || !items || !passes || !stages || !ops || !pool || (kind == 2 && !partials))
     return fail(TQ_ERR_ARG, "tq_jit_wave_run: NULL argument");
   if (kind != 0 && kind != 2) return fail(TQ_ERR_ARG, "tq_jit_wave_run: kind %d (0 forward, 2 adjoint)", kind);

@@ -470,10 +470,12 @@ static int inner_impl(const void* a, const void* b, int n, int dtype, double* ou
 
 extern "C" int tq_sv_norm2(const void* psi, int n, int dtype, double* out_dev, void* ws, size_t ws_bytes,
                            void* stream) {
+  TQ_RANGE("tq_sv_norm2");
   return inner_impl(psi, nullptr, n, dtype, out_dev, ws, ws_bytes, stream, "tq_sv_norm2");
 }
 extern "C" int tq_sv_inner_re(const void* a, const void* b, int n, int dtype, double* out_dev, void* ws,
                               size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_inner_re");
   if (!b) return fail(TQ_ERR_ARG, "tq_sv_inner_re: b is NULL");
   return inner_impl(a, b, n, dtype, out_dev, ws, ws_bytes, stream, "tq_sv_inner_re");
 }
@@ -488,6 +490,7 @@ extern "C" size_t tq_sv_expect_z_workspace_bytes(int n) {
 
 extern "C" int tq_sv_expect_z_all(const void* psi, int n, int dtype, double* out_dev, void* ws, size_t ws_bytes,
                                   void* stream) {
+  TQ_RANGE("tq_sv_expect_z_all");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n == 0) return TQ_OK;
@@ -515,6 +518,7 @@ extern "C" size_t tq_sv_qubit_rdm_workspace_bytes(int n) {
 
 extern "C" int tq_sv_qubit_rdm(const void* psi, int n, int dtype, int qubit, double* out_dev, void* ws,
                                size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_qubit_rdm");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if ((rc = check_qubit(n, qubit))) return rc;
@@ -536,6 +540,7 @@ extern "C" int tq_sv_qubit_rdm(const void* psi, int n, int dtype, int qubit, dou
 }
 
 extern "C" int tq_sv_probabilities(const void* psi, int n, int dtype, void* probs, void* stream) {
+  TQ_RANGE("tq_sv_probabilities");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (!psi || !probs) return fail(TQ_ERR_ARG, "tq_sv_probabilities: NULL pointer");
@@ -569,6 +574,7 @@ extern "C" size_t tq_sv_pauli_expectation_workspace_bytes(int n, int n_groups) {
 extern "C" int tq_sv_pauli_expectation(const void* psi, int n, int dtype, const tq_pauli_group* groups, int n_groups,
                                        const tq_pauli_term* terms, int n_terms, double* out_dev, void* ws,
                                        size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_pauli_expectation");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (!psi || !out_dev) return fail(TQ_ERR_ARG, "tq_sv_pauli_expectation: NULL pointer");
@@ -597,6 +603,7 @@ extern "C" int tq_sv_pauli_expectation(const void* psi, int n, int dtype, const 
 
 extern "C" int tq_sv_apply_pauli_sum(const void* psi, void* out, int n, int dtype, const tq_pauli_group* groups,
                                      int n_groups, const tq_pauli_term* terms, int n_terms, void* stream) {
+  TQ_RANGE("tq_sv_apply_pauli_sum");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (!psi || !out) return fail(TQ_ERR_ARG, "tq_sv_apply_pauli_sum: NULL pointer");
@@ -639,6 +646,7 @@ extern "C" size_t tq_sv_sample_workspace_bytes(int n, int64_t shots) {
 
 extern "C" int tq_sv_sample(const void* psi, int n, int dtype, int64_t shots, uint64_t seed, int64_t* out_indices,
                             void* ws, size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_sample");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (shots < 0) return fail(TQ_ERR_ARG, "tq_sv_sample: negative shots");

@@ -271,6 +271,7 @@ extern "C" int tq_sv_tile_max_bits(int dtype) { return (dtype == TQ_C64 || dtype
 
 extern "C" int tq_sv_run_tiles(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
                                const tq_tile_op* ops, const double* theta, void* stream) {
+  TQ_RANGE("tq_sv_run_tiles");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_passes < 0) return fail(TQ_ERR_ARG, "tq_sv_run_tiles: negative pass count");
@@ -290,6 +291,7 @@ extern "C" size_t tq_sv_adjoint_tiles_workspace_bytes(int n, int n_slots) {
 extern "C" int tq_sv_adjoint_tiles(void* psi, void* lam, int n, int dtype, const tq_tile_pass* passes, int n_passes,
                                    const tq_tile_op* ops, const double* theta, int n_slots, double* slot_out,
                                    void* ws, size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_adjoint_tiles");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_passes < 0 || n_slots < 0) return fail(TQ_ERR_ARG, "tq_sv_adjoint_tiles: negative count");
@@ -341,6 +343,7 @@ __global__ void k_generator_im(const typename C2<R>::T* psi, const typename C2<R
 
 extern "C" int tq_sv_generator_im(const void* psi, const void* lam, int n, int dtype, uint64_t xm, uint64_t zm,
                                   uint64_t cm, double* out_dev, void* ws, size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_generator_im");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (!psi || !lam || !out_dev) return fail(TQ_ERR_ARG, "tq_sv_generator_im: NULL pointer");
@@ -442,6 +445,7 @@ static int run_staged(void* psi, int n, const tq_tile_pass* passes, int n_passes
 extern "C" int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass* passes, int n_passes,
                                 const tq_tile_stage* stages, const tq_tile_op* ops, const double* theta,
                                 void* stream) {
+  TQ_RANGE("tq_sv_run_staged");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n_passes < 0) return fail(TQ_ERR_ARG, "tq_sv_run_staged: negative pass count");

@@ -151,6 +151,7 @@ extern "C" size_t tq_traj_kraus_workspace_bytes(int n, int n_traj) {
 extern "C" int tq_traj_kraus(void* psi, int n, int n_traj, int dtype, int qubit, const double* kraus_dev, int n_ops,
                              const double* status_dev, int32_t* chosen_dev, void* ws, size_t ws_bytes,
                              void* stream) {
+  TQ_RANGE("tq_traj_kraus");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n < 1) return fail(TQ_ERR_ARG, "tq_traj_kraus: a channel needs at least one qubit");

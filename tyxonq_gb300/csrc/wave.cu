@@ -553,6 +553,7 @@ extern "C" size_t tq_sv_pauli_sum_tiled_workspace_bytes(int n, int dtype, int n_
 extern "C" int tq_sv_pauli_sum_tiled(const void* psi, void* out, int n, int dtype, const tq_pauli_group* groups,
                                      int n_groups, const tq_pauli_term* terms, int n_terms, double* energy_out,
                                      void* ws, size_t ws_bytes, void* stream) {
+  TQ_RANGE("tq_sv_pauli_sum_tiled");
   int rc = check_n(n, dtype);
   if (rc) return rc;
   if (n < kTiledHb) return fail(TQ_ERR_ARG, "tq_sv_pauli_sum_tiled: n=%d below %d", n, kTiledHb);
@@ -610,6 +611,7 @@ extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n
                            const tq_tile_op* ops, const tq_pauli_group* groups, const tq_pauli_term* terms,
                            const double* theta, void* pool, double* partials, double* norm_partials,
                            int max_pass_ops, void* stream) {
+  TQ_RANGE("tq_wave_run");
   if (dtype != TQ_C64 && dtype != TQ_C128) return fail(TQ_ERR_ARG, "tq_wave_run: bad dtype %d", dtype);
   if (kind < 0 || kind > 2) return fail(TQ_ERR_ARG, "tq_wave_run: bad kind %d", kind);
   if (n_items < 0) return fail(TQ_ERR_ARG, "tq_wave_run: negative item count");
@@ -646,6 +648,7 @@ __global__ void k_wave_normalize(const double* __restrict__ norm_partials, const
 extern "C" int tq_wave_normalize(const double* norm_partials, const int32_t* first, const int32_t* count,
                                  const int32_t* inst, const int32_t* goff, const int32_t* gcount, int n_rows,
                                  double* energies, double* grads, void* stream) {
+  TQ_RANGE("tq_wave_normalize");
   if (n_rows < 0) return fail(TQ_ERR_ARG, "tq_wave_normalize: negative count");
   if (n_rows == 0) return TQ_OK;
   if (!norm_partials || !first || !count || !inst || !goff || !gcount || !energies || !grads)
@@ -659,6 +662,7 @@ extern "C" int tq_wave_normalize(const double* norm_partials, const int32_t* fir
 extern "C" int tq_wave_reduce(const double* partials, const int32_t* first, const int32_t* count,
                               const int32_t* stride, const double* scale, const int32_t* out_index, int n_out,
                               double* out, int accumulate, void* stream) {
+  TQ_RANGE("tq_wave_reduce");
   if (n_out < 0) return fail(TQ_ERR_ARG, "tq_wave_reduce: negative count");
   if (n_out == 0) return TQ_OK;
   if (!partials || !first || !count || !stride || !scale || !out_index || !out)
