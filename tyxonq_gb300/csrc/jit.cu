@@ -158,7 +158,8 @@ extern "C" int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi
   if (!ws || ws_bytes < need)
     return fail(TQ_ERR_WORKSPACE, "tq_jit_run_staged: workspace of %zu bytes, %zu needed", ws_bytes, need);
   if ((reinterpret_cast<uintptr_t>(ws) & 15) != 0) return fail(TQ_ERR_ARG, "tq_jit_run_staged: workspace not 16-byte aligned");
-  const int tmax = dtype == TQ_C64 ? 13 : 12;
+  // 5-bit stages hold twice the amplitudes per thread: one more tile bit
+  const int tmax = (dtype == TQ_C64 ? 13 : 12) + (stage_bits == 5 ? 1 : 0);
   for (int p = 0; p < n_passes; ++p) {
     const tq_tile_pass& tp = passes[p];
     if (tp.op_end == tp.op_begin) continue;
@@ -201,20 +202,28 @@ extern "C" int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi
     const int threads = 1 << (tp.t - stage_bits);
     const int64_t ntiles = int64_t(1) << (n - tp.t);
     cudaKernel_t k = static_cast<JitKernel*>(kernels[p])->kernel;
-    // occupancy with double buffering sets the grid; one buffer when every CTA owns one tile
-    size_t smem = dtype == TQ_C64 ? jit_smem_bytes<float>(tp.t, tp.nlow, nops, 1)
-                                  : jit_smem_bytes<double>(tp.t, tp.nlow, nops, 1);
-    cudaError_t e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem, dev);
+    // Buffering: double (the next tile streams in while a CTA computes) unless
+    // single buffers let more CTAs share an SM (then resident CTAs overlap each
+    // other's loads) or every CTA owns one tile.
+    const size_t smem1 = dtype == TQ_C64 ? jit_smem_bytes<float>(tp.t, tp.nlow, nops, 0)
+                                         : jit_smem_bytes<double>(tp.t, tp.nlow, nops, 0);
+    const size_t smem2 = dtype == TQ_C64 ? jit_smem_bytes<float>(tp.t, tp.nlow, nops, 1)
+                                         : jit_smem_bytes<double>(tp.t, tp.nlow, nops, 1);
+    if (smem1 > 227 * 1024)
+      return fail(TQ_ERR_ARG, "tq_jit_run_staged: pass %d needs %zu bytes of shared memory", p, smem1);
+    const bool dbuf_fits = smem2 <= 227 * 1024;
+    cudaError_t e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)(dbuf_fits ? smem2 : smem1), dev);
     if (e != cudaSuccess) return cuda_status(e, "tq_jit_run_staged: shared memory attribute");
-    int occ = 1;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, threads, smem);
+    int occ1 = 1, occ2 = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, (const void*)k, threads, smem1);
+    if (e == cudaSuccess && dbuf_fits) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void*)k, threads, smem2);
     if (e != cudaSuccess) return cuda_status(e, "tq_jit_run_staged: occupancy");
-    if (occ < 1) occ = 1;
+    if (occ1 < 1) occ1 = 1;
+    int dbuf = (dbuf_fits && occ2 >= 1 && occ2 >= occ1 && ntiles > (int64_t)sms * occ2) ? 1 : 0;
+    const int occ = dbuf ? occ2 : occ1;
+    const size_t smem = dbuf ? smem2 : smem1;
     const int64_t cap = (int64_t)sms * occ;
-    int dbuf = ntiles > cap ? 1 : 0;
-    if (!dbuf)
-      smem = dtype == TQ_C64 ? jit_smem_bytes<float>(tp.t, tp.nlow, nops, 0)
-                             : jit_smem_bytes<double>(tp.t, tp.nlow, nops, 0);
     const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
     void* rops = ws;
     void* args[] = {&psi, &n, &P, (void*)&stages, (void*)&ops, &rops, &dbuf};

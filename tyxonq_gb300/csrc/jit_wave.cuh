@@ -90,9 +90,11 @@ __device__ __forceinline__ void jit_wave_forward(const tq_wave_item* __restrict_
     T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
     __syncthreads();
     w_hoff(hoff, P);
-    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, false, false);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
+    // the tile streams in (cp.async) while the op records are compiled
+    if (I.basis_lo < 0) w_load<R>(s, psi, base, hoff, P);
+    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, false, false);
     if (I.basis_lo >= 0) {
       const int N = 1 << P.t;
       const int lm = (1 << P.nlow) - 1;
@@ -101,7 +103,6 @@ __device__ __forceinline__ void jit_wave_forward(const tq_wave_item* __restrict_
         s[pphys(j)] = cplx<R>(gi == (int64_t)I.basis_lo ? R(1) : R(0), R(0));
       }
     } else {
-      w_load<R>(s, psi, base, hoff, P);
       w_commit_wait();
     }
     __syncthreads();
@@ -139,12 +140,13 @@ __device__ __forceinline__ void jit_wave_adjoint(const tq_wave_item* __restrict_
     T2* lam = reinterpret_cast<T2*>(pool) + I.lam_off;
     __syncthreads();
     w_hoff(hoff, P);
-    for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = R(0);
-    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, true, true);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
+    // psi and lam tiles stream in (cp.async) while the op records are compiled
     w_load<R>(sp, psi, base, hoff, P);
     w_load<R>(sl, lam, base, hoff, P);
+    for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = R(0);
+    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, true, true);
     w_commit_wait();
     __syncthreads();
     body(sp, sl, rops, wpart, (uint64_t)base, nwarps, warp, lane);

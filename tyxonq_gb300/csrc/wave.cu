@@ -44,9 +44,11 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
     T2* psi = reinterpret_cast<T2*>(pool) + I.psi_off;
     __syncthreads();  // previous item's readers of s / hoff / rops are done
     w_hoff(hoff, P);
-    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, false, false);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
+    // the tile streams in (cp.async) while the op records are compiled
+    if (I.basis_lo < 0) w_load<R>(s, psi, base, hoff, P);
+    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, false, false);
     if (I.basis_lo >= 0) {
       // first pass of the instance: the tile of |basis> (psi was never written)
       const int N = 1 << P.t;
@@ -56,7 +58,6 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
         s[pphys(j)] = cplx<R>(gi == (int64_t)I.basis_lo ? R(1) : R(0), R(0));
       }
     } else {
-      w_load<R>(s, psi, base, hoff, P);
       w_commit_wait();
     }
     __syncthreads();
@@ -308,12 +309,13 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, RB == 3 ? 2 : 1)
     const double* th = theta + I.theta_off;
     __syncthreads();
     w_hoff(hoff, P);
-    for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = R(0);
-    rops_build<R>(rops, ops, op0, op0 + nops, th, true, true);
     __syncthreads();
     const int64_t base = w_base(I.tile, P);
+    // psi and lam tiles stream in (cp.async) while the op records are compiled
     w_load<R>(sp, psi, base, hoff, P);
     w_load<R>(sl, lam, base, hoff, P);
+    for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = R(0);
+    rops_build<R>(rops, ops, op0, op0 + nops, th, true, true);
     w_commit_wait();
     __syncthreads();
     for (int si = P.op_begin; si < P.op_end; ++si) {

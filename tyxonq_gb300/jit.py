@@ -406,7 +406,8 @@ def pass_source(t: int, body: str, double: bool, rb: int = 4) -> str:
         "}",
         "}  // namespace tq",
         "",
-        f'extern "C" __global__ void __launch_bounds__({1 << (t - rb)}, 1) {KERNEL_NAME}({T2}* psi, int n, '
+        f'extern "C" __global__ void __launch_bounds__({1 << (t - rb)}, {2 if (t - rb) <= 8 else 1}) '
+        f'{KERNEL_NAME}({T2}* psi, int n, '
         "const tq::PassArgs P, const tq_tile_stage* __restrict__ stages, "
         f"const tq_tile_op* __restrict__ ops, const tq::ROp<{R}>* __restrict__ rops_g, int dbuf) {{",
         f"  tq::jit_staged_forward<{R}>(psi, n, P, stages, rops_g, dbuf, "
@@ -490,8 +491,8 @@ def specialise(enc, dtype, device="cuda") -> JitStaged | None:
     when no pass qualifies (with stages wider than 4 bits: None unless every
     pass qualifies, since the library kernel takes at most 4)."""
     double = dtype == torch.complex128
-    tmax = 12 if double else 13
     rb = int(getattr(enc, "rb", 4))
+    tmax = (12 if double else 13) + (1 if rb == 5 else 0)
     srcs, where = [], []
     for pi in range(enc.n_passes):
         p = enc.passes[pi]
