@@ -100,16 +100,19 @@ def test_oversized_request_is_rejected_not_hung():
 
 @pytest.mark.gpu
 def test_results_same_alone_and_in_the_mix():
+    """Library kernels only (specialise=False): the mix changes no bit.  With
+    specialised kernels a session switches kernels once they are compiled, so
+    results then agree within the complex64 tolerance (next test)."""
     trace = make_trace(16, rate=1e6, seed=3, n_range=(10, 17), depth_range=(2, 4), terms_range=(20, 120),
                        grad_fraction=0.5, iterations=2)
     alone = {}
-    srv1 = VqeServer(max_inflight=1)
+    srv1 = VqeServer(max_inflight=1, specialise=False)
     for r in trace:
         rr = VqeRequest(r.session, r.n, r.structure, r.n_params, r.H, r.theta, r.grad)
         srv1.submit(rr)
         srv1.drain()
         alone[id(r)] = rr
-    srv = VqeServer(max_inflight=8)
+    srv = VqeServer(max_inflight=8, specialise=False)
     stats = replay(srv, trace)
     assert stats["errors"] == 0
     for r in trace:
@@ -125,6 +128,30 @@ def test_results_same_alone_and_in_the_mix():
         psi, _ = sv.run_ops(r.n, [(nm, *qs) if p is None else (nm, *qs, float(r.theta[p])) for nm, qs, p in r.structure])
         e_ref = sv.pauli_expectation(psi, r.H.codes, r.H.coeffs)
         assert abs(r.energy - e_ref) < 1e-5 * r.H.one_norm()
+
+
+@pytest.mark.gpu
+def test_specialised_sessions_match_the_oracle():
+    """Sessions whose kernels are compiled while they serve: every request of
+    a trace (three optimizer steps per session, 14-18 qubits, half with
+    gradients) against the oracle, complex64 tolerances (1e-5 absolute energies,
+    1e-4 gradients), and the kernels in place by the end."""
+    from oracle import sv
+
+    trace = make_trace(12, rate=1e6, seed=8, n_range=(14, 18), depth_range=(2, 3), terms_range=(20, 80),
+                       grad_fraction=0.5, iterations=3)
+    srv = VqeServer(max_inflight=4)
+    stats = replay(srv, trace)
+    assert stats["errors"] == 0
+    for sess in srv.sessions.values():
+        if sess.jit is not None:
+            assert sess.jit.result() > 0
+    for r in trace:
+        gates = [(nm, list(qs), p, 1.0) for nm, qs, p in r.structure]
+        e_ref, g_ref = sv.grad_adjoint(r.n, gates, r.theta, r.H.codes, r.H.coeffs)
+        assert abs(r.energy - e_ref) < 1e-5
+        if r.grad:
+            np.testing.assert_allclose(r.gradient, g_ref, atol=1e-4)
 
 
 def test_footprint_counts_tables_workspace_and_partials():

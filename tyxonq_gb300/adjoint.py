@@ -216,7 +216,10 @@ class _StagedReverse:
         ntile = 1 << (n - t)
         blocks, rows, base = [], [], 0
         self.runs = []  # (first item, item count) per adjoint pass
+        self.run_pids = []  # pass id of each run
+        self.kernels: dict = {}  # pass id -> specialised kernel (specialise())
         for pid, nops, pslots in enc["adj"]:
+            self.run_pids.append(pid)
             it = np.zeros(ntile, dtype=WAVE_ITEM_DTYPE)
             it["lam_off"] = N
             it["pass"] = pid
@@ -246,6 +249,10 @@ class _StagedReverse:
         pa = np.zeros(len(enc_plan.passes), dtype=PASS_DTYPE)
         for k, (tt, nl, b0, e0, pos) in enumerate(enc_plan.passes):
             pa[k] = (tt, nl, b0, e0, pos)
+        self._host = (np.concatenate(enc_plan.stages) if enc_plan.stages else np.zeros(0, STAGE_DTYPE),
+                      np.concatenate(enc_plan.ops) if enc_plan.ops else np.zeros(0, TILE_OP_DTYPE),
+                      list(enc_plan.passes))
+        self.device = torch.device(device)
         self.items_dev = _dev(items, device)
         self.passes_dev = _dev(pa, device)
         self.stages_dev = _dev(np.concatenate(enc_plan.stages) if enc_plan.stages else np.zeros(1, STAGE_DTYPE),
@@ -262,6 +269,20 @@ class _StagedReverse:
         self.grads = torch.zeros(max(n_params, 1), dtype=torch.float64, device=device)
         self.n_params = n_params
 
+    def specialise(self) -> int:
+        """Circuit-specialised kernels for the adjoint passes (4-bit stages);
+        returns how many passes have one.  Safe to call from another thread:
+        run() takes each kernel once it is in place."""
+        from . import jit
+
+        if self.rb != 4:
+            return 0
+        stages, ops, passes = self._host
+        rows = {pid: passes[pid] for pid in self.run_pids}
+        kern = jit.wave_kernels(2, self.t, stages, ops, rows, self.dt == 1, self.max_ops, self.device)
+        self.kernels = kern
+        return len(kern)
+
     def run(self, theta: torch.Tensor) -> torch.Tensor:
         from .waves import WAVE_ITEM_DTYPE
 
@@ -269,7 +290,15 @@ class _StagedReverse:
         st = K.stream_ptr(self.grads.device)
         isz = WAVE_ITEM_DTYPE.itemsize
         self.grads.zero_()
-        for first, count in self.runs:
+        kern = self.kernels
+        for (first, count), pid in zip(self.runs, self.run_pids):
+            k = kern.get(pid)
+            if k:
+                nat.call("tq_jit_wave_run", P(k), 2, self.dt, P(self.items_dev.data_ptr() + isz * first), count,
+                         self.t, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
+                         P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.pool.data_ptr()),
+                         P(self.partials.data_ptr()), self.max_ops, st)
+                continue
             nat.call("tq_wave_run", 2, self.dt, P(self.items_dev.data_ptr() + isz * first), count, self.t, 12,
                      self.rb, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
                      P(self.ops_dev.data_ptr()), None, None, P(theta.data_ptr()), P(self.pool.data_ptr()),
@@ -327,6 +356,7 @@ class ParametricEstimator:
                                 and cold <= STAGED_ADJOINT_MAX_COLD else None)
         self.psi = torch.empty(1 << self.n, dtype=dtype, device=self.device)
         self.lam = None
+        self._jit_ws: dict = {}  # this session's op-record workspaces of the specialised passes
 
     def footprint_bytes(self, grad: bool) -> int:
         """Device bytes a session of this estimator holds: see estimate_footprint."""
@@ -352,7 +382,20 @@ class ParametricEstimator:
             self.theta.copy_(torch.as_tensor(np.asarray(theta, dtype=np.float64)).reshape(-1), non_blocking=True)
         nat.call("tq_sv_init_basis", ctypes.c_void_p(self.psi.data_ptr()), self.n, K.dtype_tag(self.psi),
                  self.init_basis, K.stream_ptr(self.device))
-        return self.prog.forward.run(self.psi, self.theta)
+        return self.prog.forward.run(self.psi, self.theta, self._jit_ws)
+
+    def specialise(self) -> int:
+        """Circuit-specialised kernels for the forward passes and, when built,
+        the staged reverse sweep.  Meant to run on a worker thread while the
+        session already serves requests with the library kernels: each pass
+        switches to its specialised kernel once that is in place (the program
+        may be shared with other sessions; op records use this session's
+        workspace).  Returns the number of specialised passes."""
+        cnt = self.prog.forward.specialise(self.dtype, self.device, stage_bits=4)
+        staged = self._staged
+        if staged is not None:
+            cnt += staged.specialise()
+        return cnt
 
     def energy_async(self, theta) -> torch.Tensor:
         """Enqueue an energy evaluation on the current stream; returns a device

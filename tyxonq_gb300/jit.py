@@ -537,15 +537,25 @@ def specialise_wide(enc, dtype, device="cuda"):
     return wide
 
 
-def run_staged(js: JitStaged, enc, psi: torch.Tensor, n: int, dtag: int, theta_ptr, stream) -> None:
-    """Launch every pass of enc (specialised kernels; the interpreter for passes without one)."""
+def run_staged(js: JitStaged, enc, psi: torch.Tensor, n: int, dtag: int, theta_ptr, stream,
+               ws: dict | None = None) -> None:
+    """Launch every pass of enc (specialised kernels; the interpreter for passes
+    without one).  The op records of a call live in a workspace: `ws` (a dict
+    owned by the caller, keyed by segment) when given -- programs shared by
+    callers that run concurrently on different streams need one each -- else
+    the segment's own."""
     st_d, ops_d = enc.device_tables(psi.device)
     lib = nat.load()
     n_ops = len(enc.ops_host)
     need = int(lib.tq_jit_rops_bytes(dtag, n_ops))
-    if js.ws is None or js.ws.numel() < need or js.ws.device != psi.device:
-        js.ws = torch.empty(max(need, 16), dtype=torch.uint8, device=psi.device)
+    buf = ws.get(id(enc)) if ws is not None else js.ws
+    if buf is None or buf.numel() < need or buf.device != psi.device:
+        buf = torch.empty(max(need, 16), dtype=torch.uint8, device=psi.device)
+        if ws is not None:
+            ws[id(enc)] = buf
+        else:
+            js.ws = buf
     P = ctypes.c_void_p
     nat.call("tq_jit_run_staged", js.kernels, js.rb, P(psi.data_ptr()), n, dtag, enc.passes, enc.n_passes,
              enc.stages_host.ctypes.data_as(P), P(st_d.data_ptr()), P(ops_d.data_ptr()), n_ops, theta_ptr,
-             P(js.ws.data_ptr()), js.ws.numel(), stream)
+             P(buf.data_ptr()), buf.numel(), stream)

@@ -476,9 +476,11 @@ class ForwardProgram:
     n_gates: int
     n_passes: int
 
-    def run(self, psi: torch.Tensor, theta: torch.Tensor | None = None) -> torch.Tensor:
+    def run(self, psi: torch.Tensor, theta: torch.Tensor | None = None, ws: dict | None = None) -> torch.Tensor:
         """Apply the program in place; theta (float64 device tensor) feeds the
-        ops compiled with device-side angles."""
+        ops compiled with device-side angles.  ws: the caller's workspace dict
+        for the specialised passes' op records (needed when callers on
+        different streams share this program)."""
         from .engine import execute_plain
 
         dt = K.dtype_tag(psi)
@@ -489,7 +491,7 @@ class ForwardProgram:
             elif kind == "staged" and obj.jit is not None:
                 from . import jit
 
-                jit.run_staged(obj.jit, obj, psi, self.n, dt, th, K.stream_ptr(psi.device))
+                jit.run_staged(obj.jit, obj, psi, self.n, dt, th, K.stream_ptr(psi.device), ws)
             elif kind == "staged" and obj.rb > STAGE_BITS:  # pragma: no cover - never built without kernels
                 raise RuntimeError("a 5-bit staged segment needs its specialised kernels")
             elif kind == "staged":

@@ -83,7 +83,10 @@ def default_estimator_factory(req: VqeRequest, dtype, device):
             while len(_PROGRAMS) > _PROGRAMS_MAX:
                 _PROGRAMS.popitem(last=False)
     pg, prog = hit
-    return ParametricEstimator(req.n, pg, req.n_params, req.H, dtype=dtype, device=device, prog=prog)
+    est = ParametricEstimator(req.n, pg, req.n_params, req.H, dtype=dtype, device=device, prog=prog)
+    if req.grad:
+        est._ensure_staged()  # the reverse sweep's tables, here rather than on the serving loop
+    return est
 
 
 @dataclass
@@ -93,14 +96,18 @@ class _Session:
     busy: bool = False
     pending: deque = field(default_factory=deque)
     building: Future | None = None  # estimator under construction on the compile worker
+    jit: Future | None = None  # circuit-specialised kernels under construction
 
 
 class VqeServer:
     def __init__(self, device="cuda", dtype=torch.complex64, hbm_budget: int | None = None, max_inflight: int = 8,
                  estimator_factory: Callable | None = None, streams: Sequence | None = None,
-                 compile_workers: int = 1):
+                 compile_workers: int = 1, specialise: bool = True):
         """compile_workers > 0: new sessions' estimators are built on a worker
-        thread while the loop keeps admitting and polling other requests."""
+        thread while the loop keeps admitting and polling other requests.
+        specialise: each session's circuit-specialised kernels are compiled on
+        another worker thread; until they are in place its requests run the
+        library's kernels."""
         self.device = torch.device(device)
         self.dtype = dtype
         if hbm_budget is None:
@@ -117,6 +124,7 @@ class VqeServer:
         self.used = 0
         self.completed: list[VqeRequest] = []
         self.pool = ThreadPoolExecutor(compile_workers) if compile_workers > 0 else None
+        self.jit_pool = ThreadPoolExecutor(1) if specialise else None
 
     # ------------------------------------------------------------ memory
     def _footprint(self, req: VqeRequest) -> int:
@@ -202,6 +210,15 @@ class VqeServer:
         ev, e_h, sv_h = self._launch(sess, req, si)
         self.inflight.append((req, si, ev, e_h, sv_h, sess))
 
+    def _specialise(self, sess: _Session) -> None:
+        """Queue the session's kernel specialisation (once, and once more when its
+        reverse sweep appears after an energy-only start)."""
+        if self.jit_pool is None or not hasattr(sess.est, "specialise"):
+            return
+        staged = getattr(sess.est, "_staged", None)
+        if sess.jit is None or (sess.jit.done() and staged is not None and not staged.kernels):
+            sess.jit = self.jit_pool.submit(sess.est.specialise)
+
     def _launch(self, sess: _Session, req: VqeRequest, si: int):
         """Enqueue the request's device work on stream si; returns (event, host
         energy buffer, host slot-value buffer or None)."""
@@ -210,6 +227,7 @@ class VqeServer:
         with torch.cuda.stream(stream):
             if sess.est is None:
                 sess.est = self.factory(req, self.dtype, self.device)
+            self._specialise(sess)
             if req.grad:
                 e, sv = sess.est.energy_and_grad_async(req.theta)
             else:
