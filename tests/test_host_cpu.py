@@ -488,3 +488,60 @@ def test_staged_reverse_tables_cover_every_parametrised_op():
         lay = out[b:b + c]
         assert len(set(lay.tolist())) == len(lay)
     assert sorted(set(out.tolist())) == list(range(p))
+
+
+def test_specialised_sources_compile_with_nvrtc():
+    """Circuit-specialised kernels are generated on the host and compiled by the
+    library's NVRTC entry point (no GPU needed): a staged pass of a 28-qubit
+    random circuit (real, diagonal, i-symmetric and general 2x2 routines), the
+    same pass re-encoded with 5-bit stages, and the wave forward and adjoint
+    bodies of an HEA pass."""
+    import collections
+    import time
+
+    import torch
+
+    from tyxonq_gb300 import jit as J
+    from tyxonq_gb300.workloads import hea_rz_ops_params
+
+    class _C:
+        def __init__(self, n, o):
+            self.num_qubits, self.ops = n, o
+
+    gates, _ = lower_ops(_C(28, random_circuit(28, 40, seed=1)), mode="run")
+    prog = P.compile_forward(gates, 28, torch.complex64, t=13)
+    enc = [o for k, o in prog.segments if k == "staged"][0]
+    used = collections.Counter()
+    srcs = []
+    for pi in range(enc.n_passes):
+        lines = J._pass_body(enc.stages_host, enc.ops_host, enc.passes[pi], False, enc.stage_bits, 4)
+        assert lines is not None
+        for ln in lines:
+            used.update(re.findall(r"([a-z_0-9]+)<R, NR", ln))
+        if pi == 3:
+            srcs.append(J.pass_source(int(enc.passes[pi].t), "\n".join(lines), False, 4))
+    # real and diagonal single-qubit products take the cheap routines
+    assert used["j_ureal"] > 0 and used["r_d1"] > 0 and used["r_perm"] > 0
+    plans, g, params, slots, n = enc.source
+    wide = P.encode_staged(n, plans, g, params=params, rb=5)
+    p = wide.passes[0]
+    srcs.append(J.pass_source(int(p.t), "\n".join(J._pass_body(wide.stages_host, wide.ops_host, p, False,
+                                                                 wide.stage_bits, 5)), False, 5))
+    n = 16
+    struct = hea_rz_ops_params(n, 2)
+    th = np.random.default_rng(0).uniform(-1, 1, 64)
+    ops = [(nm, *qs) if pp is None else (nm, *qs, float(th[pp])) for nm, qs, pp in struct]
+    hg, _ = lower_ops(_C(n, ops), mode="run")
+    henc = [o for k, o in P.compile_forward(hg, n, torch.complex64, t=13).segments if k == "staged"][0]
+    hp = henc.passes[0]
+    row = (int(hp.t), 0, int(hp.op_begin), int(hp.op_end), 0)
+    srcs.append(J.wave_source(0, 13, "\n".join(J._pass_body(henc.stages_host, henc.ops_host, hp, False)), False))
+    srcs.append(J.wave_source(2, 13, "\n".join(J._adj_body(henc.stages_host, henc.ops_host, row, False, 10**6)),
+                              False))
+    from concurrent.futures import ThreadPoolExecutor
+
+    t0 = time.time()
+    with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        blobs = list(ex.map(J._build_cubin, srcs))
+    assert all(len(b) > 1000 for b in blobs)
+    assert time.time() - t0 < 300

@@ -11,6 +11,7 @@
 // and the fixed-order gradient partials are those of the library kernels.
 #pragma once
 
+#include "jit_staged.cuh"  // register routines shared with the staged passes
 #include "wave_io.cuh"
 
 namespace tq {

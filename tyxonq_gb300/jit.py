@@ -65,7 +65,7 @@ def _op_code(o, double: bool) -> tuple:
     kind = int(o["kind"])
     a, b = int(o["a"]), int(o["b"])
     if kind == TOP_U1:
-        return "u1", a
+        return _u1_routine(o, double)
     if kind == TOP_D1:
         if int(o["pidx"]) >= 0:
             return "dh", a
@@ -95,6 +95,65 @@ def _op_code(o, double: bool) -> tuple:
             return None, None  # the interpreter's (i & cm) == cm never holds: no-op
         return "prot", (xm, int(o["zm"]) & 15, int(o["cm"]))
     return None, None
+
+
+def _shape2(o, double: bool) -> str | None:
+    """Shape of the 2x2 an op contributes to a fused run, as the device builds
+    it (op_mat2): "diag" (off-diagonals zero), "real" (all entries real),
+    "dense", or None when the values are only known on the device."""
+    kind = int(o["kind"])
+    if kind == TOP_U1:
+        m = [_mat(o, e, double) for e in range(4)]
+        if m[1] == 0 and m[2] == 0:
+            return "diag"
+        return "real" if all(v.imag == 0 for v in m) else "dense"
+    if kind == TOP_D1:
+        if int(o["pidx"]) >= 0:
+            return "diag"
+        return "diag"
+    if kind == TOP_PROT:
+        xm, zm = int(o["xm"]) & 15, int(o["zm"]) & 15
+        if xm == 0:
+            return "diag"
+        if int(o["pidx"]) >= 0:
+            ny = bin(int(o["xm"]) & int(o["zm"])).count("1") & 3
+            return "real" if ny & 1 else "dense"
+        m = [_mat(o, e, double) for e in range(2)]
+        return "real" if all(v.imag == 0 for v in m) else "dense"
+    return None
+
+
+def _has_complex_diag(ops, k: int, j: int, double: bool) -> bool:
+    """Whether a diagonal factor of ops[k:k+j] may be complex (device angles or
+    complex entries): then a product with real factors is not real."""
+    for i in range(j):
+        o = ops[k + i]
+        if _shape2(o, double) != "diag":
+            continue
+        kind = int(o["kind"])
+        if kind == TOP_U1:
+            if _mat(o, 0, double).imag != 0 or _mat(o, 3, double).imag != 0:
+                return True
+        elif kind == TOP_D1:
+            if int(o["pidx"]) >= 0 or _mat(o, 0, double).imag != 0 or _mat(o, 1, double).imag != 0:
+                return True
+        else:
+            return True  # a Z rotation: c +- w with imaginary w
+    return False
+
+
+def _u1_routine(o, double: bool) -> tuple:
+    """Cheapest register routine for a fixed single-bit 2x2 (TOP_U1): the
+    record holds the matrix m0..m3."""
+    m = [_mat(o, e, double) for e in range(4)]
+    a = int(o["a"])
+    if m[1] == 0 and m[2] == 0:
+        return "d03", a
+    if all(v.imag == 0 for v in m):
+        return "ureal", a
+    if m[0] == m[3] and m[0].imag == 0 and m[1].real == 0 and m[2].real == 0:
+        return "ri", a
+    return "u1", a
 
 
 def _single_bit(o) -> int | None:
@@ -133,6 +192,10 @@ def _emit_op(lines: list, k_rel: int, o, routine: str, arg, signed: bool) -> Non
             call = f"r_d1<R, NR, {arg}>(x, r.m[0], r.m[1]);"
     elif routine == "dh":
         call = f"r_dh<R, NR, {arg}>(x, r.m[1]);"
+    elif routine == "d03":  # diagonal held as a dense 2x2: diag(m0, m3)
+        call = f"r_d1<R, NR, {arg}>(x, r.m[0], r.m[3]);"
+    elif routine == "ureal":
+        call = f"j_ureal<R, NR, {arg}>(x, r.m[0].x, r.m[1].x, r.m[2].x, r.m[3].x);"
     elif routine == "perm":
         mode, a, b = arg
         call = f"r_perm<R, NR, {mode}, {a}, {b}>(x);"
@@ -189,7 +252,15 @@ def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool, stage_bits:
                 j = 1
                 while j <= fuse and j < 16 and k + j < len(ops) and _single_bit(ops[k + j]) == K:
                     j += 1
-                _emit_op(lines, k - op0, o, "u1", K, False)
+                # the product's shape from its factors: diagonal or real products stay so
+                shapes = {_shape2(ops[k + i], double) for i in range(j)}
+                if shapes <= {"diag"}:
+                    routine = "d03"
+                elif shapes <= {"diag", "real"} and not ("diag" in shapes and _has_complex_diag(ops, k, j, double)):
+                    routine = "ureal"
+                else:
+                    routine = "u1"
+                _emit_op(lines, k - op0, o, routine, K, False)
                 k += j
                 continue
             routine, arg = _op_code(o, double)
@@ -250,6 +321,10 @@ def _emit_adj_op(lines: list, k_rel: int, o, double: bool) -> None:
                 body.append(f"r_d1<R, NR, {arg}>({arr}, r.m[0], r.m[1]);")
         elif routine == "dh":
             body.append(f"r_dh<R, NR, {arg}>({arr}, r.m[1]);")
+        elif routine == "d03":
+            body.append(f"r_d1<R, NR, {arg}>({arr}, r.m[0], r.m[3]);")
+        elif routine == "ureal":
+            body.append(f"j_ureal<R, NR, {arg}>({arr}, r.m[0].x, r.m[1].x, r.m[2].x, r.m[3].x);")
         elif routine == "perm":
             mode, a, b = arg
             body.append(f"r_perm<R, NR, {mode}, {a}, {b}>({arr});")
