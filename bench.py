@@ -521,6 +521,28 @@ def bench_single_gates(n: int, reps: int = 4) -> dict:
                      "sector_bytes": sum(sector_bytes) / len(sector_bytes),
                      "sector_gbs": sum(sector_bytes) / (sum(times) * 1e-3) / 1e9,
                      "qubit_pairs": pairs}
+    # dense k-qubit unitaries (k = 3..5) on spread qubits: 2^k complex MACs (8 * 2^k flops) per
+    # amplitude on the FP32 cores; GB/s over the read+write of every amplitude
+    rng = np.random.default_rng(9)
+    for k in (3, 4, 5):
+        d = 1 << k
+        uk = np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))[0]
+        mk, qk = K._mat(uk, d), nat.int_array(qs[:k])
+        for _ in range(2):
+            nat.call("tq_sv_apply_kq", P, n, 0, qk, k, mk, st)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(reps):
+            a, b = _events()
+            a.record()
+            nat.call("tq_sv_apply_kq", P, n, 0, qk, k, mk, st)
+            b.record()
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+        ms = sum(times) / len(times)
+        out[f"dense_{k}q"] = {"ms": ms, "alg_bytes": 2 * N * S, "gbs": 2 * N * S / (ms * 1e-3) / 1e9,
+                              "tflops": 8 * d * N / (ms * 1e-3) / 1e12, "launches": len(times),
+                              "qubits": qs[:k]}
     del psi
     torch.cuda.empty_cache()
     return out
