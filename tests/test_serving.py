@@ -204,3 +204,88 @@ def test_slow_estimator_builds_do_not_block_other_requests():
     srv.drain()
     assert slow.error is None and slow.energy == 8.0
 
+
+
+class _FakeBatcher:
+    """Micro-batch device work replaced by tickets (energy = n, gradient = 2 theta)."""
+
+    def __init__(self, res_max=12, delay=1):
+        self.res_max, self.delay = res_max, delay
+        self.sessions = {}
+        self.launched = []
+
+    def fits(self, n):
+        return n <= self.res_max
+
+    def table_bytes(self, n, n_gates, n_groups, n_terms):
+        return 1000
+
+    def register(self, key, n, structure, n_params, H):
+        self.sessions[key] = n
+        return n
+
+    def release_retired(self):
+        pass
+
+    def launch(self, items, stream):
+        self.launched.append([k for k, _ in items])
+        return {"event": {"left": self.delay}, "res": [(float(self.sessions[k]), np.asarray(t) * 2) for k, t in items]}
+
+    @staticmethod
+    def results(ticket):
+        return ticket["res"]
+
+
+def test_small_requests_are_coalesced_across_sessions():
+    """Waiting small requests of different sessions share one micro-batch;
+    requests of one session stay in order (one per batch); each request gets
+    its own results; large requests keep their own streams."""
+    srv = _FakeServer(hbm_budget=1 << 30, streams=[None] * 4, delay=1)
+    srv.batcher = _FakeBatcher()
+    reqs = []
+    for k in range(6):
+        r = VqeRequest(f"s{k}", 10 + (k % 3), [], 3, None, np.arange(3.0) + k, grad=(k % 2 == 0))
+        reqs.append(r)
+    reqs += [VqeRequest("s0", 10, [], 3, None, np.ones(3), grad=True)]  # second request of s0
+    big = _req("big", 16, grad=True)
+    for r in reqs + [big]:
+        srv.submit(r)
+    srv.drain()
+    assert all(r.error is None and r.done is not None for r in reqs + [big])
+    first = srv.batcher.launched[0]
+    assert sorted(first) == sorted(f"s{k}" for k in range(6))  # one launch for six sessions
+    assert srv.batcher.launched[1] == ["s0"]  # the same session's next request: the next batch
+    assert srv.batch_sizes == [6, 1]
+    for r in reqs:
+        assert r.energy == float(r.n)
+        if r.grad:
+            np.testing.assert_array_equal(r.gradient, np.asarray(r.theta) * 2)
+        else:
+            assert r.gradient is None
+    assert big.energy == 16.0  # through the per-request path
+    assert srv.used <= srv.budget
+
+
+@pytest.mark.gpu
+def test_coalesced_small_requests_match_the_oracle():
+    """Small requests (8-12 qubits) of many sessions evaluated in shared
+    micro-batches: every energy and gradient against the oracle (complex64
+    tolerances), and fewer launches than requests."""
+    from oracle import sv
+
+    trace = make_trace(48, rate=1e6, seed=11, n_range=(8, 12), depth_range=(2, 4), terms_range=(20, 120),
+                       grad_fraction=0.5, iterations=2)
+    srv = VqeServer(max_inflight=4)
+    assert srv.batcher is not None
+    stats = replay(srv, trace)
+    assert stats["errors"] == 0
+    assert stats["batched_requests"] == len(trace)
+    assert stats["micro_batches"] < len(trace)
+    for r in trace:
+        gates = [(nm, list(qs), p, 1.0) for nm, qs, p in r.structure]
+        e_ref, g_ref = sv.grad_adjoint(r.n, gates, r.theta, r.H.codes, r.H.coeffs)
+        assert abs(r.energy - e_ref) < 1e-5
+        if r.grad:
+            np.testing.assert_allclose(r.gradient, g_ref, atol=1e-4)
+        else:
+            assert r.gradient is None

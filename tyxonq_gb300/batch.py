@@ -296,13 +296,10 @@ class BatchedVQE:
         rparams = {Gn - 1 - gi: v for gi, v in params.items()}
         slots = {ri: rparams[ri][0] for ri in rparams}
         if not streamed:
-            allq = list(range(n - 1, -1, -1))  # bit 0 first: local bit = global bit
-            enc_f, _ = encode_passes(n, [PassPlan(allq, list(range(Gn)), n)], gates, fuse=True, params=params)
-            enc_a, _ = encode_passes(n, [PassPlan(allq, list(range(Gn)), n)], rgates, fuse=False, slots=slots,
-                                     params=rparams)
-            fb = self._add_ops(ops_all, enc_f.ops_host)
-            ab = self._add_ops(ops_all, enc_a.ops_host)
-            return fb, len(enc_f.ops_host), ab, len(enc_a.ops_host)
+            f_ops, a_ops = encode_resident(n, gates, params)
+            fb = self._add_ops(ops_all, f_ops)
+            ab = self._add_ops(ops_all, a_ops)
+            return fb, len(f_ops), ab, len(a_ops)
         out = []
         for which, gl, pr, sl in (("fwd", gates, params, None), ("adj", rgates, rparams, slots)):
             t = self.sched.t_fwd if which == "fwd" else self.sched.t_adj
@@ -446,6 +443,21 @@ class BatchedVQE:
             out.append(grads[o:o + p])
             o += p
         return out
+
+
+def encode_resident(n: int, gates: list, params: dict) -> tuple[np.ndarray, np.ndarray]:
+    """Op records of a shared-memory-resident instance: the forward list (runs of
+    single-qubit ops fused) and the adjoint list (reversed gates, slots =
+    parameter indices), bit positions global (the whole state is one tile)."""
+    rgates = list(reversed(gates))
+    Gn = len(gates)
+    rparams = {Gn - 1 - gi: v for gi, v in params.items()}
+    slots = {ri: rparams[ri][0] for ri in rparams}
+    allq = list(range(n - 1, -1, -1))  # bit 0 first: local bit = global bit
+    enc_f, _ = encode_passes(n, [PassPlan(allq, list(range(Gn)), n)], gates, fuse=True, params=params)
+    enc_a, _ = encode_passes(n, [PassPlan(allq, list(range(Gn)), n)], rgates, fuse=False, slots=slots,
+                             params=rparams)
+    return enc_f.ops_host, enc_a.ops_host
 
 
 def _to_dev(arr: np.ndarray, device) -> torch.Tensor:

@@ -13,8 +13,11 @@ over time.  The server
     estimator is built on a worker thread (the loop keeps admitting and
     polling), and sessions with the same circuit structure share one compiled
     program;
-  * enqueues every admitted request on its own CUDA stream, so the work of
-    requests that arrive while others run overlaps on the device, and
+  * gathers requests small enough for the shared-memory-resident classes
+    (up to 13 qubits) across sessions into micro-batches: one launch per
+    size class evaluates every waiting small request (coalesce.py);
+  * enqueues every other admitted request on its own CUDA stream, so the work
+    of requests that arrive while others run overlaps on the device, and
     completes requests by polling their events;
   * records arrival / admission / completion times for p50 / p99 latency.
 
@@ -97,17 +100,22 @@ class _Session:
     pending: deque = field(default_factory=deque)
     building: Future | None = None  # estimator under construction on the compile worker
     jit: Future | None = None  # circuit-specialised kernels under construction
+    small: bool = False  # tables in the micro-batch arenas (coalesce.ResidentBatcher)
 
 
 class VqeServer:
     def __init__(self, device="cuda", dtype=torch.complex64, hbm_budget: int | None = None, max_inflight: int = 8,
                  estimator_factory: Callable | None = None, streams: Sequence | None = None,
-                 compile_workers: int = 1, specialise: bool = True):
+                 compile_workers: int = 1, specialise: bool = True, coalesce: bool = True,
+                 max_batch: int = 256):
         """compile_workers > 0: new sessions' estimators are built on a worker
         thread while the loop keeps admitting and polling other requests.
         specialise: each session's circuit-specialised kernels are compiled on
         another worker thread; until they are in place its requests run the
-        library's kernels."""
+        library's kernels.
+        coalesce: requests small enough for the shared-memory-resident classes
+        (coalesce.ResidentBatcher) are gathered across sessions into
+        micro-batches of up to max_batch requests, one launch per size class."""
         self.device = torch.device(device)
         self.dtype = dtype
         if hbm_budget is None:
@@ -125,6 +133,22 @@ class VqeServer:
         self.completed: list[VqeRequest] = []
         self.pool = ThreadPoolExecutor(compile_workers) if compile_workers > 0 else None
         self.jit_pool = ThreadPoolExecutor(1) if specialise else None
+        self.batcher = None
+        if coalesce and self.device.type == "cuda":
+            from .coalesce import ResidentBatcher
+
+            self.batcher = ResidentBatcher(self.device, dtype)
+        self.max_batch = int(max_batch)
+        self.small_wait: list = []  # (req, sess) admitted, waiting for the next micro-batch
+        self.batches: list = []  # (stream slot, ticket, [(req, sess)])
+        self.batch_sizes: list[int] = []
+
+    def _small(self, req: VqeRequest) -> bool:
+        return self.batcher is not None and self.batcher.fits(req.n)
+
+    def busy(self) -> bool:
+        """Requests queued, waiting for a micro-batch or running."""
+        return bool(self.queue or self.inflight or self.small_wait or self.batches)
 
     # ------------------------------------------------------------ memory
     def _footprint(self, req: VqeRequest) -> int:
@@ -132,6 +156,12 @@ class VqeServer:
         H psi workspace and reverse-sweep partials (adjoint.estimate_footprint)."""
         from .adjoint import estimate_footprint
 
+        if self._small(req):
+            # states live in shared memory: the session's tables only, in the batcher's
+            # append-only arenas (twice the tables: an arena grows by doubling), once
+            if req.session in self.batcher.sessions:
+                return 0
+            return 2 * self.batcher.table_bytes(req.n, len(req.structure), req.H.n_groups, req.H.n_terms)
         n_param = sum(1 for _, _, p in req.structure if p is not None)
         return estimate_footprint(req.n, len(req.structure), n_param, req.H.n_groups, req.H.n_terms, req.grad,
                                   self.dtype)
@@ -141,7 +171,7 @@ class VqeServer:
             if self.used + need <= self.budget:
                 break
             s = self.sessions[key]
-            if not s.busy and not s.pending:
+            if not s.busy and not s.pending and not s.small:  # arena tables are never freed
                 self.used -= s.bytes
                 del self.sessions[key]
         return self.used + need <= self.budget
@@ -155,11 +185,15 @@ class VqeServer:
     def step(self) -> int:
         """Admit what fits, poll running work; returns the number completed now."""
         self._admit()
-        return self._poll()
+        done = self._poll()
+        if self.batcher is not None:
+            done += self._poll_batches()
+            self._launch_batch()
+        return done
 
     def drain(self, timeout: float = 600.0) -> None:
         t0 = time.perf_counter()
-        while self.queue or self.inflight:
+        while self.busy():
             if not self.step():
                 time.sleep(0.0002)
             if time.perf_counter() - t0 > timeout:
@@ -174,7 +208,8 @@ class VqeServer:
             if sess is not None and sess.busy:
                 keep.append(req)  # same-session requests run in order
                 continue
-            if not self.free_streams:
+            small = self._small(req)
+            if not small and not self.free_streams:
                 keep.append(req)
                 continue
             need = self._footprint(req)
@@ -193,7 +228,6 @@ class VqeServer:
 
     def _start(self, req: VqeRequest, need: int) -> None:
         sess = self.sessions.get(req.session)
-        si = self.free_streams.popleft()
         if sess is None:
             sess = _Session(None, 0)
             self.sessions[req.session] = sess
@@ -202,6 +236,17 @@ class VqeServer:
         self.sessions.move_to_end(req.session)
         sess.busy = True
         req.admitted = time.perf_counter()
+        if self._small(req):
+            sess.small = True
+            if sess.est is None and sess.building is None:
+                reg = (self.batcher.register, req.session, req.n, req.structure, req.n_params, req.H)
+                if self.pool is not None:
+                    sess.building = self.pool.submit(*reg)
+                else:
+                    sess.est = reg[0](*reg[1:])
+            self.small_wait.append((req, sess))
+            return
+        si = self.free_streams.popleft()
         if sess.est is None and self.pool is not None:
             # build off the loop; launched by _poll once the estimator exists
             sess.building = self.pool.submit(self.factory, req, self.dtype, self.device)
@@ -244,6 +289,59 @@ class VqeServer:
 
     def _ready(self, ev) -> bool:
         return ev.query()
+
+    # ------------------------------------------------------------ micro-batches
+    def _launch_batch(self) -> None:
+        """One micro-batch of every waiting small request whose session tables
+        are in place, on a free stream."""
+        if not self.small_wait or not self.free_streams:
+            return
+        ready, rest = [], []
+        for req, sess in self.small_wait:
+            if sess.est is None and sess.building is not None and sess.building.done():
+                try:
+                    sess.est = sess.building.result()
+                except Exception as exc:  # a session whose tables cannot be built fails its request
+                    req.error = f"{type(exc).__name__}: {exc}"
+                    req.done = time.perf_counter()
+                    sess.busy = False
+                    self.completed.append(req)
+                    sess.building = None
+                    continue
+                sess.building = None
+            if sess.est is not None and len(ready) < self.max_batch:
+                ready.append((req, sess))
+            else:
+                rest.append((req, sess))
+        self.small_wait = rest
+        if not ready:
+            return
+        if not self.batches:
+            self.batcher.release_retired()
+        si = self.free_streams.popleft()
+        ticket = self.batcher.launch([(r.session, r.theta) for r, _ in ready], self.streams[si])
+        self.batches.append((si, ticket, ready))
+        self.batch_sizes.append(len(ready))
+
+    def _poll_batches(self) -> int:
+        done = 0
+        still = []
+        for si, ticket, members in self.batches:
+            if not self._ready(ticket["event"]):
+                still.append((si, ticket, members))
+                continue
+            now = time.perf_counter()
+            for (req, sess), (e, g) in zip(members, self.batcher.results(ticket)):
+                req.energy = e
+                if req.grad:
+                    req.gradient = g
+                req.done = now
+                sess.busy = False
+                self.completed.append(req)
+                done += 1
+            self.free_streams.append(si)
+        self.batches = still
+        return done
 
     def _poll(self) -> int:
         done = 0
@@ -315,7 +413,7 @@ def replay(server: VqeServer, trace: Sequence[VqeRequest], timeout: float = 600.
     pending = deque(sorted(trace, key=lambda r: r.arrival))
     for r in pending:
         r.arrival = t0 + r.arrival
-    while pending or server.queue or server.inflight:
+    while pending or server.busy():
         now = time.perf_counter()
         while pending and pending[0].arrival <= now:
             server.submit(pending.popleft())
@@ -327,4 +425,6 @@ def replay(server: VqeServer, trace: Sequence[VqeRequest], timeout: float = 600.
     lat = np.array([r.latency for r in trace if r.error is None])
     return {"requests": len(trace), "errors": sum(r.error is not None for r in trace), "wall_s": wall,
             "throughput_rps": len(trace) / wall, "p50_ms": float(np.percentile(lat, 50) * 1e3),
-            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3)}
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+            "micro_batches": len(getattr(server, "batch_sizes", [])),
+            "batched_requests": int(sum(getattr(server, "batch_sizes", [])))}
