@@ -101,8 +101,10 @@ __device__ __forceinline__ void hpsi_one_term(cplx<R>* acc, const cplx<R>* pv, R
 // of the table (the host sorts them by m >> hb), and each distinct source tile
 // is copied once into shared memory, where every group that shares it reads
 // its partners.
+constexpr int kHpsiThreads = 256;  // every launch of k_wave_hpsi: output j = tid + 256 k
+
 template <typename R, int PER>
-__global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restrict__ items, int n_items, int hbits,
+__global__ void __launch_bounds__(kHpsiThreads) k_wave_hpsi(const tq_wave_item* __restrict__ items, int n_items, int hbits,
                                                    const tq_pauli_group* __restrict__ groups,
                                                    const tq_pauli_term* __restrict__ terms, void* pool,
                                                    void* lam_pool, double* partials, double* norm_partials) {
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
     cplx<R> acc[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) acc[k] = cplx<R>(0, 0);
-    const bool full = (HN >= PER * (int)blockDim.x);
+    const bool full = (HN == PER * kHpsiThreads);
     const int gend = I.group_begin + I.group_count;
     // source tiles double-buffered: the next run's tile streams in while this run computes
     auto issue = [&](cplx<R>* dst, int64_t h) {
@@ -146,14 +148,24 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
       cp_async_wait_group<1>();
       __syncthreads();
       for (; g < ge; ++g) {
-        const uint64_t m = __ldg(&groups[g].flip);
-        const int first = __ldg(&groups[g].first_term), cnt = __ldg(&groups[g].n_terms);
+        // the 16-byte group record {flip, first_term, n_terms} in one load
+        const int4 gr = __ldg(reinterpret_cast<const int4*>(&groups[g]));
+        const uint64_t m = (uint64_t)(uint32_t)gr.x | ((uint64_t)(uint32_t)gr.y << 32);
+        const int first = gr.z, cnt = gr.w;
         const int ml = (int)(m & (uint64_t)(HN - 1));
         cplx<R> pv[PER], W[PER];
+        if (full) {
+          // output j = tid | k << 8 (disjoint bits), so its partner j ^ ml is
+          // (tid ^ ml) ^ (k << 8): one XOR with a constant per amplitude
+          const int a0 = (int)threadIdx.x ^ ml;
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-          const int j = threadIdx.x + k * blockDim.x;
-          pv[k] = (full || j < HN) ? cb[j ^ ml] : cplx<R>(0, 0);
+          for (int k = 0; k < PER; ++k) pv[k] = cb[a0 ^ (k << 8)];
+        } else {
+#pragma unroll
+          for (int k = 0; k < PER; ++k) {
+            const int j = threadIdx.x + k * kHpsiThreads;
+            pv[k] = j < HN ? cb[j ^ ml] : cplx<R>(0, 0);
+          }
         }
         // src_k = (t0 | tid | k << 8) ^ m with disjoint bit fields (t0 is a multiple
         // of 2^hb = PER * 256), so parity(src_k & zy) = parity(((t0 | tid) ^ m) & zy)
@@ -239,7 +251,7 @@ __global__ void __launch_bounds__(256) k_wave_hpsi(const tq_wave_item* __restric
     R eloc = 0, nloc = 0;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-      const int j = threadIdx.x + k * blockDim.x;
+      const int j = threadIdx.x + k * kHpsiThreads;
       if (j < HN) {
         const T2 a = psi[t0 + j];
         eloc += a.x * acc[k].x + a.y * acc[k].y;
