@@ -519,13 +519,13 @@ def test_specialised_sources_compile_with_nvrtc():
         for ln in lines:
             used.update(re.findall(r"([a-z_0-9]+)<R, NR", ln))
         if pi == 3:
-            srcs.append(J.pass_source(int(enc.passes[pi].t), "\n".join(lines), False, 4))
+            srcs.append(J.pass_source(enc.passes[pi], "\n".join(lines), False, 4))
     # real and diagonal single-qubit products take the cheap routines
     assert used["j_ureal"] > 0 and used["r_d1"] > 0 and used["r_perm"] > 0
     plans, g, params, slots, n = enc.source
     wide = P.encode_staged(n, plans, g, params=params, rb=5)
     p = wide.passes[0]
-    srcs.append(J.pass_source(int(p.t), "\n".join(J._pass_body(wide.stages_host, wide.ops_host, p, False,
+    srcs.append(J.pass_source(p, "\n".join(J._pass_body(wide.stages_host, wide.ops_host, p, False,
                                                                  wide.stage_bits, 5)), False, 5))
     n = 16
     struct = hea_rz_ops_params(n, 2)

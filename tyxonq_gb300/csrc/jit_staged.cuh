@@ -84,6 +84,100 @@ __device__ __forceinline__ void j_prot(cplx<R>* x, cplx<R> c, cplx<R> w) {
   }
 }
 
+// Pass geometry known when the kernel is generated (struct G: tile bits T,
+// contiguous low bits NLOW, POS[k] = global bit of local bit k, THREADS).
+// Local index -> offset from the tile base: a bit deposit, so it is additive
+// over disjoint bit sets and a thread's part is computed once per kernel.
+template <typename G>
+__device__ __forceinline__ int64_t geo_off(int64_t j) {
+  int64_t off = j & ((int64_t(1) << G::NLOW) - 1);
+#pragma unroll
+  for (int k = G::NLOW; k < G::T; ++k) off |= ((j >> k) & 1) << G::POS[k];
+  return off;
+}
+
+// Global index of local index 0 of tile g (the tile's bits cleared).
+template <typename G>
+__device__ __forceinline__ int64_t geo_base(int64_t g) {
+  int64_t x = g << G::NLOW;
+#pragma unroll
+  for (int k = G::NLOW; k < G::T; ++k) x = insert_zero(x, G::POS[k]);
+  return x;
+}
+
+// The tile loop of one forward pass with the geometry compiled in: thread
+// tid moves the 16-byte chunks tid + i * THREADS (i < PER); chunk i's global
+// offset is the thread's part plus a constant and its shared-memory index the
+// thread's padded index plus a constant, so a chunk costs one copy instruction
+// and its address arithmetic folds into immediates.  Memory schedule and
+// shared-memory layout as jit_staged_forward (the offset table region is left
+// unused).
+template <typename R, typename G, typename Body>
+__device__ __forceinline__ void jit_staged_forward_g(typename C2<R>::T* psi, int n, const PassArgs& P,
+                                                     const tq_tile_stage* __restrict__ stages,
+                                                     const ROp<R>* __restrict__ rops_g, int dbuf, Body body) {
+  typedef typename C2<R>::T T2;
+  constexpr int A = 16 / sizeof(cplx<R>);
+  constexpr int NC = (1 << G::T) / A;
+  static_assert(NC % G::THREADS == 0, "chunks per tile must be a multiple of the threads");
+  constexpr int PER = NC / G::THREADS;
+  constexpr int S = A * G::THREADS;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int PT = padded_len(G::T);
+  cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem);
+  cplx<R>* buf1 = buf0 + (dbuf ? PT : 0);
+  ROp<R>* rops = reinterpret_cast<ROp<R>*>(smem + (size_t)(dbuf ? 2 : 1) * PT * sizeof(cplx<R>) +
+                                           staged_hoff_bytes(G::T, G::NLOW));
+  const int op0 = stages[P.op_begin].op_begin;
+  const int nwords = (stages[P.op_end - 1].op_end - op0) * (int)(sizeof(ROp<R>) / 16);
+  const uint4* src = reinterpret_cast<const uint4*>(rops_g + op0);
+  uint4* dst = reinterpret_cast<uint4*>(rops);
+  for (int w = threadIdx.x; w < nwords; w += blockDim.x) dst[w] = __ldg(&src[w]);
+  const int j0 = A * (int)threadIdx.x;
+  const int64_t toff = geo_off<G>(j0);
+  const int sp0 = pphys(j0);
+  auto load = [&](cplx<R>* s, int64_t base) {
+    const T2* gp = psi + base + toff;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) cp_async16(&s[sp0 + pphys(i * S)], &gp[geo_off<G>((int64_t)i * S)]);
+  };
+  auto store = [&](const cplx<R>* s, int64_t base) {
+    T2* gp = psi + base + toff;
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+      *reinterpret_cast<float4*>(&gp[geo_off<G>((int64_t)i * S)]) =
+          *reinterpret_cast<const float4*>(&s[sp0 + pphys(i * S)]);
+  };
+  __syncthreads();
+  const int64_t ntiles = int64_t(1) << (n - G::T);
+  int64_t g = blockIdx.x;
+  if (g < ntiles) load(buf0, geo_base<G>(g));
+  cp_async_commit();
+  int cur = 0;
+  for (; g < ntiles; g += gridDim.x) {
+    const int64_t gn = g + gridDim.x;
+    cplx<R>* s = cur ? buf1 : buf0;
+    if (dbuf) {
+      if (gn < ntiles) load(cur ? buf0 : buf1, geo_base<G>(gn));
+      cp_async_commit();
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
+    }
+    __syncthreads();
+    const int64_t gbase = geo_base<G>(g);
+    body(s, rops, (uint64_t)gbase);
+    store(s, gbase);
+    __syncthreads();
+    if (!dbuf && gn < ntiles) {
+      load(buf0, geo_base<G>(gn));
+      cp_async_commit();
+    }
+    cur ^= dbuf;
+  }
+  cp_async_wait_group<0>();
+}
+
 // The tile loop of one forward pass (same memory schedule as k_staged_forward:
 // persistent CTAs, cp.async double buffering when a CTA owns several tiles,
 // the pass's op records in shared memory).  body(s, rops, gbase) applies every

@@ -400,15 +400,23 @@ __global__ void k_wave_reduce(const double* __restrict__ partials, const int32_t
                               const int32_t* __restrict__ count, const int32_t* __restrict__ stride,
                               const double* __restrict__ scale, const int32_t* __restrict__ out_index, int n_out,
                               double* out, int accumulate) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_out; r += gridDim.x * blockDim.x) {
+  // one warp per output: lane l sums partials l, l + 32, ... in order, then a
+  // fixed shuffle tree (the same order on every launch)
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_out; r += warps) {
     double s = 0;
     const int f = first[r], c = count[r], st = stride[r];
-    for (int j = 0; j < c; ++j) s += partials[(int64_t)f + (int64_t)j * st];
-    s *= scale[r];
-    if (accumulate)
-      out[out_index[r]] += s;
-    else
-      out[out_index[r]] = s;
+    for (int j = lane; j < c; j += 32) s += partials[(int64_t)f + (int64_t)j * st];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      s *= scale[r];
+      if (accumulate)
+        out[out_index[r]] += s;
+      else
+        out[out_index[r]] = s;
+    }
   }
 }
 
@@ -646,16 +654,25 @@ extern "C" int tq_wave_run(int kind, int dtype, const tq_wave_item* items, int n
 // row r covers instance inst[r], whose norm partials are
 // norm_partials[first[r] .. first[r] + count[r]) (summed in order) and whose
 // gradient entries are grads[goff[r] .. goff[r] + gcount[r]).
+// One warp per row: lane l sums partials l, l + 32, ... in order, then a fixed
+// shuffle tree; the result does not depend on the launch, so replays are
+// bit-identical.
 __global__ void k_wave_normalize(const double* __restrict__ norm_partials, const int32_t* __restrict__ first,
                                  const int32_t* __restrict__ count, const int32_t* __restrict__ inst,
                                  const int32_t* __restrict__ goff, const int32_t* __restrict__ gcount, int n_rows,
                                  double* energies, double* grads) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_rows; r += warps) {
     double q = 0;
-    for (int j = 0; j < count[r]; ++j) q += norm_partials[first[r] + j];
+    const int f = first[r], c = count[r];
+    for (int j = lane; j < c; j += 32) q += norm_partials[f + j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
     const double inv = q > 0 ? 1.0 / q : 1.0;
-    energies[inst[r]] *= inv;
-    for (int j = 0; j < gcount[r]; ++j) grads[goff[r] + j] *= inv;
+    if (lane == 0) energies[inst[r]] *= inv;
+    const int g0 = goff[r], gc = gcount[r];
+    for (int j = lane; j < gc; j += 32) grads[g0 + j] *= inv;
   }
 }
 
@@ -667,8 +684,8 @@ extern "C" int tq_wave_normalize(const double* norm_partials, const int32_t* fir
   if (n_rows == 0) return TQ_OK;
   if (!norm_partials || !first || !count || !inst || !goff || !gcount || !energies || !grads)
     return fail(TQ_ERR_ARG, "tq_wave_normalize: NULL pointer");
-  k_wave_normalize<<<(n_rows + 127) / 128, 128, 0, (cudaStream_t)stream>>>(norm_partials, first, count, inst, goff,
-                                                                            gcount, n_rows, energies, grads);
+  k_wave_normalize<<<(n_rows + 3) / 4, 128, 0, (cudaStream_t)stream>>>(norm_partials, first, count, inst, goff,
+                                                                        gcount, n_rows, energies, grads);
   TQ_CHECK_LAUNCH("tq_wave_normalize");
   return TQ_OK;
 }
@@ -682,7 +699,8 @@ extern "C" int tq_wave_reduce(const double* partials, const int32_t* first, cons
   if (!partials || !first || !count || !stride || !scale || !out_index || !out)
     return fail(TQ_ERR_ARG, "tq_wave_reduce: NULL pointer");
   const int threads = 256;
-  const int grid = (n_out + threads - 1) / threads;
+  const int64_t want = ((int64_t)n_out * 32 + threads - 1) / threads;  // a warp per output
+  const int grid = (int)(want < 4096 ? want : 4096);
   k_wave_reduce<<<grid, threads, 0, (cudaStream_t)stream>>>(partials, first, count, stride, scale, out_index, n_out,
                                                             out, accumulate);
   TQ_CHECK_LAUNCH("tq_wave_reduce");

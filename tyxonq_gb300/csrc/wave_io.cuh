@@ -8,9 +8,12 @@
 
 namespace tq {
 
+// tmask: the global bits of local bits nlow .. t-1 (ascending), kept as one
+// mask so that the per-item deposits below run in registers (an indexed
+// position array would live in local memory).
 struct WPass {
   int t, nlow, op_begin, op_end;
-  int pos[TQ_TILE_MAX_BITS];
+  uint64_t tmask;
 };
 
 __device__ __forceinline__ WPass wload_pass(const tq_tile_pass* p) {
@@ -19,8 +22,11 @@ __device__ __forceinline__ WPass wload_pass(const tq_tile_pass* p) {
   s.nlow = p->nlow;
   s.op_begin = p->op_begin;
   s.op_end = p->op_end;
+  uint64_t m = 0;
 #pragma unroll
-  for (int i = 0; i < TQ_TILE_MAX_BITS; ++i) s.pos[i] = p->pos[i];
+  for (int i = 0; i < TQ_TILE_MAX_BITS; ++i)
+    if (i >= s.nlow && i < s.t) m |= uint64_t(1) << p->pos[i];
+  s.tmask = m;
   return s;
 }
 
@@ -28,8 +34,12 @@ __device__ __forceinline__ void w_hoff(int64_t* hoff, const WPass& P) {
   const int nh = 1 << (P.t - P.nlow);
   for (int h = threadIdx.x; h < nh; h += blockDim.x) {
     int64_t off = 0;
-    for (int k = 0; k < P.t - P.nlow; ++k)
-      if ((h >> k) & 1) off |= int64_t(1) << P.pos[P.nlow + k];
+    uint64_t m = P.tmask;
+    for (int k = 0; m; ++k) {
+      const uint64_t low = m & (~m + 1);  // lowest remaining tile bit
+      m ^= low;
+      if ((h >> k) & 1) off |= (int64_t)low;
+    }
     hoff[h] = off;
   }
 }
@@ -41,7 +51,7 @@ __host__ __device__ __forceinline__ size_t w_hoff_bytes(int t) { return sizeof(i
 
 __device__ __forceinline__ int64_t w_base(int64_t g, const WPass& P) {
   int64_t x = g << P.nlow;
-  for (int k = P.nlow; k < P.t; ++k) x = insert_zero(x, P.pos[k]);
+  for (uint64_t m = P.tmask; m; m &= m - 1) x = insert_zero(x, __ffsll((long long)m) - 1);
   return x;
 }
 

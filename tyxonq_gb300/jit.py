@@ -464,13 +464,22 @@ def cache_dir() -> Path:
     return Path(d) if d else Path.home() / ".cache" / "tyxonq_gb300" / "jit"
 
 
-def pass_source(t: int, body: str, double: bool, rb: int = 4) -> str:
+def pass_source(p, body: str, double: bool, rb: int = 4) -> str:
+    """Source of one staged pass kernel: p is the pass (TilePass: t, nlow, pos),
+    whose geometry is compiled in (tile loads and stores with constant
+    offsets)."""
     R = "double" if double else "float"
     T2 = "double2" if double else "float2"
+    t, nlow = int(p.t), int(p.nlow)
+    pos = [int(p.pos[k]) for k in range(t)]
     return "\n".join([
         '#include "jit_staged.cuh"',
         "",
         "namespace tq {",
+        "struct JitGeom {",
+        f"  static constexpr int T = {t}, NLOW = {nlow}, THREADS = {1 << (t - rb)};",
+        f"  static constexpr int POS[{t}] = {{{', '.join(map(str, pos))}}};",
+        "};",
         "template <typename R>",
         "__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ s, const ROp<R>* __restrict__ rops, "
         "const tq_tile_op* __restrict__ ops, uint64_t gbase) {",
@@ -485,7 +494,7 @@ def pass_source(t: int, body: str, double: bool, rb: int = 4) -> str:
         f'{KERNEL_NAME}({T2}* psi, int n, '
         "const tq::PassArgs P, const tq_tile_stage* __restrict__ stages, "
         f"const tq_tile_op* __restrict__ ops, const tq::ROp<{R}>* __restrict__ rops_g, int dbuf) {{",
-        f"  tq::jit_staged_forward<{R}>(psi, n, P, stages, rops_g, dbuf, "
+        f"  tq::jit_staged_forward_g<{R}, tq::JitGeom>(psi, n, P, stages, rops_g, dbuf, "
         f"[&](tq::cplx<{R}>* s, const tq::ROp<{R}>* rops, uint64_t gbase) "
         f"{{ tq::jit_body<{R}>(s, rops, ops, gbase); }});",
         "}",
@@ -576,7 +585,7 @@ def specialise(enc, dtype, device="cuda") -> JitStaged | None:
         lines = _pass_body(enc.stages_host, enc.ops_host, p, double, enc.stage_bits, rb)
         if lines is None:
             continue
-        srcs.append(pass_source(int(p.t), "\n".join(lines), double, rb))
+        srcs.append(pass_source(p, "\n".join(lines), double, rb))
         where.append(pi)
     if not srcs or (rb > 4 and len(srcs) < sum(1 for pi in range(enc.n_passes)
                                                if enc.passes[pi].op_end > enc.passes[pi].op_begin)):
