@@ -234,9 +234,26 @@ struct KqParams {
   cplx<R> u[(1 << K) * (1 << K)];
 };
 
+__device__ __forceinline__ void ld_pair(const cplx<float>* p, cplx<float>& a, cplx<float>& b) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  a = cplx<float>(v.x, v.y);
+  b = cplx<float>(v.z, v.w);
+}
+__device__ __forceinline__ void ld_pair(const cplx<double>* p, cplx<double>& a, cplx<double>& b) {
+  a = p[0];
+  b = p[1];
+}
+
+// The matrix is copied once per CTA into shared memory and read two entries per
+// 16-byte load (the same address in every lane: a broadcast); two accumulators
+// per output row halve the dependent FMA chain.  Rows are not unrolled (all 32
+// rows at once would need 32 accumulators next to the 32 inputs).
 template <typename R, int K>
 __global__ void k_kq(typename C2<R>::T* psi, int64_t items, const __grid_constant__ KqParams<R, K> P) {
   constexpr int D = 1 << K;
+  __shared__ __align__(16) cplx<R> su[D * D];
+  for (int e = threadIdx.x; e < D * D; e += blockDim.x) su[e] = P.u[e];
+  __syncthreads();
   GRID_STRIDE(v, items) {
     int64_t b = v;
 #pragma unroll
@@ -246,10 +263,16 @@ __global__ void k_kq(typename C2<R>::T* psi, int64_t items, const __grid_constan
     for (int j = 0; j < D; ++j) x[j] = ld<R>(psi, b + P.offs[j]);
 #pragma unroll 1
     for (int r = 0; r < D; ++r) {
-      cplx<R> acc(0, 0);
+      const cplx<R>* row = su + r * D;
+      cplx<R> a0(0, 0), a1(0, 0);
 #pragma unroll
-      for (int c = 0; c < D; ++c) acc = cfma(P.u[r * D + c], x[c], acc);
-      st<R>(psi, b + P.offs[r], acc);
+      for (int c = 0; c < D; c += 2) {
+        cplx<R> m0, m1;
+        ld_pair(row + c, m0, m1);
+        a0 = cfma(m0, x[c], a0);
+        a1 = cfma(m1, x[c + 1], a1);
+      }
+      st<R>(psi, b + P.offs[r], cplx<R>(a0.x + a1.x, a0.y + a1.y));
     }
   }
 }
@@ -327,7 +350,10 @@ static void launch_kq(void* psi, int n, const int* pos, const double* u, cudaStr
   for (int e = 0; e < D * D; ++e) P.u[e] = cplx<R>((R)u[2 * e], (R)u[2 * e + 1]);
   const int64_t items = (int64_t(1) << n) >> K;
   const int threads = (sizeof(R) == 8 && K >= 4) ? 64 : 128;
-  k_kq<R, K><<<grid_for(items, threads), threads, 0, s>>>((typename C2<R>::T*)psi, items, P);
+  // persistent-sized grid: every CTA copies the matrix once
+  unsigned grid = grid_for(items, threads);
+  if (grid > 152u * 16u) grid = 152u * 16u;
+  k_kq<R, K><<<grid, threads, 0, s>>>((typename C2<R>::T*)psi, items, P);
 }
 
 }  // namespace tq
