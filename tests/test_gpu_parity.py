@@ -389,3 +389,64 @@ def test_staged_single_state_reverse_sweep_matches_tile_passes(dtype, monkeypatc
             tm[k] -= 1e-4
             fd = (staged.energy(tp) - staged.energy(tm)) / 2e-4
             assert abs(fd - g[k]) < 1e-6, (k, fd, g[k])
+
+
+@pytest.mark.parametrize("dtype", [C128, C64])
+def test_tiled_pauli_sum_general_complex_weights(dtype):
+    """tq_sv_pauli_sum_tiled with term weights that are neither real nor
+    imaginary (the C tables accept any complex weight): groups of one term,
+    of a few terms and of many terms (the class-sum path), against
+    (H psi)_i = sum_t w_t (-1)^popc((i ^ flip) & zy_t) psi_(i ^ flip) on the host."""
+    from tyxonq_gb300 import _native as nat
+    from tyxonq_gb300 import kernels as K
+    from tyxonq_gb300.hamiltonian import random_pauli_sum, sort_terms_by_class
+
+    n = 14
+    rng = np.random.default_rng(21)
+    H = random_pauli_sum(n, 200, rng)
+    g, t = H.pack()
+    t = sort_terms_by_class(g, t, 12).copy()
+    # one group with many terms: the diagonal group (flip 0) gets extra Z strings
+    extra = np.zeros(9, dtype=t.dtype)
+    extra["zy"] = rng.integers(1, 1 << n, size=9, dtype=np.uint64)
+    g0 = g.copy()
+    if len(g0) == 0 or g0[0]["flip"] != 0:  # no diagonal group yet: add one in front
+        g0 = np.concatenate([np.zeros(1, dtype=g0.dtype), g0])
+    t = np.concatenate([t[:g0[0]["n_terms"]], extra, t[g0[0]["n_terms"]:]])
+    g0["first_term"][1:] += len(extra)
+    g0[0]["n_terms"] += len(extra)
+    t = sort_terms_by_class(g0, t, 12).copy()
+    phase = np.exp(1j * rng.uniform(0, 2 * np.pi, len(t)))
+    w = (np.where(t["w_re"] != 0, t["w_re"], 0.3) + 1j * t["w_im"]) * phase
+    t["w_re"], t["w_im"] = w.real, w.imag
+    t["f_re"], t["f_im"] = w.real, w.imag
+    assert (np.abs(w.real) > 0).all() and (np.abs(w.imag) > 0).all()
+    v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    v /= np.linalg.norm(v)
+    idx = np.arange(1 << n, dtype=np.uint64)
+    ref = np.zeros(1 << n, dtype=np.complex128)
+    for gi in range(len(g0)):
+        m = np.uint64(g0[gi]["flip"])
+        src = idx ^ m
+        for k in range(g0[gi]["first_term"], g0[gi]["first_term"] + g0[gi]["n_terms"]):
+            x = src & np.uint64(t[k]["zy"])
+            for sh in (32, 16, 8, 4, 2, 1):
+                x ^= x >> np.uint64(sh)
+            par = x & np.uint64(1)
+            ref += w[k] * np.where(par == 1, -1.0, 1.0) * v[src.astype(np.int64)]
+    psi = K.from_array(v, dtype=dtype)
+    out = torch.empty_like(psi)
+    e_dev = torch.empty(1, dtype=torch.float64, device="cuda")
+    gd = torch.from_numpy(np.frombuffer(g0.tobytes(), dtype=np.uint8).copy()).cuda()
+    td = torch.from_numpy(np.frombuffer(t.tobytes(), dtype=np.uint8).copy()).cuda()
+    lib = nat.load()
+    dt = K.dtype_tag(psi)
+    ws = torch.empty(int(lib.tq_sv_pauli_sum_tiled_workspace_bytes(n, dt, len(g0), 1)), dtype=torch.uint8,
+                     device="cuda")
+    nat.call("tq_sv_pauli_sum_tiled", K._ptr(psi), K._ptr(out), n, dt, K._ptr(gd), len(g0), K._ptr(td), len(t),
+             K._ptr(e_dev), K._ptr(ws), ws.numel(), K.stream_ptr(psi.device))
+    torch.cuda.synchronize()
+    nrm = float(np.abs(w).sum())
+    tol = 1e-11 * nrm if dtype == C128 else 1e-5 * nrm
+    np.testing.assert_allclose(out.cpu().numpy(), ref, atol=tol)
+    assert abs(float(e_dev.item()) - float(np.vdot(v, ref).real)) < tol

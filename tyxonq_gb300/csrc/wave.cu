@@ -102,6 +102,9 @@ __device__ __forceinline__ void hpsi_one_term(cplx<R>* acc, const cplx<R>* pv, R
 // is copied once into shared memory, where every group that shares it reads
 // its partners.
 constexpr int kHpsiThreads = 256;  // every launch of k_wave_hpsi: output j = tid + 256 k
+// Groups of up to this many terms apply each term with constant-sign FMAs; larger
+// ones sum the terms per sign class and take a Walsh-Hadamard transform.
+constexpr int kHpsiFewTerms = 4;
 
 template <typename R, int PER>
 __global__ void __launch_bounds__(kHpsiThreads) k_wave_hpsi(const tq_wave_item* __restrict__ items, int n_items, int hbits,
@@ -156,10 +159,13 @@ __global__ void __launch_bounds__(kHpsiThreads) k_wave_hpsi(const tq_wave_item* 
         cplx<R> pv[PER], W[PER];
         if (full) {
           // output j = tid | k << 8 (disjoint bits), so its partner j ^ ml is
-          // (tid ^ ml) ^ (k << 8): one XOR with a constant per amplitude
-          const int a0 = (int)threadIdx.x ^ ml;
+          // (tid ^ ml) ^ (k << 8); as a byte offset into the dynamic shared
+          // memory (source buffer base HN or 0 is a disjoint high bit), one XOR
+          // with a constant per amplitude and the buffer base an immediate
+          constexpr int SH = sizeof(cplx<R>) == 8 ? 3 : 4;
+          const int ab = ((((int)threadIdx.x ^ ml)) << SH) | ((buf ? HN : 0) << SH);
 #pragma unroll
-          for (int k = 0; k < PER; ++k) pv[k] = cb[a0 ^ (k << 8)];
+          for (int k = 0; k < PER; ++k) pv[k] = *reinterpret_cast<const cplx<R>*>(smem + (ab ^ (k << (8 + SH))));
         } else {
 #pragma unroll
           for (int k = 0; k < PER; ++k) {
@@ -172,40 +178,27 @@ __global__ void __launch_bounds__(kHpsiThreads) k_wave_hpsi(const tq_wave_item* 
         // XOR parity(k & c) with c = (zy >> 8) & (PER - 1): one popcount per term
         // and thread.
         const uint64_t sbase = (uint64_t)((t0 | (int64_t)threadIdx.x) ^ (int64_t)m);
-        const cplx<R> w1 = cnt == 1 ? term_w<R>(&terms[first]) : cplx<R>(0, 0);
-        if (cnt == 1 && (w1.x == R(0) || w1.y == R(0))) {
-          // one term (most groups of a random Pauli sum) with a real or imaginary
-          // weight (c * i^ny for real c): each amplitude takes two FMAs with a
-          // signed weight.  The sign of amplitude k is (-1)^(p0 + popc(k & c)):
-          // p0 per thread, c = the term's Z/Y bits among the k bits (the same for
-          // every thread), so one uniform switch over c selects code whose
-          // per-k signs are constants.  A general complex weight takes the path below.
-          const uint64_t zy = __ldg(&terms[first].zy);
-          const int p0 = __popcll(sbase & zy) & 1;
-          const int c = (int)(zy >> 8) & (PER - 1);
-          if (w1.y == R(0))
-            hpsi_one_term<R, PER, false>(acc, pv, p0 ? -w1.x : w1.x, c);
-          else
-            hpsi_one_term<R, PER, true>(acc, pv, p0 ? -w1.y : w1.y, c);
+        if (cnt <= kHpsiFewTerms) {
+          // few terms (most groups of a random Pauli sum have one): each term adds
+          // (-1)^(p0 + popc(k & c)) w pv[k] to amplitude k, p0 per thread and c =
+          // the term's Z/Y bits among the k bits (the same for every thread), so a
+          // uniform switch over c selects code whose per-k signs are constants; a
+          // real weight (or the real part) is two FMAs per amplitude, an imaginary
+          // one (or part) two more.  Weights c * i^ny of a Pauli sum are one or the
+          // other.
+          for (int tt = 0; tt < cnt; ++tt) {
+            const uint64_t zy = __ldg(&terms[first + tt].zy);
+            const cplx<R> w_ = term_w<R>(&terms[first + tt]);
+            const int p0 = __popcll(sbase & zy) & 1;
+            const int c = (int)(zy >> 8) & (PER - 1);
+            if (w_.x != R(0)) hpsi_one_term<R, PER, false>(acc, pv, p0 ? -w_.x : w_.x, c);
+            if (w_.y != R(0)) hpsi_one_term<R, PER, true>(acc, pv, p0 ? -w_.y : w_.y, c);
+          }
           continue;
         }
 #pragma unroll
         for (int k = 0; k < PER; ++k) W[k] = cplx<R>(0, 0);
-        if (cnt <= 2 || PER == 1) {
-          // few terms: signs per amplitude directly
-          for (int tt = 0; tt < cnt; ++tt) {
-            const uint64_t zy = __ldg(&terms[first + tt].zy);
-            const cplx<R> w_ = term_w<R>(&terms[first + tt]);
-            const R wr = w_.x, wi = w_.y;
-            const int p0 = __popcll(sbase & zy) & 1;
-            const int c = (int)(zy >> 8) & (PER - 1);
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-              const bool neg = (p0 ^ __popc(k & c)) & 1;
-              W[k] = cplx<R>(W[k].x + (neg ? -wr : wr), W[k].y + (neg ? -wi : wi));
-            }
-          }
-        } else {
+        {
           // many terms: sum per class c (W_c), then f_k = sum_c W_c (-1)^{popc(k & c)},
           // a PER-point Walsh-Hadamard transform.  Terms sorted by c make the class
           // switches rare; the result does not depend on the order.
