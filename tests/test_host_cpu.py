@@ -545,3 +545,28 @@ def test_specialised_sources_compile_with_nvrtc():
         blobs = list(ex.map(J._build_cubin, srcs))
     assert all(len(b) > 1000 for b in blobs)
     assert time.time() - t0 < 300
+
+
+def test_commuted_diagonals_preserve_the_state_and_meet_their_neighbours():
+    """commute_diagonals moves diagonal single-qubit gates only past gates they
+    commute with (CZ, CX on its control, other qubits, other diagonals): the
+    state is the oracle's for the original order, and most diagonals of the
+    28-qubit random-circuit generator end next to a single-qubit gate on their
+    qubit (so the encoder fuses them)."""
+    n = 9
+    gates, _ = lower_ops(_C(n, random_circuit(n, 24, seed=4)), mode="run")
+    order = P.commute_diagonals(gates)
+    assert sorted(order) == list(range(len(gates)))
+    psi0 = np.zeros(1 << n, dtype=np.complex128)
+    psi0[0] = 1
+    a, b = psi0.copy(), psi0.copy()
+    for g in gates:
+        a = _oracle_apply(a, g, n)
+    for i in order:
+        b = _oracle_apply(b, gates[i], n)
+    np.testing.assert_allclose(b, a, atol=1e-12)
+    moved = [gates[i] for i in order]
+    d1 = [k for k, g in enumerate(moved) if g.kind == "d1"]
+    near = sum(1 for k in d1 if any(0 <= k + d < len(moved) and moved[k + d].kind == "u1"
+                                    and moved[k + d].qubits == moved[k].qubits for d in (-1, 1)))
+    assert near >= len(d1) // 2

@@ -65,6 +65,53 @@ def _canon(g: Gate) -> Gate:
     return g
 
 
+# ---------------------------------------------------------------- diagonal commuting
+def _commutes_with_diag(h: Gate, q: int) -> bool:
+    """Whether gate h commutes exactly with any diagonal single-qubit gate on q."""
+    if q not in h.qubits:
+        return True
+    if h.kind in ("d1", "cz"):
+        return True
+    return h.kind == "cx" and h.qubits[0] == q  # a diagonal on the control commutes
+
+
+def _is_1q_on(h: Gate, q: int) -> bool:
+    return h.kind in ("u1", "d1") and len(h.qubits) == 1 and h.qubits[0] == q
+
+
+def commute_diagonals(gates: Sequence[Gate]) -> list[int]:
+    """An execution order in which each diagonal single-qubit gate sits next to
+    a single-qubit gate on the same qubit whenever only gates it commutes with
+    (gates on other qubits, CZ, CX controlled by it, other diagonals) stand
+    between them: first moved back to the previous such gate, else forward to
+    the next one.  Adjacent single-qubit gates on one qubit are fused into one
+    2x2 by the pass encoder, so each move removes one register routine.  The
+    order is a list of gate indices; the state it produces equals the
+    original's up to rounding."""
+    def backward(order: list[int], skip_merged: bool) -> list[int]:
+        out: list[int] = []
+        for gi in order:
+            g = gates[gi]
+            if g.kind == "d1" and len(g.qubits) == 1:
+                q = g.qubits[0]
+                if skip_merged and out and _is_1q_on(gates[out[-1]], q):
+                    out.append(gi)
+                    continue
+                j = len(out) - 1
+                while j >= 0 and not _is_1q_on(gates[out[j]], q) and _commutes_with_diag(gates[out[j]], q):
+                    j -= 1
+                if j >= 0 and _is_1q_on(gates[out[j]], q):
+                    out.insert(j + 1, gi)
+                    continue
+            out.append(gi)
+        return out
+
+    order = backward(list(range(len(gates))), False)
+    # forward moves: the same scan on the reversed order (merged diagonals stay)
+    rev = backward(order[::-1], True)
+    return rev[::-1]
+
+
 # ---------------------------------------------------------------- planning
 @dataclass
 class PassPlan:
@@ -725,6 +772,13 @@ def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int
     if any(g.kind == "kraus" for g in gates):
         raise NotImplementedError("Kraus channels are stochastic steps between programs (GpuStatevectorEngine)")
     gates = [_canon(g) for g in gates]
+    if fuse:
+        order = commute_diagonals(gates)
+        if order != list(range(len(gates))):
+            gates = [gates[i] for i in order]
+            if params is not None:
+                where = {old: new for new, old in enumerate(order)}
+                params = {where[gi]: v for gi, v in params.items()}
     if t is None:
         t = default_tile_bits(n, dtype)
     t = min(t, n)
