@@ -111,7 +111,8 @@ __device__ __forceinline__ int64_t geo_base(int64_t g) {
 // thread's padded index plus a constant, so a chunk costs one copy instruction
 // and its address arithmetic folds into immediates.  Memory schedule and
 // shared-memory layout as jit_staged_forward (the offset table region is left
-// unused).
+// unused).  body(s, rops, gbase, on_free, gt): with G::DIRECT the body's last
+// stage stores to gt = psi + gbase and calls on_free once its inputs are read.
 template <typename R, typename G, typename Body>
 __device__ __forceinline__ void jit_staged_forward_g(typename C2<R>::T* psi, int n, const PassArgs& P,
                                                      const tq_tile_stage* __restrict__ stages,
@@ -166,12 +167,25 @@ __device__ __forceinline__ void jit_staged_forward_g(typename C2<R>::T* psi, int
     }
     __syncthreads();
     const int64_t gbase = geo_base<G>(g);
-    body(s, rops, (uint64_t)gbase);
-    store(s, gbase);
-    __syncthreads();
-    if (!dbuf && gn < ntiles) {
-      load(buf0, geo_base<G>(gn));
-      cp_async_commit();
+    if constexpr (G::DIRECT) {
+      // the body's last stage reads its registers, calls on_free (a single
+      // buffer then takes the next tile while the stage computes) and stores
+      // its results to psi itself
+      auto on_free = [&]() {
+        if (!dbuf && gn < ntiles) {
+          load(buf0, geo_base<G>(gn));
+          cp_async_commit();
+        }
+      };
+      body(s, rops, (uint64_t)gbase, on_free, psi + gbase);
+    } else {
+      body(s, rops, (uint64_t)gbase, []() {}, psi + gbase);
+      store(s, gbase);
+      __syncthreads();
+      if (!dbuf && gn < ntiles) {
+        load(buf0, geo_base<G>(gn));
+        cp_async_commit();
+      }
     }
     cur ^= dbuf;
   }

@@ -211,11 +211,37 @@ def _emit_op(lines: list, k_rel: int, o, routine: str, arg, signed: bool) -> Non
     lines.append(f"    {{ {pre}{call} }}")
 
 
+def _geo_off(j: int, nlow: int, pos: list) -> int:
+    """Offset from the tile base of local index j (the device's geo_off)."""
+    off = j & ((1 << nlow) - 1)
+    for k in range(nlow, len(pos)):
+        if (j >> k) & 1:
+            off |= 1 << pos[k]
+    return off
+
+
+# The last stage stores its registers straight to global memory when none of its
+# register bits is below this one (each warp store then covers whole 32-byte sectors).
+DIRECT_MIN_BIT = 2
+
+
+def direct_last_ok(stages: np.ndarray, p, stage_bits: list | None = None) -> bool:
+    """Whether pass p's last stage may store its registers directly to global memory."""
+    se = int(p.op_end)
+    if se <= int(p.op_begin):
+        return False
+    bits = [int(v) for v in (stage_bits[se - 1] if stage_bits is not None else stages[se - 1]["bits"])]
+    return all(v >= DIRECT_MIN_BIT for v in bits)
+
+
 def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool, stage_bits: list | None = None,
-               rb: int = 4) -> list[str] | None:
+               rb: int = 4, direct_geo: tuple | None = None) -> list[str] | None:
     """Body lines of one pass (stages[p.op_begin:p.op_end]) with rb-bit register
     stages (stage_bits: every stage's bits, needed for rb > 4), or None if the
-    interpreter must run it."""
+    interpreter must run it.  direct_geo = (nlow, pos): the last stage reads its
+    registers, releases the tile buffer (barrier, then on_free() issues the next
+    tile's load) and stores its results straight to the tile in global memory
+    (gt) at offsets from the compiled-in geometry."""
     NR = 1 << rb
     sb, se = int(p.op_begin), int(p.op_end)
     if se <= sb:
@@ -243,6 +269,10 @@ def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool, stage_bits:
                     j |= 1 << bits[k]
             offs.append(_pphys(j))
         lines.append("    " + " ".join(f"x[{i}] = s[p0 + {offs[i]}];" for i in range(NR)))
+        last_direct = direct_geo is not None and si == se - 1
+        if last_direct:
+            lines.append("    __syncthreads();  // every register read: the buffer takes the next tile")
+            lines.append("    on_free();")
         k, k1 = int(st["op_begin"]), int(st["op_end"])
         while k < k1:
             o = ops[k]
@@ -267,8 +297,20 @@ def _pass_body(stages: np.ndarray, ops: np.ndarray, p, double: bool, stage_bits:
             signed = bool(int(o["zo"]) or int(o["zg"]))
             _emit_op(lines, k - op0, o, routine, arg, signed)
             k += 1
-        lines.append("    " + " ".join(f"s[p0 + {offs[i]}] = x[{i}];" for i in range(NR)))
-        lines.append("    __syncthreads();")
+        if last_direct:
+            nlow, pos = direct_geo
+            gofs = []
+            for i in range(NR):
+                j = 0
+                for kk in range(rb):
+                    if (i >> kk) & 1:
+                        j |= 1 << bits[kk]
+                gofs.append(_geo_off(j, nlow, pos))
+            lines.append("    const int64_t g0 = geo_off<JitGeom>(b);")
+            lines.append("    " + " ".join(f"gt[g0 + {gofs[i]}LL] = {{x[{i}].x, x[{i}].y}};" for i in range(NR)))
+        else:
+            lines.append("    " + " ".join(f"s[p0 + {offs[i]}] = x[{i}];" for i in range(NR)))
+            lines.append("    __syncthreads();")
         lines.append("  }")
     return lines
 
@@ -464,10 +506,11 @@ def cache_dir() -> Path:
     return Path(d) if d else Path.home() / ".cache" / "tyxonq_gb300" / "jit"
 
 
-def pass_source(p, body: str, double: bool, rb: int = 4) -> str:
+def pass_source(p, body: str, double: bool, rb: int = 4, direct: bool = False) -> str:
     """Source of one staged pass kernel: p is the pass (TilePass: t, nlow, pos),
     whose geometry is compiled in (tile loads and stores with constant
-    offsets)."""
+    offsets); direct: the body's last stage stores to global memory itself
+    (_pass_body with direct_geo)."""
     R = "double" if double else "float"
     T2 = "double2" if double else "float2"
     t, nlow = int(p.t), int(p.nlow)
@@ -478,11 +521,12 @@ def pass_source(p, body: str, double: bool, rb: int = 4) -> str:
         "namespace tq {",
         "struct JitGeom {",
         f"  static constexpr int T = {t}, NLOW = {nlow}, THREADS = {1 << (t - rb)};",
+        f"  static constexpr bool DIRECT = {'true' if direct else 'false'};",
         f"  static constexpr int POS[{t}] = {{{', '.join(map(str, pos))}}};",
         "};",
-        "template <typename R>",
+        "template <typename R, typename F>",
         "__device__ __forceinline__ void jit_body(cplx<R>* __restrict__ s, const ROp<R>* __restrict__ rops, "
-        "const tq_tile_op* __restrict__ ops, uint64_t gbase) {",
+        "const tq_tile_op* __restrict__ ops, uint64_t gbase, F&& on_free, typename C2<R>::T* __restrict__ gt) {",
         "  const int tid = threadIdx.x;",
         f"  constexpr int NR = {1 << rb};",
         "  cplx<R> x[NR];",
@@ -495,8 +539,8 @@ def pass_source(p, body: str, double: bool, rb: int = 4) -> str:
         "const tq::PassArgs P, const tq_tile_stage* __restrict__ stages, "
         f"const tq_tile_op* __restrict__ ops, const tq::ROp<{R}>* __restrict__ rops_g, int dbuf) {{",
         f"  tq::jit_staged_forward_g<{R}, tq::JitGeom>(psi, n, P, stages, rops_g, dbuf, "
-        f"[&](tq::cplx<{R}>* s, const tq::ROp<{R}>* rops, uint64_t gbase) "
-        f"{{ tq::jit_body<{R}>(s, rops, ops, gbase); }});",
+        f"[&](tq::cplx<{R}>* s, const tq::ROp<{R}>* rops, uint64_t gbase, auto&& on_free, {T2}* gt) "
+        f"{{ tq::jit_body<{R}>(s, rops, ops, gbase, on_free, gt); }});",
         "}",
         "",
     ])
@@ -582,10 +626,12 @@ def specialise(enc, dtype, device="cuda") -> JitStaged | None:
         p = enc.passes[pi]
         if not (9 <= int(p.t) <= tmax) or int(p.t) - rb < 5:
             continue
-        lines = _pass_body(enc.stages_host, enc.ops_host, p, double, enc.stage_bits, rb)
+        direct = direct_last_ok(enc.stages_host, p, enc.stage_bits)
+        geo = (int(p.nlow), [int(p.pos[k]) for k in range(int(p.t))]) if direct else None
+        lines = _pass_body(enc.stages_host, enc.ops_host, p, double, enc.stage_bits, rb, direct_geo=geo)
         if lines is None:
             continue
-        srcs.append(pass_source(p, "\n".join(lines), double, rb))
+        srcs.append(pass_source(p, "\n".join(lines), double, rb, direct=direct))
         where.append(pi)
     if not srcs or (rb > 4 and len(srcs) < sum(1 for pi in range(enc.n_passes)
                                                if enc.passes[pi].op_end > enc.passes[pi].op_begin)):
