@@ -251,9 +251,12 @@ __device__ __forceinline__ void ld_pair(const cplx<double>* p, cplx<double>& a, 
 template <typename R, int K>
 __global__ void k_kq(typename C2<R>::T* psi, int64_t items, const __grid_constant__ KqParams<R, K> P) {
   constexpr int D = 1 << K;
-  __shared__ __align__(16) cplx<R> su[D * D];
-  for (int e = threadIdx.x; e < D * D; e += blockDim.x) su[e] = P.u[e];
-  __syncthreads();
+  constexpr bool SMEM = K >= 4;  // up to 8x8 the constant-bank operands measured faster
+  __shared__ __align__(16) cplx<R> su[SMEM ? D * D : 2];
+  if constexpr (SMEM) {
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) su[e] = P.u[e];
+    __syncthreads();
+  }
   GRID_STRIDE(v, items) {
     int64_t b = v;
 #pragma unroll
@@ -261,6 +264,16 @@ __global__ void k_kq(typename C2<R>::T* psi, int64_t items, const __grid_constan
     cplx<R> x[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) x[j] = ld<R>(psi, b + P.offs[j]);
+    if constexpr (!SMEM) {
+#pragma unroll 1
+      for (int r = 0; r < D; ++r) {
+        cplx<R> acc(0, 0);
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc = cfma(P.u[r * D + c], x[c], acc);
+        st<R>(psi, b + P.offs[r], acc);
+      }
+      continue;
+    }
 #pragma unroll 1
     for (int r = 0; r < D; ++r) {
       const cplx<R>* row = su + r * D;
@@ -350,9 +363,9 @@ static void launch_kq(void* psi, int n, const int* pos, const double* u, cudaStr
   for (int e = 0; e < D * D; ++e) P.u[e] = cplx<R>((R)u[2 * e], (R)u[2 * e + 1]);
   const int64_t items = (int64_t(1) << n) >> K;
   const int threads = (sizeof(R) == 8 && K >= 4) ? 64 : 128;
-  // persistent-sized grid: every CTA copies the matrix once
+  // persistent-sized grid where every CTA copies the matrix once
   unsigned grid = grid_for(items, threads);
-  if (grid > 152u * 16u) grid = 152u * 16u;
+  if (K >= 4 && grid > 152u * 16u) grid = 152u * 16u;
   k_kq<R, K><<<grid, threads, 0, s>>>((typename C2<R>::T*)psi, items, P);
 }
 
