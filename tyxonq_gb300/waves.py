@@ -55,6 +55,9 @@ def _dev(arr: np.ndarray, device) -> torch.Tensor:
     return torch.frombuffer(bytearray(arr.tobytes() or b"\0" * 16), dtype=torch.uint8).to(device)
 
 
+MAX_FORK = 8  # side-by-side sub-launches of one wave launch
+
+
 class WavePlan:
     def __init__(self, entries, dtype, device, t: int = 12, hbits: int = 12, budget: int = 48 << 20,
                  max_ops: int = 256, lanes: int = 1, adj_stage_bits: int = 4, jit: bool = False):
@@ -179,6 +182,8 @@ class WavePlan:
         # circuit-specialised kernels: one per distinct pass body; the items of each
         # forward / adjoint launch are grouped by body, one sub-launch per group
         self.jit_sub: dict = {}
+        self.device = torch.device(device)
+        self._aux: dict = {}  # lane -> side streams for the sub-launches of one launch
         if jit and items:
             self._specialise(items, device)
         pool_base = np.concatenate([[0], np.cumsum(lane_pool)]).astype(np.int64)
@@ -307,6 +312,25 @@ class WavePlan:
         return {"fwd": fwd, "adj": adj}
 
     # ------------------------------------------------------------ execution
+    def _fork(self, lane: int, stream, width: int):
+        """(the launching stream, [it and width - 1 side streams of this lane that wait on it])."""
+        aux = self._aux.setdefault(lane, [])
+        while len(aux) < width - 1:
+            aux.append(torch.cuda.Stream(self.device))
+        base = torch.cuda.ExternalStream(int(stream.value), device=self.device)
+        ev = torch.cuda.Event()
+        ev.record(base)
+        for a in aux[:width - 1]:
+            a.wait_event(ev)
+        return base, [base] + aux[:width - 1]
+
+    @staticmethod
+    def _join(base, branch) -> None:
+        for a in branch[1:]:
+            ev = torch.cuda.Event()
+            ev.record(a)
+            base.wait_event(ev)
+
     def launch(self, groups_dev, terms_dev, theta, energies, grads, stream, lane_streams=None,
                kinds=(0, 1, 2), on_launch=None) -> None:
         """Enqueue every launch; lane l's on lane_streams[l] when given, else all on `stream`.
@@ -324,7 +348,16 @@ class WavePlan:
                 continue
             if L[0] == "run" and li in self.jit_sub:
                 kind = L[1]
-                for b0, c0, k in self.jit_sub[li]:
+                subs = self.jit_sub[li]
+                # the sub-launches of one launch touch disjoint items: without a profiler
+                # they run side by side (fork on side streams, join before the next launch),
+                # so a launch split by kernel still fills the GPU like one launch
+                fork = on_launch is None and len(subs) > 1
+                if fork:
+                    base, branch = self._fork(lane, stream, min(len(subs), MAX_FORK))
+                for si, (b0, c0, k) in enumerate(subs):
+                    if fork:
+                        stream = ctypes.c_void_p(branch[si % len(branch)].cuda_stream)
                     cb("start", kind, c0, bool(k))
                     if k:
                         nat.call("tq_jit_wave_run", P(k), kind, self.dt, P(self.items_dev.data_ptr() + isz * b0), c0,
@@ -339,6 +372,9 @@ class WavePlan:
                                  P(theta.data_ptr()), P(self.pool.data_ptr()), P(self.partials.data_ptr()), None,
                                  self.fwd_max_ops if kind == 0 else self.adj_max_ops, stream)
                     cb("end", kind, c0, bool(k))
+                if fork:
+                    self._join(base, branch)
+                    stream = ctypes.c_void_p(base.cuda_stream)
             elif L[0] == "run":
                 _, kind, b, c = L
                 if c == 0:
