@@ -443,6 +443,23 @@ def bench_small_configs(reps: int = 10) -> dict:
                           "energy_grad_ms": per_call_ms(lambda: est.energy_and_grad(theta)),
                           "energy_ms": per_call_ms(lambda: est.energy(theta)),
                           "shots4096_ms": per_call_ms(shots), "dtype": "c128"}}
+    # the same circuit through the drop-in chain API (the engine the plug-in installs):
+    # c.compile().device(provider="simulator", device="statevector").run(shots=4096) and
+    # c.state(), host results, per call; default complex64 and the complex128 option
+    from tyxonq_gb300.circuit import Circuit
+
+    chain = {}
+    for dname in ("complex64", "complex128"):
+        c = Circuit(12)
+        for l in range(4):
+            for q in range(12):
+                c.ry(q, theta=float(th12[l, q]))
+            for q in range(11):
+                c.cx(q, q + 1)
+        run = lambda: c.compile().device(provider="simulator", device="statevector", dtype=dname).run(shots=4096)
+        st = lambda: c.state(dtype=dname, form="numpy")
+        chain[dname] = {"run_shots4096_ms": per_call_ms(run), "state_ms": per_call_ms(st)}
+    out["hea12_chain_api"] = chain
     h, g = chem.random_integrals(8, seed=7)
     ucc = {}
     for name, kw in (("c128_rotations", {"dtype": torch.complex128, "trotter": True}),

@@ -804,8 +804,34 @@ def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int
     return ForwardProgram(n, out, len(gates), npass)
 
 
+_FUSED_CACHE: "OrderedDict" = None  # gate-list key -> ForwardProgram (engine calls of the same circuit)
+_FUSED_CACHE_MAX = 64
+
+
+def _gate_key(g: Gate) -> tuple:
+    return (g.kind, tuple(g.qubits), None if g.mat is None else np.asarray(g.mat).tobytes(),
+            None if g.rot is None else (g.rot[0], float(g.rot[1])), g.pauli)
+
+
 def execute_fused(psi: torch.Tensor, gates: Sequence[Gate]) -> torch.Tensor:
+    """Run the gates as a fused program; programs of circuits seen before (same
+    gates, angles and matrices, size, dtype and device) are reused from a
+    small LRU cache instead of being planned and encoded again."""
+    global _FUSED_CACHE
+    from collections import OrderedDict
+
     n = K._check_state(psi)
     if n == 0:
         return psi
-    return compile_forward(gates, n, psi.dtype).run(psi)
+    if _FUSED_CACHE is None:
+        _FUSED_CACHE = OrderedDict()
+    key = (n, psi.dtype, str(psi.device), tuple(_gate_key(g) for g in gates))
+    prog = _FUSED_CACHE.get(key)
+    if prog is None:
+        prog = compile_forward(gates, n, psi.dtype)
+        _FUSED_CACHE[key] = prog
+        while len(_FUSED_CACHE) > _FUSED_CACHE_MAX:
+            _FUSED_CACHE.popitem(last=False)
+    else:
+        _FUSED_CACHE.move_to_end(key)
+    return prog.run(psi)
