@@ -29,9 +29,10 @@ if str(ROOT) not in sys.path:
 
 METRIC = "VQE energy+grad evals/s batched vs plain GPU; p50/p99 latency; gate HBM GB/s"
 
-# DRAM bytes read + written by one k_staged_forward launch of the 28-qubit pass,
-# from the ncu capture summarised in profiles/k_staged_forward_28q_c64.txt
-STAGED_PASS_DRAM_BYTES = 4.2654e9
+# DRAM bytes read + written by one tq_jit_staged_pass launch of the 28-qubit
+# circuit (mean of the two passes of the ncu capture summarised in
+# profiles/tq_jit_staged_pass_28q_c64.txt)
+STAGED_PASS_DRAM_BYTES = 4.2358e9
 # DRAM bytes per item of the wave adjoint kernel (L2-resident states): from the
 # ncu capture of tq_jit_wave_adjoint; None until captured
 WAVE_ADJ_DRAM_BYTES_PER_ITEM = None
