@@ -317,7 +317,9 @@ class WavePlan:
         aux = self._aux.setdefault(lane, [])
         while len(aux) < width - 1:
             aux.append(torch.cuda.Stream(self.device))
-        base = torch.cuda.ExternalStream(int(stream.value), device=self.device)
+        ptr = stream.value if isinstance(stream, ctypes.c_void_p) else stream
+        base = (torch.cuda.ExternalStream(int(ptr), device=self.device) if ptr
+                else torch.cuda.default_stream(self.device))  # a null handle is the default stream
         ev = torch.cuda.Event()
         ev.record(base)
         for a in aux[:width - 1]:
