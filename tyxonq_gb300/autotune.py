@@ -120,7 +120,7 @@ def tune_forward(gates, n: int, dtype=torch.complex64, candidates: Sequence[int]
 # ---------------------------------------------------------------- batched schedule
 TUNED_DIR = Path(__file__).resolve().parent / "tuned"
 SCHEDULE_FIELDS = ("res8_max", "res4_max", "res2_max", "res1_max", "wave_t", "wave_hbits", "wave_budget",
-                   "wave_lanes", "wave_max_ops", "wave_adj_stage_bits", "wave_jit")
+                   "wave_lanes", "wave_max_ops", "wave_adj_stage_bits", "wave_jit", "wave_fork")
 
 
 def _gpu_tag(device=None) -> str:
@@ -172,9 +172,11 @@ def _candidates(field: str, cur: dict, dtype) -> list:
     if field == "wave_t":
         return [11, 12, 13] if c64 else [11, 12]
     if field == "wave_budget":
-        return [32 << 20, 48 << 20, 64 << 20, 96 << 20]
+        return [32 << 20, 48 << 20, 64 << 20, 96 << 20, 128 << 20]
     if field == "wave_lanes":
-        return [1, 2, 3]
+        return [1, 2, 3, 4]
+    if field == "wave_fork":
+        return [0, 1]
     if field == "wave_adj_stage_bits":
         return [3, 4]
     if field == "wave_max_ops":
@@ -212,21 +214,29 @@ def time_batched(instances, schedule, dtype=torch.complex64, steps: int = 3, flu
 
 def tune_batched(instances, dtype=torch.complex64, steps: int = 3, order: Sequence[str] | None = None,
                  log: Callable[[str], None] | None = None):
-    """Coordinate descent over the batched schedule from the current default;
-    returns (Schedule, [(fields, ms)] of every candidate timed)."""
+    """Coordinate descent over the batched schedule, from the faster of the
+    builtin schedule and the one saved for this GPU; returns (Schedule,
+    [(fields, ms)] of every candidate timed)."""
     from dataclasses import asdict, replace
 
     from .batch import Schedule
 
-    best = Schedule.builtin(dtype)
-    cur = asdict(best)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     table = []
-    best_ms = time_batched(instances, best, dtype, steps, flush)
-    table.append(({k: cur[k] for k in SCHEDULE_FIELDS}, best_ms))
-    if log:
-        log(f"start {best_ms:.2f} ms")
-    for field in order or ("wave_lanes", "wave_budget", "wave_adj_stage_bits", "wave_t", "wave_max_ops",
+    starts = [Schedule.builtin(dtype)]
+    saved = load_schedule(dtype)
+    if saved:
+        starts.append(replace(starts[0], **saved))
+    best, best_ms = None, float("inf")
+    for st in starts:
+        ms = time_batched(instances, st, dtype, steps, flush)
+        table.append(({k: asdict(st)[k] for k in SCHEDULE_FIELDS}, ms))
+        if log:
+            log(f"start {'saved' if st is not starts[0] else 'builtin'}: {ms:.2f} ms")
+        if ms < best_ms:
+            best, best_ms = st, ms
+    cur = asdict(best)
+    for field in order or ("wave_fork", "wave_lanes", "wave_budget", "wave_adj_stage_bits", "wave_t", "wave_max_ops",
                            "res1_max", "res2_max", "res4_max", "res8_max"):
         for v in _candidates(field, cur, dtype):
             if v == cur[field]:
@@ -258,7 +268,7 @@ def main() -> None:
 
     ap = argparse.ArgumentParser(description="tune the batched VQE schedule on this GPU")
     ap.add_argument("--count", type=int, default=4096)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--out", default=None)
     args = ap.parse_args()
     insts = batched_vqe(args.count, seed=3)

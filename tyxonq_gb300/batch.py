@@ -65,6 +65,7 @@ class Schedule:
     wave_max_ops: int = 256
     wave_adj_stage_bits: int = 4  # register bits per adjoint stage (3: 8 amplitudes of psi and of lam per thread)
     wave_jit: int = 1  # circuit-specialised wave kernels (runtime-compiled per distinct pass body)
+    wave_fork: int = 1  # the per-kernel sub-launches of one wave launch run side by side (1) or in order (0)
 
     @classmethod
     def builtin(cls, dtype) -> "Schedule":
@@ -258,7 +259,8 @@ class BatchedVQE:
             sc = self.sched
             self.waves = WavePlan(wave_entries, dtype, dev, t=sc.wave_t, hbits=sc.wave_hbits, budget=sc.wave_budget,
                                   lanes=sc.wave_lanes, adj_stage_bits=sc.wave_adj_stage_bits,
-                                  max_ops=sc.wave_max_ops, jit=bool(sc.wave_jit) and _jit_enabled())
+                                  max_ops=sc.wave_max_ops, jit=bool(sc.wave_jit) and _jit_enabled(),
+                                  fork=bool(sc.wave_fork))
             self.n_structures += self.waves.n_structures
         lib = nat.load()
         order = ["streamed", "res1", "res2", "res4", "res8"]

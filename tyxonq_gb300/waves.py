@@ -60,7 +60,8 @@ MAX_FORK = 8  # side-by-side sub-launches of one wave launch
 
 class WavePlan:
     def __init__(self, entries, dtype, device, t: int = 12, hbits: int = 12, budget: int = 48 << 20,
-                 max_ops: int = 256, lanes: int = 1, adj_stage_bits: int = 4, jit: bool = False):
+                 max_ops: int = 256, lanes: int = 1, adj_stage_bits: int = 4, jit: bool = False,
+                 fork: bool = True):
         """entries: list of dicts with keys idx (instance index), n, gates,
         params, key (structure key), theta_off, grad_offset, basis,
         group_begin, group_count.  Waves are dealt round-robin to `lanes`
@@ -184,6 +185,7 @@ class WavePlan:
         self.jit_sub: dict = {}
         self.device = torch.device(device)
         self._aux: dict = {}  # lane -> side streams for the sub-launches of one launch
+        self.fork = bool(fork)
         if jit and items:
             self._specialise(items, device)
         pool_base = np.concatenate([[0], np.cumsum(lane_pool)]).astype(np.int64)
@@ -354,7 +356,7 @@ class WavePlan:
                 # the sub-launches of one launch touch disjoint items: without a profiler
                 # they run side by side (fork on side streams, join before the next launch),
                 # so a launch split by kernel still fills the GPU like one launch
-                fork = on_launch is None and len(subs) > 1
+                fork = self.fork and on_launch is None and len(subs) > 1
                 if fork:
                     base, branch = self._fork(lane, stream, min(len(subs), MAX_FORK))
                 for si, (b0, c0, k) in enumerate(subs):
