@@ -33,9 +33,12 @@ METRIC = "VQE energy+grad evals/s batched vs plain GPU; p50/p99 latency; gate HB
 # circuit (mean of the two passes of the ncu capture summarised in
 # profiles/tq_jit_staged_pass_28q_c64.txt)
 STAGED_PASS_DRAM_BYTES = 4.2358e9
-# DRAM bytes per item of the wave adjoint kernel (L2-resident states): from the
-# ncu capture of tq_jit_wave_adjoint; None until captured
-WAVE_ADJ_DRAM_BYTES_PER_ITEM = None
+# DRAM bytes per item of the specialised wave adjoint (psi and lam tiles of 2^12
+# complex64 amplitudes): ncu capture of tq_jit_wave_adjoint on the 512-instance
+# batch, 256 / 512 / 768 items per launch, 65.7-66.5 KB each; ncu flushes the
+# caches before a captured launch, so this is the cold-cache figure (the tiles'
+# first reads), an upper bound for the benchmark's L2-resident waves
+WAVE_ADJ_DRAM_BYTES_PER_ITEM = 6.6e4
 
 
 def _peaks():
