@@ -438,7 +438,25 @@ TQ_API int tq_wave_normalize(const double* norm_partials, const int32_t* first, 
  * both stand in for the reference's per-instance loop (devices/base.py:378-381). */
 TQ_API int tq_jit_wave_run(void* kernel, int kind, int dtype, const tq_wave_item* items, int n_items, int t,
                            const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
-                           const double* theta, void* pool, double* partials, int max_ops, void* stream);
+                           const double* theta, const void* rops, void* pool, double* partials, int max_ops,
+                           void* stream);
+
+/* Op records of wave passes, built once per evaluation instead of once per
+ * tile: job j writes n_ops records (tq_jit_rops_bytes each) for ops
+ * [op_begin, op_begin + n_ops) with the angles at theta + theta_off, adjoint
+ * records (with gradient terms) when flags & 1, to out + out_record.  Passing
+ * out to tq_jit_wave_run as rops makes each item copy its records from
+ * rops + item.group_begin records (forward and adjoint items do not use their
+ * group fields otherwise); NULL rops: the kernel builds them per item. */
+typedef struct {
+  int32_t op_begin;
+  int32_t n_ops;
+  int32_t theta_off;
+  int32_t flags;
+  int64_t out_record;
+} tq_rop_job;
+TQ_API int tq_wave_rops(int dtype, const tq_rop_job* jobs, int n_jobs, const tq_tile_op* ops, const double* theta,
+                        void* out, void* stream);
 
 /* H psi and / or <psi|H|psi> of one state (n >= 12) through the wave H psi
  * kernel: output tiles of 4096 amplitudes, 16 per thread, each group's terms

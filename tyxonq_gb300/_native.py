@@ -85,7 +85,8 @@ SIGNATURES: dict[str, tuple] = {
     "tq_jit_unload": (c_int, [_P]),
     "tq_jit_rops_bytes": (c_size_t, [c_int, c_int]),
     "tq_jit_run_staged": (c_int, [_P, c_int, _P, c_int, c_int, _P, c_int, _P, _P, _P, c_int, _P, _P, c_size_t, _P]),
-    "tq_jit_wave_run": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, c_int, _P]),
+    "tq_jit_wave_run": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, c_int, _P]),
+    "tq_wave_rops": (c_int, [c_int, _P, c_int, _P, _P, _P, _P]),
     "tq_sv_adjoint_tiles_workspace_bytes": (c_size_t, [c_int, c_int]),
     "tq_sv_adjoint_tiles": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, _P, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_generator_im": (c_int, [_P, _P, c_int, c_int, c_uint64, c_uint64, c_uint64, _P, _P, c_size_t, _P]),

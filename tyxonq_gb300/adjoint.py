@@ -200,7 +200,7 @@ class _StagedReverse:
         from collections import defaultdict
 
         from .program import STAGE_DTYPE, TILE_OP_DTYPE
-        from .waves import PASS_DTYPE, WAVE_ITEM_DTYPE, WavePlan, _dev
+        from .waves import PASS_DTYPE, ROP_JOB_DTYPE, WAVE_ITEM_DTYPE, WavePlan, _dev, rop_jobs
 
         gates = [_canon(p.gate) for p in pgates]
         for g in gates:
@@ -246,6 +246,17 @@ class _StagedReverse:
             self.layers.append((o, len(layers[lay])))
             o += len(layers[lay])
         items = np.concatenate(blocks) if blocks else np.zeros(0, dtype=WAVE_ITEM_DTYPE)
+        # op records of every adjoint pass, compiled once per sweep (tq_wave_rops)
+        st_all = np.concatenate(enc_plan.stages) if enc_plan.stages else np.zeros(0, STAGE_DTYPE)
+        launches = [("run", 2, first, count) for first, count in self.runs]
+        rows_it, jobs = rop_jobs([tuple(r) for r in items.tolist()], launches, list(enc_plan.passes), st_all)
+        if len(rows_it):
+            items["group_begin"] = [r[7] for r in rows_it]
+        n_rec = int(jobs["out_record"][-1] + jobs["n_ops"][-1]) if len(jobs) else 0
+        self.rop_jobs_dev = _dev(jobs if len(jobs) else np.zeros(1, ROP_JOB_DTYPE), device)
+        self.n_rop_jobs = len(jobs)
+        self.rops_buf = torch.empty(max(int(nat.load().tq_jit_rops_bytes(enc_plan.dt, n_rec)), 16), dtype=torch.uint8,
+                                    device=device)
         pa = np.zeros(len(enc_plan.passes), dtype=PASS_DTYPE)
         for k, (tt, nl, b0, e0, pos) in enumerate(enc_plan.passes):
             pa[k] = (tt, nl, b0, e0, pos)
@@ -291,13 +302,16 @@ class _StagedReverse:
         isz = WAVE_ITEM_DTYPE.itemsize
         self.grads.zero_()
         kern = self.kernels
+        if kern and self.n_rop_jobs:
+            nat.call("tq_wave_rops", self.dt, P(self.rop_jobs_dev.data_ptr()), self.n_rop_jobs,
+                     P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.rops_buf.data_ptr()), st)
         for (first, count), pid in zip(self.runs, self.run_pids):
             k = kern.get(pid)
             if k:
                 nat.call("tq_jit_wave_run", P(k), 2, self.dt, P(self.items_dev.data_ptr() + isz * first), count,
                          self.t, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
-                         P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.pool.data_ptr()),
-                         P(self.partials.data_ptr()), self.max_ops, st)
+                         P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.rops_buf.data_ptr()),
+                         P(self.pool.data_ptr()), P(self.partials.data_ptr()), self.max_ops, st)
                 continue
             nat.call("tq_wave_run", 2, self.dt, P(self.items_dev.data_ptr() + isz * first), count, self.t, 12,
                      self.rb, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),

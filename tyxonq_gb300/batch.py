@@ -65,7 +65,7 @@ class Schedule:
     wave_max_ops: int = 256
     wave_adj_stage_bits: int = 4  # register bits per adjoint stage (3: 8 amplitudes of psi and of lam per thread)
     wave_jit: int = 1  # circuit-specialised wave kernels (runtime-compiled per distinct pass body)
-    wave_fork: int = 1  # the per-kernel sub-launches of one wave launch run side by side (1) or in order (0)
+    wave_fork: int = 0  # the per-kernel sub-launches of one wave launch run side by side (1) or in order (0)
 
     @classmethod
     def builtin(cls, dtype) -> "Schedule":
@@ -352,6 +352,7 @@ class BatchedVQE:
                      P(self.energies.data_ptr()), P(self.grads.data_ptr()),
                      P(self.counters.data_ptr() + 4 * k), s)
         if self.waves is not None:
+            self.waves.compile_rops(self.theta, ctypes.c_void_p(main.cuda_stream))
             lanes = [main]
             if self.waves.lanes > 1:
                 if getattr(self, "_lane_streams", None) is None:
@@ -417,6 +418,7 @@ class BatchedVQE:
         return out
 
     def launch_waves_only(self, stream, on_launch=None) -> None:
+        self.waves.compile_rops(self.theta, ctypes.c_void_p(stream.cuda_stream))
         self.waves.launch(self.groups_dev, self.terms_dev, self.theta, self.energies, self.grads,
                           ctypes.c_void_p(stream.cuda_stream), None, on_launch=on_launch)
 

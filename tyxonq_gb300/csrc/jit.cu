@@ -46,6 +46,18 @@ __global__ void k_rops_compile(ROp<R>* out, const tq_tile_op* __restrict__ ops, 
   if (k < n_ops) rop_build<R>(out[k], ops, k, theta, false, false);
 }
 
+// Op records of wave passes: one CTA per job, one thread per op.
+template <typename R>
+__global__ void k_wave_rops(const tq_rop_job* __restrict__ jobs, int n_jobs, const tq_tile_op* __restrict__ ops,
+                            const double* __restrict__ theta, ROp<R>* out) {
+  for (int j = blockIdx.x; j < n_jobs; j += gridDim.x) {
+    const tq_rop_job J = jobs[j];
+    const bool adj = (J.flags & 1) != 0;
+    for (int k = threadIdx.x; k < J.n_ops; k += blockDim.x)
+      rop_build<R>(out[J.out_record + k], ops, J.op_begin + k, theta + J.theta_off, adj, adj);
+  }
+}
+
 }  // namespace tq
 
 using namespace tq;
@@ -233,9 +245,27 @@ extern "C" int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi
   return TQ_OK;
 }
 
+extern "C" int tq_wave_rops(int dtype, const tq_rop_job* jobs, int n_jobs, const tq_tile_op* ops, const double* theta,
+                            void* out, void* stream) {
+  TQ_RANGE("tq_wave_rops");
+  if (dtype != TQ_C64 && dtype != TQ_C128) return fail(TQ_ERR_ARG, "tq_wave_rops: dtype tag %d", dtype);
+  if (n_jobs < 0) return fail(TQ_ERR_ARG, "tq_wave_rops: negative job count");
+  if (n_jobs == 0) return TQ_OK;
+  if (!jobs || !ops || !theta || !out) return fail(TQ_ERR_ARG, "tq_wave_rops: NULL argument");
+  if ((reinterpret_cast<uintptr_t>(out) & 15) != 0) return fail(TQ_ERR_ARG, "tq_wave_rops: output not 16-byte aligned");
+  const unsigned grid = (unsigned)(n_jobs < 152 * 16 ? n_jobs : 152 * 16);
+  if (dtype == TQ_C64)
+    k_wave_rops<float><<<grid, 128, 0, (cudaStream_t)stream>>>(jobs, n_jobs, ops, theta, (ROp<float>*)out);
+  else
+    k_wave_rops<double><<<grid, 128, 0, (cudaStream_t)stream>>>(jobs, n_jobs, ops, theta, (ROp<double>*)out);
+  TQ_CHECK_LAUNCH("tq_wave_rops");
+  return TQ_OK;
+}
+
 extern "C" int tq_jit_wave_run(void* kernel, int kind, int dtype, const tq_wave_item* items, int n_items, int t,
                                const tq_tile_pass* passes, const tq_tile_stage* stages, const tq_tile_op* ops,
-                               const double* theta, void* pool, double* partials, int max_ops, void* stream) {
+                               const double* theta, const void* rops, void* pool, double* partials, int max_ops,
+                               void* stream) {
   TQ_RANGE("tq_jit_wave_run");
   if (!kernel || !items || !passes || !stages || !ops || !pool || (kind == 2 && !partials))
     return fail(TQ_ERR_ARG, "tq_jit_wave_run: NULL argument");
@@ -257,10 +287,12 @@ extern "C" int tq_jit_wave_run(void* kernel, int kind, int dtype, const tq_wave_
   cudaKernel_t k = static_cast<JitKernel*>(kernel)->kernel;
   e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem, dev);
   if (e != cudaSuccess) return cuda_status(e, "tq_jit_wave_run: shared memory attribute");
-  void* args_f[] = {(void*)&items, &n_items, (void*)&passes, (void*)&stages, (void*)&ops, (void*)&theta, &pool,
-                    &max_ops};
-  void* args_a[] = {(void*)&items, &n_items, (void*)&passes, (void*)&stages, (void*)&ops, (void*)&theta, &pool,
-                    (void*)&partials, &max_ops};
+  if (rops && (reinterpret_cast<uintptr_t>(rops) & 15) != 0)
+    return fail(TQ_ERR_ARG, "tq_jit_wave_run: op records not 16-byte aligned");
+  void* args_f[] = {(void*)&items, &n_items, (void*)&passes, (void*)&stages, (void*)&ops, (void*)&theta,
+                    (void*)&rops, &pool, &max_ops};
+  void* args_a[] = {(void*)&items, &n_items, (void*)&passes, (void*)&stages, (void*)&ops, (void*)&theta,
+                    (void*)&rops, &pool, (void*)&partials, &max_ops};
   e = cudaLaunchKernel((const void*)k, dim3((unsigned)n_items), dim3(threads), kind == 0 ? args_f : args_a, smem,
                        (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_status(e, "tq_jit_wave_run: launch");

@@ -69,6 +69,23 @@ __device__ __forceinline__ void j_part(R part, R* wpart, int slot, int nwarps, i
   if (lane == 0) wpart[slot * nwarps + warp] = part;
 }
 
+// The item's op records in shared memory: copied from the records compiled once
+// per evaluation (tq_wave_rops; rops_g + item.group_begin records), or built
+// here when there are none.
+template <typename R>
+__device__ __forceinline__ void wave_rops(ROp<R>* rops, const void* __restrict__ rops_g, const tq_wave_item& I,
+                                          const tq_tile_op* __restrict__ ops, int op0, int nops,
+                                          const double* __restrict__ theta, bool adj) {
+  if (rops_g != nullptr) {
+    constexpr int W = (int)(sizeof(ROp<R>) / 16);
+    const uint4* src = reinterpret_cast<const uint4*>(rops_g) + (size_t)I.group_begin * W;
+    uint4* dst = reinterpret_cast<uint4*>(rops);
+    for (int w = threadIdx.x; w < nops * W; w += blockDim.x) dst[w] = __ldg(&src[w]);
+  } else {
+    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, adj, adj);
+  }
+}
+
 // Forward pass items: k_wave_forward with the stage loop replaced by
 // body(s, rops, gbase) (ends with a barrier after the last stage).
 template <typename R, typename Body>
@@ -76,7 +93,7 @@ __device__ __forceinline__ void jit_wave_forward(const tq_wave_item* __restrict_
                                                  const tq_tile_pass* __restrict__ passes,
                                                  const tq_tile_stage* __restrict__ stages,
                                                  const tq_tile_op* __restrict__ ops, const double* __restrict__ theta,
-                                                 void* pool, int max_ops, Body body) {
+                                                 const void* __restrict__ rops_g, void* pool, int max_ops, Body body) {
   extern __shared__ __align__(16) unsigned char smem[];
   typedef typename C2<R>::T T2;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
@@ -95,7 +112,7 @@ __device__ __forceinline__ void jit_wave_forward(const tq_wave_item* __restrict_
     const int64_t base = w_base(I.tile, P);
     // the tile streams in (cp.async) while the op records are compiled
     if (I.basis_lo < 0) w_load<R>(s, psi, base, hoff, P);
-    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, false, false);
+    wave_rops<R>(rops, rops_g, I, ops, op0, nops, theta, false);
     if (I.basis_lo >= 0) {
       const int N = 1 << P.t;
       const int lm = (1 << P.nlow) - 1;
@@ -119,7 +136,8 @@ __device__ __forceinline__ void jit_wave_adjoint(const tq_wave_item* __restrict_
                                                  const tq_tile_pass* __restrict__ passes,
                                                  const tq_tile_stage* __restrict__ stages,
                                                  const tq_tile_op* __restrict__ ops, const double* __restrict__ theta,
-                                                 void* pool, double* partials, int max_ops, Body body) {
+                                                 const void* __restrict__ rops_g, void* pool, double* partials,
+                                                 int max_ops, Body body) {
   extern __shared__ __align__(16) unsigned char smem[];
   typedef typename C2<R>::T T2;
   const int nwarps = blockDim.x >> 5;
@@ -147,7 +165,7 @@ __device__ __forceinline__ void jit_wave_adjoint(const tq_wave_item* __restrict_
     w_load<R>(sp, psi, base, hoff, P);
     w_load<R>(sl, lam, base, hoff, P);
     for (int k = threadIdx.x; k < nops * nwarps; k += blockDim.x) wpart[k] = R(0);
-    rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, true, true);
+    wave_rops<R>(rops, rops_g, I, ops, op0, nops, theta, true);
     w_commit_wait();
     __syncthreads();
     body(sp, sl, rops, wpart, (uint64_t)base, nwarps, warp, lane);

@@ -441,17 +441,18 @@ def wave_source(kind: int, t: int, body: str, double: bool) -> str:
     src = head + [body, "}", "}  // namespace tq", ""]
     common = ("const tq_wave_item* __restrict__ items, int n_items, const tq_tile_pass* __restrict__ passes, "
               "const tq_tile_stage* __restrict__ stages, const tq_tile_op* __restrict__ ops, "
-              "const double* __restrict__ theta, void* pool")
+              "const double* __restrict__ theta, const void* __restrict__ rops_g, void* pool")
     if kind == 0:
         src.append(f'extern "C" __global__ void __launch_bounds__({threads}) {WAVE_FWD_KERNEL}({common}, int max_ops) {{')
-        src.append(f"  tq::jit_wave_forward<{R}>(items, n_items, passes, stages, ops, theta, pool, max_ops, "
+        src.append(f"  tq::jit_wave_forward<{R}>(items, n_items, passes, stages, ops, theta, rops_g, pool, max_ops, "
                    f"[&](tq::cplx<{R}>* s, const tq::ROp<{R}>* rops, uint64_t gbase) "
                    f"{{ tq::jit_body<{R}>(s, rops, ops, gbase); }});")
     else:
         minb = 2 if threads <= 256 else 1
         src.append(f'extern "C" __global__ void __launch_bounds__({threads}, {minb}) {WAVE_ADJ_KERNEL}({common}, '
                    "double* partials, int max_ops) {")
-        src.append(f"  tq::jit_wave_adjoint<{R}>(items, n_items, passes, stages, ops, theta, pool, partials, max_ops, "
+        src.append(f"  tq::jit_wave_adjoint<{R}>(items, n_items, passes, stages, ops, theta, rops_g, pool, partials, "
+                   "max_ops, "
                    f"[&](tq::cplx<{R}>* sp, tq::cplx<{R}>* sl, const tq::ROp<{R}>* rops, {R}* wpart, uint64_t gbase, "
                    f"int nwarps, int warp, int lane) "
                    f"{{ tq::jit_body<{R}>(sp, sl, rops, ops, wpart, gbase, nwarps, warp, lane); }});")

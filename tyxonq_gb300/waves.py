@@ -33,6 +33,43 @@ WAVE_ITEM_DTYPE = np.dtype({
     "offsets": [0, 8, 16, 20, 24, 28, 32, 36, 40, 44],
     "itemsize": 48,
 })
+ROP_JOB_DTYPE = np.dtype({"names": ["op_begin", "n_ops", "theta_off", "flags", "out_record"],
+                          "formats": ["<i4", "<i4", "<i4", "<i4", "<i8"], "offsets": [0, 4, 8, 12, 16],
+                          "itemsize": 24})
+
+
+def rop_jobs(items: list, launches, passes: list, stages: np.ndarray) -> tuple[list, np.ndarray]:
+    """Op-record jobs (tq_rop_job) for the forward and adjoint items: one per
+    distinct (kind, pass, instance angles); returns the items with
+    group_begin = the first record of their job, and the job table."""
+    index: dict = {}
+    jobs = []
+    nrec = 0
+    out = list(items)
+    for L in launches:
+        if L[0] != "run" or L[1] not in (0, 2):
+            continue
+        kind = L[1]
+        for i in range(L[2], L[2] + L[3]):
+            row = out[i]
+            key = (kind, int(row[2]), int(row[4]))
+            if key not in index:
+                pa = passes[int(row[2])]
+                sb, se = int(pa[2]), int(pa[3])
+                op0 = int(stages[sb]["op_begin"]) if se > sb else 0
+                nops = int(stages[se - 1]["op_end"]) - op0 if se > sb else 0
+                index[key] = nrec
+                jobs.append((op0, nops, int(row[4]), 1 if kind == 2 else 0, nrec))
+                nrec += nops
+            out[i] = tuple(row[:7]) + (index[key],) + tuple(row[8:])
+    tab = np.zeros(len(jobs), dtype=ROP_JOB_DTYPE)
+    for k, j in enumerate(jobs):
+        tab[k] = j
+    if nrec >= 2 ** 31:
+        raise NotImplementedError("too many op records for one wave plan")
+    return out, tab
+
+
 # passes of a wave keep at least this many contiguous low bits (the kernels'
 # offset table holds 2^(t - WAVE_MIN_NLOW) entries)
 WAVE_MIN_NLOW = 4
@@ -186,6 +223,15 @@ class WavePlan:
         self.device = torch.device(device)
         self._aux: dict = {}  # lane -> side streams for the sub-launches of one launch
         self.fork = bool(fork)
+        # op records of the forward and adjoint items, compiled once per evaluation
+        # (compile_rops) for the specialised kernels instead of once per tile
+        st_all = np.concatenate(self.stages) if self.stages else np.zeros(0, STAGE_DTYPE)
+        items, jobs = rop_jobs(items, launches, self.passes, st_all)
+        self.rop_jobs_dev = _dev(jobs if len(jobs) else np.zeros(1, ROP_JOB_DTYPE), device)
+        self.n_rop_jobs = len(jobs)
+        n_rec = int(jobs["out_record"][-1] + jobs["n_ops"][-1]) if len(jobs) else 0
+        self.rops_buf = torch.empty(max(int(nat.load().tq_jit_rops_bytes(self.dt, n_rec)), 16), dtype=torch.uint8,
+                                    device=device)
         if jit and items:
             self._specialise(items, device)
         pool_base = np.concatenate([[0], np.cumsum(lane_pool)]).astype(np.int64)
@@ -314,6 +360,14 @@ class WavePlan:
         return {"fwd": fwd, "adj": adj}
 
     # ------------------------------------------------------------ execution
+    def compile_rops(self, theta, stream) -> None:
+        """Build the op records of every forward and adjoint (pass, instance) pair
+        from theta (one launch; the specialised wave kernels copy them per item)."""
+        if self.n_rop_jobs:
+            P = ctypes.c_void_p
+            nat.call("tq_wave_rops", self.dt, P(self.rop_jobs_dev.data_ptr()), self.n_rop_jobs,
+                     P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.rops_buf.data_ptr()), stream)
+
     def _fork(self, lane: int, stream, width: int):
         """(the launching stream, [it and width - 1 side streams of this lane that wait on it])."""
         aux = self._aux.setdefault(lane, [])
@@ -366,7 +420,8 @@ class WavePlan:
                     if k:
                         nat.call("tq_jit_wave_run", P(k), kind, self.dt, P(self.items_dev.data_ptr() + isz * b0), c0,
                                  self.t, P(self.passes_dev.data_ptr()), P(self.stages_dev.data_ptr()),
-                                 P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.pool.data_ptr()),
+                                 P(self.ops_dev.data_ptr()), P(theta.data_ptr()), P(self.rops_buf.data_ptr()),
+                                 P(self.pool.data_ptr()),
                                  P(self.partials.data_ptr()), self.fwd_max_ops if kind == 0 else self.adj_max_ops,
                                  stream)
                     else:
