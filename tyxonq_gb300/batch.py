@@ -31,7 +31,7 @@ import torch
 
 from . import _native as nat
 from . import kernels as K
-from .hamiltonian import GROUP_DTYPE, TERM_DTYPE, PauliSum, sort_terms_by_class
+from .hamiltonian import GROUP_DTYPE, TERM_DTYPE, PauliSum, order_groups_for_tiles, sort_terms_by_class
 from .ir import Gate, _rot_gate
 from .program import TILE_OP_DTYPE, PassPlan, TilePass, encode_passes, plan_passes
 
@@ -180,8 +180,9 @@ class BatchedVQE:
             if cname == "streamed" and self.sched.large == "waves":
                 t = sort_terms_by_class(g, t, self.sched.wave_hbits)
                 # groups whose flips share the bits above the H psi tile read the same
-                # partner tile: neighbours in the loop, so it is reused from L1
-                g = g[np.lexsort((g["flip"], g["flip"] >> np.uint64(self.sched.wave_hbits)))]
+                # partner tile: neighbours in the loop, so it is staged once; inside such a
+                # run, one-term groups of one sign class run back to back
+                g = order_groups_for_tiles(g, t, self.sched.wave_hbits)
                 wave_entries.append({"idx": i, "n": n, "gates": gates, "params": params, "key": (n, skey),
                                      "theta_offset": theta_off, "theta_off": theta_off, "grad_offset": theta_off,
                                      "basis": int(getattr(inst, "basis", 0)), "group_begin": n_groups_total,

@@ -95,6 +95,34 @@ __device__ __forceinline__ void hpsi_one_term(cplx<R>* acc, const cplx<R>* pv, R
   }
 }
 
+// A run of one-term groups whose term has sign class C (Z/Y bits 8 .. 11), from
+// group g on; returns the first group after the run.  Partner loads by byte
+// offset: output j = tid | k << 8, partner (tid ^ ml) ^ (k << 8) in the source
+// buffer at byte offset bo.
+template <typename R, int PER, int C>
+__device__ __forceinline__ int hpsi_run_c(cplx<R>* acc, const unsigned char* smem, int bo, int g, int ge, int HN,
+                                          int64_t tbase, const tq_pauli_group* __restrict__ groups,
+                                          const tq_pauli_term* __restrict__ terms) {
+  constexpr int SH = sizeof(cplx<R>) == 8 ? 3 : 4;
+  for (; g < ge; ++g) {
+    const int4 gr = __ldg(reinterpret_cast<const int4*>(&groups[g]));
+    if (gr.w != 1) break;
+    const uint64_t zy = __ldg(&terms[gr.z].zy);
+    if (((int)(zy >> 8) & (PER - 1)) != C) break;
+    const uint64_t m = (uint64_t)(uint32_t)gr.x | ((uint64_t)(uint32_t)gr.y << 32);
+    const int ml = (int)(m & (uint64_t)(HN - 1));
+    const int ab = ((((int)threadIdx.x ^ ml)) << SH) | bo;
+    cplx<R> pv[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) pv[k] = *reinterpret_cast<const cplx<R>*>(smem + (ab ^ (k << (8 + SH))));
+    const int p0 = __popcll((uint64_t)(tbase ^ (int64_t)m) & zy) & 1;
+    const cplx<R> w = term_w<R>(&terms[gr.z]);
+    if (w.x != R(0)) hpsi_one_term_c<R, PER, C, false>(acc, pv, p0 ? -w.x : w.x);
+    if (w.y != R(0)) hpsi_one_term_c<R, PER, C, true>(acc, pv, p0 ? -w.y : w.y);
+  }
+  return g;
+}
+
 // Item = output tile of HN = 2^hb amplitudes (256 threads x PER).  The partner
 // of output i under a group with flip m is psi[i ^ m]: it lies in source tile
 // (tile ^ (m >> hb)) at offset (i ^ m) mod HN.  Groups are visited in the order
@@ -153,6 +181,24 @@ __global__ void __launch_bounds__(kHpsiThreads) k_wave_hpsi(const tq_wave_item* 
       for (; g < ge; ++g) {
         // the 16-byte group record {flip, first_term, n_terms} in one load
         const int4 gr = __ldg(reinterpret_cast<const int4*>(&groups[g]));
+        if (full && gr.w == 1) {
+          // a run of one-term groups of one sign class (the host orders them so):
+          // one dispatch on the class for the whole run
+          const int c = (int)(__ldg(&terms[gr.z].zy) >> 8) & (PER - 1);
+          const int bo = (buf ? HN : 0) * (int)sizeof(cplx<R>);
+          const int64_t tb = t0 | (int64_t)threadIdx.x;
+          int gn = g + 1;
+          switch (c) {
+#define TQ_HR(C_) \
+  case C_: if constexpr (C_ < PER) gn = hpsi_run_c<R, PER, C_>(acc, smem, bo, g, ge, HN, tb, groups, terms); break;
+            TQ_HR(0) TQ_HR(1) TQ_HR(2) TQ_HR(3) TQ_HR(4) TQ_HR(5) TQ_HR(6) TQ_HR(7)
+            TQ_HR(8) TQ_HR(9) TQ_HR(10) TQ_HR(11) TQ_HR(12) TQ_HR(13) TQ_HR(14) TQ_HR(15)
+#undef TQ_HR
+            default: break;
+          }
+          g = gn - 1;
+          continue;
+        }
         const uint64_t m = (uint64_t)(uint32_t)gr.x | ((uint64_t)(uint32_t)gr.y << 32);
         const int first = gr.z, cnt = gr.w;
         const int ml = (int)(m & (uint64_t)(HN - 1));
