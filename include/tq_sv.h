@@ -64,6 +64,19 @@ TQ_API int tq_version(void);
  * NUL-terminated when len > 0).  Returns the last error code. */
 TQ_API int tq_last_error(char* buf, size_t len);
 
+/* Checked builds.  The library's checked variant (compiled with -DTQ_CHECKED)
+ * guards the device-computed indices of its kernels: a failing check records
+ * the first failing site and index and skips the access instead of trapping.
+ * tq_check_status writes that site (0: none) and index and clears them; it
+ * returns 1 in a checked build and 0 (site 0) in the normal build.  The
+ * runtime-compiled kernels are not instrumented. */
+#define TQ_SITE_GATE 1        /* single-gate kernels: amplitude index >= 2^n */
+#define TQ_SITE_TILE 2        /* tile passes: tile amplitude index >= 2^n */
+#define TQ_SITE_WAVE_TILE 3   /* wave items: tile amplitude index >= 2^n of the instance */
+#define TQ_SITE_HPSI 4        /* H psi: partner tile or term index out of range */
+#define TQ_SITE_SAMPLE 5      /* sampler: resolved index outside the state */
+TQ_API int tq_check_status(unsigned* site, long long* index);
+
 /* ------------------------------------------------------------ state preparation */
 
 /* |basis_index> over n qubits.  Replaces init_statevector

@@ -570,3 +570,16 @@ def test_commuted_diagonals_preserve_the_state_and_meet_their_neighbours():
     near = sum(1 for k in d1 if any(0 <= k + d < len(moved) and moved[k + d].kind == "u1"
                                     and moved[k + d].qubits == moved[k].qubits for d in (-1, 1)))
     assert near >= len(d1) // 2
+
+
+def test_checked_variant_builds_and_reports_status():
+    """The -DTQ_CHECKED variant compiles and exports every declared symbol; the
+    normal build answers tq_check_status with 0 (nothing recorded, unchecked)."""
+    lib = _native.load()
+    site, index = ctypes.c_uint(7), ctypes.c_longlong(7)
+    assert lib.tq_check_status(ctypes.byref(site), ctypes.byref(index)) == 0
+    assert site.value == 0 and index.value == 0
+    path = _build.build(checked=True)
+    chk = ctypes.CDLL(str(path))
+    for name in header_symbols():
+        assert hasattr(chk, name), name

@@ -21,6 +21,9 @@ BUILD_DIR = PKG_DIR / "_build"
 LIB_DIR = PKG_DIR / "_lib"
 LIB_NAME = "libtyxonq_gb300.so"
 LIB_PATH = LIB_DIR / LIB_NAME
+# the checked variant: -DTQ_CHECKED (device-side index checks, tq_check_status)
+CHECKED_LIB_NAME = "libtyxonq_gb300_checked.so"
+CHECKED_LIB_PATH = LIB_DIR / CHECKED_LIB_NAME
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + [
@@ -53,26 +56,31 @@ def _deps() -> list[Path]:
     return sources() + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
-def needs_build() -> bool:
-    if not LIB_PATH.exists():
+def needs_build(checked: bool = False) -> bool:
+    lib = CHECKED_LIB_PATH if checked else LIB_PATH
+    if not lib.exists():
         return True
-    t = LIB_PATH.stat().st_mtime
+    t = lib.stat().st_mtime
     return any(p.stat().st_mtime > t for p in _deps())
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile and link the library; returns its path."""
-    if not force and not needs_build():
-        return LIB_PATH
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Compile and link the library (checked: the -DTQ_CHECKED variant, objects
+    in their own folder); returns its path."""
+    lib_path = CHECKED_LIB_PATH if checked else LIB_PATH
+    if not force and not needs_build(checked):
+        return lib_path
     nvcc = nvcc_path()
-    BUILD_DIR.mkdir(exist_ok=True)
+    build_dir = BUILD_DIR / "checked" if checked else BUILD_DIR
+    build_dir.mkdir(parents=True, exist_ok=True)
     LIB_DIR.mkdir(exist_ok=True)
     procs = []
     objs = []
     for src in sources():
-        obj = BUILD_DIR / (src.stem + ".o")
+        obj = build_dir / (src.stem + ".o")
         objs.append(obj)
-        cmd = [nvcc, *NVCC_FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *NVCC_FLAGS, *(["-DTQ_CHECKED"] if checked else []), "-I", str(INCLUDE), "-c", str(src),
+               "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
@@ -85,16 +93,16 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             print(out.decode(errors="replace"), file=sys.stderr)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    tmp = LIB_DIR / (LIB_NAME + ".tmp")
+    tmp = LIB_DIR / (lib_path.name + ".tmp")
     cuda_lib = Path(nvcc).resolve().parent.parent / "lib64"
     cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs), "-L", str(cuda_lib), "-lnvrtc",
            "-Xlinker", f"-rpath={cuda_lib}"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv))

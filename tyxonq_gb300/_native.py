@@ -7,6 +7,7 @@ CUDA device is visible, the first call raises ``RuntimeError``.
 from __future__ import annotations
 
 import ctypes
+import os
 import threading
 from ctypes import POINTER, c_double, c_int, c_int64, c_size_t, c_uint64, c_void_p
 
@@ -87,6 +88,7 @@ SIGNATURES: dict[str, tuple] = {
     "tq_jit_run_staged": (c_int, [_P, c_int, _P, c_int, c_int, _P, c_int, _P, _P, _P, c_int, _P, _P, c_size_t, _P]),
     "tq_jit_wave_run": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P, _P, _P, _P, _P, _P, _P, c_int, _P]),
     "tq_wave_rops": (c_int, [c_int, _P, c_int, _P, _P, _P, _P]),
+    "tq_check_status": (c_int, [_P, _P]),
     "tq_sv_adjoint_tiles_workspace_bytes": (c_size_t, [c_int, c_int]),
     "tq_sv_adjoint_tiles": (c_int, [_P, _P, c_int, c_int, _P, c_int, _P, _P, c_int, _P, _P, c_size_t, _P]),
     "tq_sv_generator_im": (c_int, [_P, _P, c_int, c_int, c_uint64, c_uint64, c_uint64, _P, _P, c_size_t, _P]),
@@ -122,8 +124,14 @@ _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None
 
 
+def checked() -> bool:
+    """TYXONQ_GB300_CHECKED=1 selects the checked library variant (device-side
+    index checks; read with check_status())."""
+    return os.environ.get("TYXONQ_GB300_CHECKED", "0") not in ("", "0")
+
+
 def library_path():
-    return _build.LIB_PATH
+    return _build.CHECKED_LIB_PATH if checked() else _build.LIB_PATH
 
 
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -134,17 +142,29 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     with _lock:
         if _lib is not None:
             return _lib
-        if _build.needs_build():
+        chk = checked()
+        if _build.needs_build(chk):
             if not build_if_missing:
-                raise RuntimeError(f"{_build.LIB_PATH} is not built; run tyxonq_gb300._build.build()")
-            _build.build()
-        lib = ctypes.CDLL(str(_build.LIB_PATH))
+                raise RuntimeError(f"{library_path()} is not built; run tyxonq_gb300._build.build()")
+            _build.build(checked=chk)
+        lib = ctypes.CDLL(str(library_path()))
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
         _lib = lib
         return lib
+
+
+def check_status() -> tuple[bool, int, int]:
+    """(checked build, first failing check site TQ_SITE_* or 0, its index);
+    clears the recorded failure."""
+    lib = load()
+    site, index = ctypes.c_uint(0), ctypes.c_longlong(0)
+    rc = lib.tq_check_status(ctypes.byref(site), ctypes.byref(index))
+    if rc < 0:
+        check(rc)
+    return rc == 1, int(site.value), int(index.value)
 
 
 def last_error() -> tuple[int, str]:

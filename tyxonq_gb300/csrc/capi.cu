@@ -37,3 +37,31 @@ extern "C" int tq_last_error(char* buf, size_t len) {
   }
   return tq::g_err_code;
 }
+
+#ifdef TQ_CHECKED
+extern "C" int tq_check_read_gates(unsigned long long* out);
+extern "C" int tq_check_read_program(unsigned long long* out);
+extern "C" int tq_check_read_wave(unsigned long long* out);
+extern "C" int tq_check_read_measure(unsigned long long* out);
+#endif
+
+extern "C" int tq_check_status(unsigned* site, long long* index) {
+  if (site) *site = 0;
+  if (index) *index = 0;
+#ifdef TQ_CHECKED
+  int (*readers[])(unsigned long long*) = {tq_check_read_gates, tq_check_read_program, tq_check_read_wave,
+                                           tq_check_read_measure};
+  for (auto rd : readers) {
+    unsigned long long w[2] = {0ull, 0ull};
+    const int e = rd(w);
+    if (e != 0) return tq::cuda_status((cudaError_t)e, "tq_check_status");
+    if (w[0] != 0ull && site && *site == 0) {
+      *site = (unsigned)w[0];
+      if (index) *index = (long long)w[1];
+    }
+  }
+  return 1;
+#else
+  return 0;
+#endif
+}

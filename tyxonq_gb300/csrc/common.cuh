@@ -90,6 +90,41 @@ __host__ __device__ __forceinline__ int64_t insert_zero2(int64_t i, int plo, int
   return insert_zero(insert_zero(i, plo), phi);
 }
 
+// ----------------------------------------------------------------- checked builds
+// With -DTQ_CHECKED (the library's checked variant) device-side index checks
+// guard the accesses whose indices kernels compute: a failing check records
+// the first failing site (TQ_SITE_*) and its index in this translation unit's
+// status words and skips the access instead of trapping, and the host reads
+// and clears them with tq_check_status.  Unchecked builds compile the checks
+// away.  TQ_DCHECK(cond, site, index, action): action (continue, return, ...)
+// runs after a failing check.
+#if defined(TQ_CHECKED) && !defined(__CUDACC_RTC__)
+static __device__ unsigned long long tq_check_word[2];
+static __device__ __noinline__ void tq_check_fail(unsigned site, long long index) {
+  if (atomicCAS(&tq_check_word[0], 0ull, (unsigned long long)site) == 0ull) tq_check_word[1] = (unsigned long long)index;
+}
+#define TQ_DCHECK(cond, site, index, action)                        \
+  do {                                                              \
+    if (!(cond)) {                                                  \
+      ::tq::tq_check_fail((unsigned)(site), (long long)(index));    \
+      action;                                                       \
+    }                                                               \
+  } while (0)
+// Host reader of this translation unit's status words (name: the unit).
+#define TQ_CHECK_UNIT(name)                                                                         \
+  extern "C" int tq_check_read_##name(unsigned long long* out) {                                   \
+    cudaError_t e = cudaMemcpyFromSymbol(out, ::tq::tq_check_word, sizeof(unsigned long long) * 2); \
+    if (e != cudaSuccess) return (int)e;                                                            \
+    const unsigned long long zero[2] = {0ull, 0ull};                                                \
+    return (int)cudaMemcpyToSymbol(::tq::tq_check_word, zero, sizeof(zero));                        \
+  }
+#else
+#define TQ_DCHECK(cond, site, index, action) \
+  do {                                       \
+  } while (0)
+#define TQ_CHECK_UNIT(name)
+#endif
+
 #ifndef __CUDACC_RTC__
 // ----------------------------------------------------------------- tracing
 // One NVTX range per entry point (kernel class): header-only NVTX v3, a no-op

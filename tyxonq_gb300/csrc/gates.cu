@@ -85,6 +85,7 @@ __global__ void k_1q_c64_vec(float4* psi4, int64_t items, int p, Mat2<float> u) 
   GRID_STRIDE(v, items) {
     const int64_t i0 = insert_zero(2 * v, p);
     const int64_t i1 = i0 | (int64_t(1) << p);
+    TQ_DCHECK((i1 >> 1) < 2 * items, TQ_SITE_GATE, i1, continue);
     float4 A = psi4[i0 >> 1], B = psi4[i1 >> 1];
     cplx<float> a0, a1, b0, b1;
     split4(A, a0, a1);
@@ -109,6 +110,7 @@ __global__ void k_1q_scalar(typename C2<R>::T* psi, int64_t items, int p, Mat2<R
   GRID_STRIDE(v, items) {
     const int64_t i0 = insert_zero(v, p);
     const int64_t i1 = i0 | (int64_t(1) << p);
+    TQ_DCHECK(i1 < 2 * items, TQ_SITE_GATE, i1, continue);
     cplx<R> a0 = ld<R>(psi, i0), a1 = ld<R>(psi, i1);
     mv2(u, a0, a1);
     st<R>(psi, i0, a0);
@@ -121,6 +123,7 @@ __global__ void k_1q_scalar(typename C2<R>::T* psi, int64_t items, int p, Mat2<R
 __global__ void k_diag_hi_c64_vec(float4* psi4, int64_t items, int p, cplx<float> d1) {
   GRID_STRIDE(v, items) {
     const int64_t i1 = insert_zero(2 * v, p) | (int64_t(1) << p);
+    TQ_DCHECK((i1 >> 1) < 2 * items, TQ_SITE_GATE, i1, continue);
     cplx<float> a, b;
     split4(psi4[i1 >> 1], a, b);
     psi4[i1 >> 1] = join4(cmul(d1, a), cmul(d1, b));
@@ -130,6 +133,7 @@ template <typename R>
 __global__ void k_diag_hi_scalar(typename C2<R>::T* psi, int64_t items, int p, cplx<R> d1) {
   GRID_STRIDE(v, items) {
     const int64_t i1 = insert_zero(v, p) | (int64_t(1) << p);
+    TQ_DCHECK(i1 < 2 * items, TQ_SITE_GATE, i1, continue);
     st<R>(psi, i1, cmul(d1, ld<R>(psi, i1)));
   }
 }
@@ -156,6 +160,7 @@ __global__ void k_2q_c64_vec(float4* psi4, int64_t items, int pa, int pb, int pl
     const int64_t b = insert_zero2(2 * v, plo, phi);
     const int64_t ia = int64_t(1) << pa, ib = int64_t(1) << pb;
     const int64_t idx[4] = {b, b | ib, b | ia, b | ia | ib};
+    TQ_DCHECK((idx[3] >> 1) < 4 * items, TQ_SITE_GATE, idx[3], continue);
     cplx<float> x[4], y[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) split4(psi4[idx[r] >> 1], x[r], y[r]);
@@ -171,6 +176,7 @@ __global__ void k_2q_scalar(typename C2<R>::T* psi, int64_t items, int pa, int p
   GRID_STRIDE(v, items) {
     const int64_t b = insert_zero2(v, plo, phi);
     const int64_t ia = int64_t(1) << pa, ib = int64_t(1) << pb;
+    TQ_DCHECK((b | ia | ib) < 4 * items, TQ_SITE_GATE, b | ia | ib, continue);
     cplx<R> a0 = ld<R>(psi, b), a1 = ld<R>(psi, b | ib), a2 = ld<R>(psi, b | ia),
             a3 = ld<R>(psi, b | ia | ib);
     mv4(u, a0, a1, a2, a3);
@@ -189,6 +195,7 @@ __global__ void k_perm2_c64_vec(float4* psi4, int64_t items, int pa, int pb, int
   GRID_STRIDE(v, items) {
     const int64_t b = insert_zero2(2 * v, plo, phi);
     const int64_t ia = int64_t(1) << pa, ib = int64_t(1) << pb;
+    TQ_DCHECK(((b | ia | ib) >> 1) < 4 * items, TQ_SITE_GATE, b | ia | ib, continue);
     if (MODE == 0) {
       float4 x = psi4[(b | ia) >> 1], y = psi4[(b | ia | ib) >> 1];
       psi4[(b | ia) >> 1] = y;
@@ -209,6 +216,7 @@ __global__ void k_perm2_scalar(typename C2<R>::T* psi, int64_t items, int pa, in
   GRID_STRIDE(v, items) {
     const int64_t b = insert_zero2(v, plo, phi);
     const int64_t ia = int64_t(1) << pa, ib = int64_t(1) << pb;
+    TQ_DCHECK((b | ia | ib) < 4 * items, TQ_SITE_GATE, b | ia | ib, continue);
     if (MODE == 0) {
       typename C2<R>::T x = psi[b | ia], y = psi[b | ia | ib];
       psi[b | ia] = y;
@@ -261,6 +269,7 @@ __global__ void k_kq(typename C2<R>::T* psi, int64_t items, const __grid_constan
     int64_t b = v;
 #pragma unroll
     for (int r = 0; r < K; ++r) b = insert_zero(b, P.sp[r]);
+    TQ_DCHECK((b | P.offs[D - 1]) < (items << K), TQ_SITE_GATE, b | P.offs[D - 1], continue);
     cplx<R> x[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) x[j] = ld<R>(psi, b + P.offs[j]);
@@ -307,6 +316,7 @@ __global__ void k_pauli_rot(typename C2<R>::T* psi, int64_t items, uint64_t m, u
     } else {
       const int64_t i = insert_zero(v, h);
       const int64_t j = i ^ (int64_t)m;
+      TQ_DCHECK(i < 2 * items && j < 2 * items, TQ_SITE_GATE, i > j ? i : j, continue);
       cplx<R> a = ld<R>(psi, i), b = ld<R>(psi, j);
       const R si = (__popcll((unsigned long long)i & zy) & 1) ? R(-1) : R(1);
       const R sj = (__popcll((unsigned long long)j & zy) & 1) ? R(-1) : R(1);
@@ -579,3 +589,4 @@ extern "C" int tq_sv_scale(void* psi, int n, int dtype, double re, double im, vo
   TQ_CHECK_LAUNCH("tq_sv_scale");
   return TQ_OK;
 }
+TQ_CHECK_UNIT(gates)

@@ -205,6 +205,7 @@ extern "C" int tq_jit_run_staged(void* const* kernels, int stage_bits, void* psi
       continue;
     }
     PassArgs P;
+    P.n = n;
     P.t = tp.t;
     P.nlow = tp.nlow;
     P.op_begin = tp.op_begin;

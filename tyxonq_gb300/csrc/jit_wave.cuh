@@ -98,7 +98,7 @@ __device__ __forceinline__ void jit_wave_forward(const tq_wave_item* __restrict_
   typedef typename C2<R>::T T2;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
-    const WPass P = wload_pass(&passes[I.pass]);
+    const WPass P = wload_pass(&passes[I.pass], I.n);
     const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
     const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
     if (P.nlow < kWaveMinNlow || nops > max_ops) continue;
@@ -144,7 +144,7 @@ __device__ __forceinline__ void jit_wave_adjoint(const tq_wave_item* __restrict_
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
-    const WPass P = wload_pass(&passes[I.pass]);
+    const WPass P = wload_pass(&passes[I.pass], I.n);
     const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
     const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
     if (P.nlow < kWaveMinNlow || nops > max_ops) continue;

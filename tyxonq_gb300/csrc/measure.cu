@@ -430,6 +430,7 @@ __global__ void k_resolve(const typename C2<R>::T* psi, int64_t N, const double*
     }
     int j = (a < len) ? a : lnz;
     if (j > lnz) j = lnz;
+    TQ_DCHECK(base + (j < 0 ? 0 : j) < N, TQ_SITE_SAMPLE, base + j, j = -1);
     out[k] = base + (j < 0 ? 0 : j);
   }
 }
@@ -757,3 +758,4 @@ extern "C" int tq_sv_sample_noalloc(const void* psi, int n, int dtype, int64_t s
   // (chunk sums, scans, spacings), so the previous call's contents need no clearing.
   return tq_sv_sample(psi, n, dtype, shots, seed, out_indices, scratch, TQ_NOALLOC_SCRATCH_BYTES, stream);
 }
+TQ_CHECK_UNIT(measure)

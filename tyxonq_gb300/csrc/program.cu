@@ -12,8 +12,9 @@ namespace tq {
 
 static const int kTileGridCap = 152 * 8;
 
-static PassArgs to_args(const tq_tile_pass& p) {
+static PassArgs to_args(const tq_tile_pass& p, int n) {
   PassArgs a;
+  a.n = n;
   a.t = p.t;
   a.nlow = p.nlow;
   a.op_begin = p.op_begin;
@@ -36,6 +37,7 @@ __device__ __forceinline__ void tile_load<float>(cplx<float>* s, const float2* p
   for (int v = threadIdx.x; v < nv; v += blockDim.x) {
     const int j = 2 * v;
     const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi + 2 <= (int64_t(1) << P.n), TQ_SITE_TILE, gi, continue);
     s4[v] = g4[gi >> 1];
   }
 }
@@ -45,7 +47,9 @@ __device__ __forceinline__ void tile_load<double>(cplx<double>* s, const double2
   const int N = 1 << P.t;
   const int lm = (1 << P.nlow) - 1;
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    const double2 v = psi[base + hoff[j >> P.nlow] + (j & lm)];
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi < (int64_t(1) << P.n), TQ_SITE_TILE, gi, continue);
+    const double2 v = psi[gi];
     s[j] = cplx<double>(v.x, v.y);
   }
 }
@@ -62,6 +66,7 @@ __device__ __forceinline__ void tile_store<float>(const cplx<float>* s, float2* 
   for (int v = threadIdx.x; v < nv; v += blockDim.x) {
     const int j = 2 * v;
     const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi + 2 <= (int64_t(1) << P.n), TQ_SITE_TILE, gi, continue);
     g4[gi >> 1] = s4[v];
   }
 }
@@ -71,7 +76,9 @@ __device__ __forceinline__ void tile_store<double>(const cplx<double>* s, double
   const int N = 1 << P.t;
   const int lm = (1 << P.nlow) - 1;
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    psi[base + hoff[j >> P.nlow] + (j & lm)] = make_double2(s[j].x, s[j].y);
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi < (int64_t(1) << P.n), TQ_SITE_TILE, gi, continue);
+    psi[gi] = make_double2(s[j].x, s[j].y);
   }
 }
 
@@ -211,7 +218,7 @@ template <typename R>
 static int run_fwd(void* psi, int n, const tq_tile_pass* passes, int n_passes, const tq_tile_op* ops,
                    const double* theta, cudaStream_t s) {
   for (int p = 0; p < n_passes; ++p) {
-    const PassArgs P = to_args(passes[p]);
+    const PassArgs P = to_args(passes[p], n);
     if (P.op_end == P.op_begin) continue;
     const size_t smem = (sizeof(cplx<R>) << P.t) + (sizeof(int64_t) << (P.t - P.nlow));
     if (smem > 48 * 1024) {
@@ -242,7 +249,7 @@ static int run_adj(void* psi, void* lam, int n, const tq_tile_pass* passes, int 
   const unsigned grid = adjoint_grid(n, passes, n_passes);
   if (n_slots > 0) cudaMemsetAsync(partials, 0, sizeof(double) * (size_t)grid * n_slots, s);
   for (int p = 0; p < n_passes; ++p) {
-    const PassArgs P = to_args(passes[p]);
+    const PassArgs P = to_args(passes[p], n);
     const int nops = P.op_end - P.op_begin;
     if (nops == 0) continue;
     const size_t smem = 2 * (sizeof(cplx<R>) << P.t) + (sizeof(int64_t) << (P.t - P.nlow)) + sizeof(double) * nops +
@@ -425,7 +432,7 @@ static int run_staged(void* psi, int n, const tq_tile_pass* passes, int n_passes
   int dev = 0, sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   for (int p = 0; p < n_passes; ++p) {
-    const PassArgs P = to_args(passes[p]);
+    const PassArgs P = to_args(passes[p], n);
     if (P.op_end == P.op_begin) continue;
     const int64_t ntiles = int64_t(1) << (n - P.t);
     const int dbuf = ntiles > sms ? 1 : 0;
@@ -458,3 +465,4 @@ extern "C" int tq_sv_run_staged(void* psi, int n, int dtype, const tq_tile_pass*
   return dtype == TQ_C64 ? run_staged<float>(psi, n, passes, n_passes, stages, ops, theta, s)
                          : run_staged<double>(psi, n, passes, n_passes, stages, ops, theta, s);
 }
+TQ_CHECK_UNIT(program)

@@ -13,6 +13,7 @@ struct PassArgs {
   int t, nlow;
   int op_begin, op_end;
   int pos[TQ_TILE_MAX_BITS];
+  int n;  // qubits of the state (index checks of checked builds)
 };
 
 // hoff[h] = global offset of local index (h << nlow).
@@ -41,7 +42,9 @@ __device__ __forceinline__ void staged_issue_load(cplx<R>* s, const typename C2<
   const int lm = (1 << P.nlow) - 1;
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
     const int j = c * A;
-    cp_async16(&s[pphys(j)], &g[base + hoff[j >> P.nlow] + (j & lm)]);
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi + A <= (int64_t(1) << P.n), TQ_SITE_TILE, gi, continue);
+    cp_async16(&s[pphys(j)], &g[gi]);
   }
 }
 
@@ -53,8 +56,9 @@ __device__ __forceinline__ void staged_store(const cplx<R>* s, typename C2<R>::T
   const int lm = (1 << P.nlow) - 1;
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
     const int j = c * A;
-    *reinterpret_cast<float4*>(&g[base + hoff[j >> P.nlow] + (j & lm)]) =
-        *reinterpret_cast<const float4*>(&s[pphys(j)]);
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi + A <= (int64_t(1) << P.n), TQ_SITE_TILE, gi, continue);
+    *reinterpret_cast<float4*>(&g[gi]) = *reinterpret_cast<const float4*>(&s[pphys(j)]);
   }
 }
 

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256)
   typedef typename C2<R>::T T2;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
-    const WPass P = wload_pass(&passes[I.pass]);
+    const WPass P = wload_pass(&passes[I.pass], I.n);
     const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
     const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
     // tables that would not fit the shared memory sized by the host (never planned)
@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(kHpsiThreads) k_wave_hpsi(const tq_wave_item* 
     const int gend = I.group_begin + I.group_count;
     // source tiles double-buffered: the next run's tile streams in while this run computes
     auto issue = [&](cplx<R>* dst, int64_t h) {
+      TQ_DCHECK((tile ^ h) < (int64_t(1) << (I.n - hb)), TQ_SITE_HPSI, tile ^ h, h = 0);
       const T2* sp = psi + ((tile ^ h) << hb);
       constexpr int A = 16 / sizeof(cplx<R>);
       if (HN >= A) {
@@ -343,7 +344,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, RB == 3 ? 2 : 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
-    const WPass P = wload_pass(&passes[I.pass]);
+    const WPass P = wload_pass(&passes[I.pass], I.n);
     const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
     const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
     // tables that would not fit the shared memory sized by the host (never planned)
@@ -745,3 +746,4 @@ extern "C" int tq_wave_reduce(const double* partials, const int32_t* first, cons
   TQ_CHECK_LAUNCH("tq_wave_reduce");
   return TQ_OK;
 }
+TQ_CHECK_UNIT(wave)

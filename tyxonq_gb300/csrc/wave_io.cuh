@@ -14,10 +14,12 @@ namespace tq {
 struct WPass {
   int t, nlow, op_begin, op_end;
   uint64_t tmask;
+  int n;  // qubits of the item's instance (index checks of checked builds)
 };
 
-__device__ __forceinline__ WPass wload_pass(const tq_tile_pass* p) {
+__device__ __forceinline__ WPass wload_pass(const tq_tile_pass* p, int n) {
   WPass s;
+  s.n = n;
   s.t = p->t;
   s.nlow = p->nlow;
   s.op_begin = p->op_begin;
@@ -67,7 +69,9 @@ __device__ __forceinline__ void w_load(cplx<R>* s, const typename C2<R>::T* g, i
   const int lm = (1 << P.nlow) - 1;
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
     const int j = c * A;
-    cp_async16(&s[pphys(j)], &g[base + hoff[j >> P.nlow] + (j & lm)]);
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi + A <= (int64_t(1) << P.n), TQ_SITE_WAVE_TILE, gi, continue);
+    cp_async16(&s[pphys(j)], &g[gi]);
   }
 }
 
@@ -79,8 +83,9 @@ __device__ __forceinline__ void w_store(const cplx<R>* s, typename C2<R>::T* g, 
   const int lm = (1 << P.nlow) - 1;
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
     const int j = c * A;
-    *reinterpret_cast<float4*>(&g[base + hoff[j >> P.nlow] + (j & lm)]) =
-        *reinterpret_cast<const float4*>(&s[pphys(j)]);
+    const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
+    TQ_DCHECK(gi + A <= (int64_t(1) << P.n), TQ_SITE_WAVE_TILE, gi, continue);
+    *reinterpret_cast<float4*>(&g[gi]) = *reinterpret_cast<const float4*>(&s[pphys(j)]);
   }
 }
 
