@@ -98,17 +98,30 @@ __device__ __forceinline__ void hpsi_one_term(cplx<R>* acc, const cplx<R>* pv, R
 // A run of one-term groups whose term has sign class C (Z/Y bits 8 .. 11), from
 // group g on; returns the first group after the run.  Partner loads by byte
 // offset: output j = tid | k << 8, partner (tid ^ ml) ^ (k << 8) in the source
-// buffer at byte offset bo.
+// buffer at byte offset bo.  The group records are software-pipelined: while
+// group g computes, the term of group g + 1 and the record of group g + 2 are
+// in flight (every index comes from a record already read, none is guessed).
 template <typename R, int PER, int C>
 __device__ __forceinline__ int hpsi_run_c(cplx<R>* acc, const unsigned char* smem, int bo, int g, int ge, int HN,
                                           int64_t tbase, const tq_pauli_group* __restrict__ groups,
                                           const tq_pauli_term* __restrict__ terms) {
   constexpr int SH = sizeof(cplx<R>) == 8 ? 3 : 4;
-  for (; g < ge; ++g) {
-    const int4 gr = __ldg(reinterpret_cast<const int4*>(&groups[g]));
-    if (gr.w != 1) break;
-    const uint64_t zy = __ldg(&terms[gr.z].zy);
-    if (((int)(zy >> 8) & (PER - 1)) != C) break;
+  auto rec = [&](int i) { return __ldg(reinterpret_cast<const int4*>(&groups[i])); };
+  int4 gr = rec(g);
+  uint64_t zy = __ldg(&terms[gr.z].zy);
+  cplx<R> w = term_w<R>(&terms[gr.z]);
+  int4 gr1 = g + 1 < ge ? rec(g + 1) : make_int4(0, 0, 0, 0);
+  for (;;) {
+    if (gr.w != 1 || ((int)(zy >> 8) & (PER - 1)) != C) break;
+    // next loads: the term of group g + 1, the record of group g + 2
+    uint64_t zy1 = 0;
+    cplx<R> w1(0, 0);
+    const bool has1 = g + 1 < ge && gr1.w >= 1;
+    if (has1) {
+      zy1 = __ldg(&terms[gr1.z].zy);
+      w1 = term_w<R>(&terms[gr1.z]);
+    }
+    const int4 gr2 = g + 2 < ge ? rec(g + 2) : make_int4(0, 0, 0, 0);
     const uint64_t m = (uint64_t)(uint32_t)gr.x | ((uint64_t)(uint32_t)gr.y << 32);
     const int ml = (int)(m & (uint64_t)(HN - 1));
     const int ab = ((((int)threadIdx.x ^ ml)) << SH) | bo;
@@ -116,9 +129,14 @@ __device__ __forceinline__ int hpsi_run_c(cplx<R>* acc, const unsigned char* sme
 #pragma unroll
     for (int k = 0; k < PER; ++k) pv[k] = *reinterpret_cast<const cplx<R>*>(smem + (ab ^ (k << (8 + SH))));
     const int p0 = __popcll((uint64_t)(tbase ^ (int64_t)m) & zy) & 1;
-    const cplx<R> w = term_w<R>(&terms[gr.z]);
     if (w.x != R(0)) hpsi_one_term_c<R, PER, C, false>(acc, pv, p0 ? -w.x : w.x);
     if (w.y != R(0)) hpsi_one_term_c<R, PER, C, true>(acc, pv, p0 ? -w.y : w.y);
+    ++g;
+    if (!has1) break;
+    gr = gr1;
+    zy = zy1;
+    w = w1;
+    gr1 = gr2;
   }
   return g;
 }
