@@ -459,8 +459,9 @@ TQ_API int tq_jit_wave_run(void* kernel, int kind, int dtype, const tq_wave_item
  * [op_begin, op_begin + n_ops) with the angles at theta + theta_off, adjoint
  * records (with gradient terms) when flags & 1, to out + out_record.  Passing
  * out to tq_jit_wave_run as rops makes each item copy its records from
- * rops + item.group_begin records (forward and adjoint items do not use their
- * group fields otherwise); NULL rops: the kernel builds them per item. */
+ * rops + item.group_begin records and reads its op count from
+ * item.group_count (forward and adjoint items do not use their group fields
+ * otherwise); NULL rops: the kernel builds them per item. */
 typedef struct {
   int32_t op_begin;
   int32_t n_ops;

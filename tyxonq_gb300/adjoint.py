@@ -252,6 +252,7 @@ class _StagedReverse:
         rows_it, jobs = rop_jobs([tuple(r) for r in items.tolist()], launches, list(enc_plan.passes), st_all)
         if len(rows_it):
             items["group_begin"] = [r[7] for r in rows_it]
+            items["group_count"] = [r[8] for r in rows_it]
         n_rec = int(jobs["out_record"][-1] + jobs["n_ops"][-1]) if len(jobs) else 0
         self.rop_jobs_dev = _dev(jobs if len(jobs) else np.zeros(1, ROP_JOB_DTYPE), device)
         self.n_rop_jobs = len(jobs)

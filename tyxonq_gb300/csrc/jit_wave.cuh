@@ -99,8 +99,11 @@ __device__ __forceinline__ void jit_wave_forward(const tq_wave_item* __restrict_
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
     const WPass P = wload_pass(&passes[I.pass], I.n);
-    const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
-    const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
+    // with compiled records the item carries its op count (group_count); the
+    // first op index is needed only to build the records here
+    const int op0 = rops_g == nullptr && P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
+    const int nops = rops_g != nullptr ? I.group_count
+                                       : (P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0);
     if (P.nlow < kWaveMinNlow || nops > max_ops) continue;
     cplx<R>* s = reinterpret_cast<cplx<R>*>(smem);
     int64_t* hoff = reinterpret_cast<int64_t*>(smem + padded_len(P.t) * sizeof(cplx<R>));
@@ -145,8 +148,11 @@ __device__ __forceinline__ void jit_wave_adjoint(const tq_wave_item* __restrict_
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const tq_wave_item I = items[it];
     const WPass P = wload_pass(&passes[I.pass], I.n);
-    const int op0 = P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
-    const int nops = P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0;
+    // with compiled records the item carries its op count (group_count); the
+    // first op index is needed only to build the records here
+    const int op0 = rops_g == nullptr && P.op_end > P.op_begin ? stages[P.op_begin].op_begin : 0;
+    const int nops = rops_g != nullptr ? I.group_count
+                                       : (P.op_end > P.op_begin ? stages[P.op_end - 1].op_end - op0 : 0);
     if (P.nlow < kWaveMinNlow || nops > max_ops) continue;
     const int PT = padded_len(P.t);
     cplx<R>* sp = reinterpret_cast<cplx<R>*>(smem);

@@ -41,7 +41,8 @@ ROP_JOB_DTYPE = np.dtype({"names": ["op_begin", "n_ops", "theta_off", "flags", "
 def rop_jobs(items: list, launches, passes: list, stages: np.ndarray) -> tuple[list, np.ndarray]:
     """Op-record jobs (tq_rop_job) for the forward and adjoint items: one per
     distinct (kind, pass, instance angles); returns the items with
-    group_begin = the first record of their job, and the job table."""
+    group_begin = the first record of their job and group_count = its op
+    count, and the job table."""
     index: dict = {}
     jobs = []
     nrec = 0
@@ -58,10 +59,10 @@ def rop_jobs(items: list, launches, passes: list, stages: np.ndarray) -> tuple[l
                 sb, se = int(pa[2]), int(pa[3])
                 op0 = int(stages[sb]["op_begin"]) if se > sb else 0
                 nops = int(stages[se - 1]["op_end"]) - op0 if se > sb else 0
-                index[key] = nrec
+                index[key] = (nrec, nops)
                 jobs.append((op0, nops, int(row[4]), 1 if kind == 2 else 0, nrec))
                 nrec += nops
-            out[i] = tuple(row[:7]) + (index[key],) + tuple(row[8:])
+            out[i] = tuple(row[:7]) + index[key] + tuple(row[9:])
     tab = np.zeros(len(jobs), dtype=ROP_JOB_DTYPE)
     for k, j in enumerate(jobs):
         tab[k] = j
