@@ -39,6 +39,9 @@ STAGED_PASS_DRAM_BYTES = 4.2358e9
 # caches before a captured launch, so this is the cold-cache figure (the tiles'
 # first reads), an upper bound for the benchmark's L2-resident waves
 WAVE_ADJ_DRAM_BYTES_PER_ITEM = 6.6e4
+# fraction of cycles the same capture's schedulers issued an instruction
+# (smsp__issue_active, 768-item launch)
+WAVE_ADJ_ISSUE_ACTIVE = 0.497
 
 
 def _peaks():
@@ -826,7 +829,10 @@ def main():
                      "bound": "l2", "achieved": waves_prof["adjoint"]["gbs"], "peak": l2_gbs, "unit": "GB/s",
                      "frac": waves_prof["adjoint"]["frac_of_l2_copy"], "traffic": WAVE_ADJ_DRAM_BYTES_PER_ITEM,
                      "traffic_unit": "DRAM bytes per item (ncu)",
-                     "peak_kind": "measured in this run: L2-resident copy (2 x 24 MiB)"},
+                     "peak_kind": "measured in this run: L2-resident copy (2 x 24 MiB)",
+                     "issue_active": WAVE_ADJ_ISSUE_ACTIVE,
+                     "issue_note": "smsp__issue_active of the same kernel from ncu: the pass is bound by "
+                                   "instruction issue and latency on L2-resident tiles, not by L2 bandwidth"},
         "roofline_c2": {"kernel": "tq_jit_staged_pass (circuit-specialised fused pass of the 28-qubit complex64 "
                                   "depth-40 random circuit, 2*N*8 B per launch)", "bound": "hbm",
                         "achieved": gk["pass_gbs"], "peak": peak, "unit": "GB/s", "frac": gk["pass_gbs"] / peak,
