@@ -200,7 +200,7 @@ class _StagedReverse:
         from collections import defaultdict
 
         from .program import STAGE_DTYPE, TILE_OP_DTYPE
-        from .waves import PASS_DTYPE, ROP_JOB_DTYPE, WAVE_ITEM_DTYPE, WavePlan, _dev, rop_jobs
+        from .waves import PASS_DTYPE, ROP_JOB_DTYPE, WAVE_ITEM_DTYPE, WavePlan, _dev
 
         gates = [_canon(p.gate) for p in pgates]
         for g in gates:
@@ -246,14 +246,21 @@ class _StagedReverse:
             self.layers.append((o, len(layers[lay])))
             o += len(layers[lay])
         items = np.concatenate(blocks) if blocks else np.zeros(0, dtype=WAVE_ITEM_DTYPE)
-        # op records of every adjoint pass, compiled once per sweep (tq_wave_rops)
+        # op records of every adjoint pass, compiled once per sweep (tq_wave_rops):
+        # one job per pass (one instance), its items point at the job's records
         st_all = np.concatenate(enc_plan.stages) if enc_plan.stages else np.zeros(0, STAGE_DTYPE)
-        launches = [("run", 2, first, count) for first, count in self.runs]
-        rows_it, jobs = rop_jobs([tuple(r) for r in items.tolist()], launches, list(enc_plan.passes), st_all)
-        if len(rows_it):
-            items["group_begin"] = [r[7] for r in rows_it]
-            items["group_count"] = [r[8] for r in rows_it]
-        n_rec = int(jobs["out_record"][-1] + jobs["n_ops"][-1]) if len(jobs) else 0
+        jobs = np.zeros(len(self.runs), dtype=ROP_JOB_DTYPE)
+        nrec = 0
+        for r, ((first, count), pid) in enumerate(zip(self.runs, self.run_pids)):
+            pa = enc_plan.passes[pid]
+            sb, se = int(pa[2]), int(pa[3])
+            op0 = int(st_all[sb]["op_begin"]) if se > sb else 0
+            nops = int(st_all[se - 1]["op_end"]) - op0 if se > sb else 0
+            jobs[r] = (op0, nops, 0, 1, nrec)
+            items["group_begin"][first:first + count] = nrec
+            items["group_count"][first:first + count] = nops
+            nrec += nops
+        n_rec = nrec
         self.rop_jobs_dev = _dev(jobs if len(jobs) else np.zeros(1, ROP_JOB_DTYPE), device)
         self.n_rop_jobs = len(jobs)
         self.rops_buf = torch.empty(max(int(nat.load().tq_jit_rops_bytes(enc_plan.dt, n_rec)), 16), dtype=torch.uint8,
