@@ -9,7 +9,7 @@ native compile pipeline's two rewrites that change results (auto
 ``measure_z`` on every qubit when none is present, auto_measure.py:23-35, and
 ``x`` -> ``rx(pi)``, gates_transform.py:31-32), honours the reference quirk
 that ``run``'s own ``shots=1024`` default wins over ``.device(shots=...)``
-(circuit.py:873,890), and returns the driver's result layout
+(circuit.py:873,890), and returns the simulator driver's result layout
 (simulators/driver.py:108-131).  With TyxonQ installed, use TyxonQ's Circuit
 together with ``tyxonq_gb300.install()`` instead.
 """
