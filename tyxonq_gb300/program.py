@@ -13,6 +13,7 @@ segments executed by the single-gate kernels.
 from __future__ import annotations
 
 import ctypes
+import threading
 from collections import deque
 from dataclasses import dataclass, field
 from typing import Sequence
@@ -806,6 +807,7 @@ def compile_forward(gates: Sequence[Gate], n: int, dtype=torch.complex64, t: int
 
 _FUSED_CACHE: "OrderedDict" = None  # gate-list key -> ForwardProgram (engine calls of the same circuit)
 _FUSED_CACHE_MAX = 64
+_FUSED_LOCK = threading.Lock()
 
 
 def _gate_key(g: Gate) -> tuple:
@@ -823,15 +825,17 @@ def execute_fused(psi: torch.Tensor, gates: Sequence[Gate]) -> torch.Tensor:
     n = K._check_state(psi)
     if n == 0:
         return psi
-    if _FUSED_CACHE is None:
-        _FUSED_CACHE = OrderedDict()
     key = (n, psi.dtype, str(psi.device), tuple(_gate_key(g) for g in gates))
-    prog = _FUSED_CACHE.get(key)
+    with _FUSED_LOCK:
+        if _FUSED_CACHE is None:
+            _FUSED_CACHE = OrderedDict()
+        prog = _FUSED_CACHE.get(key)
+        if prog is not None:
+            _FUSED_CACHE.move_to_end(key)
     if prog is None:
         prog = compile_forward(gates, n, psi.dtype)
-        _FUSED_CACHE[key] = prog
-        while len(_FUSED_CACHE) > _FUSED_CACHE_MAX:
-            _FUSED_CACHE.popitem(last=False)
-    else:
-        _FUSED_CACHE.move_to_end(key)
+        with _FUSED_LOCK:
+            _FUSED_CACHE[key] = prog
+            while len(_FUSED_CACHE) > _FUSED_CACHE_MAX:
+                _FUSED_CACHE.popitem(last=False)
     return prog.run(psi)
