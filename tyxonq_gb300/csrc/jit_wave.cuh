@@ -77,10 +77,12 @@ __device__ __forceinline__ void wave_rops(ROp<R>* rops, const void* __restrict__
                                           const tq_tile_op* __restrict__ ops, int op0, int nops,
                                           const double* __restrict__ theta, bool adj) {
   if (rops_g != nullptr) {
+    // asynchronous 16-byte copies: they complete with the item's tile loads
+    // (the caller's commit and wait), so no load round trip of their own
     constexpr int W = (int)(sizeof(ROp<R>) / 16);
     const uint4* src = reinterpret_cast<const uint4*>(rops_g) + (size_t)I.group_begin * W;
     uint4* dst = reinterpret_cast<uint4*>(rops);
-    for (int w = threadIdx.x; w < nops * W; w += blockDim.x) dst[w] = __ldg(&src[w]);
+    for (int w = threadIdx.x; w < nops * W; w += blockDim.x) cp_async16(&dst[w], &src[w]);
   } else {
     rops_build<R>(rops, ops, op0, op0 + nops, theta + I.theta_off, adj, adj);
   }
@@ -123,9 +125,8 @@ __device__ __forceinline__ void jit_wave_forward(const tq_wave_item* __restrict_
         const int64_t gi = base + hoff[j >> P.nlow] + (j & lm);
         s[pphys(j)] = cplx<R>(gi == (int64_t)I.basis_lo ? R(1) : R(0), R(0));
       }
-    } else {
-      w_commit_wait();
     }
+    w_commit_wait();  // the tile and the op records
     __syncthreads();
     body(s, rops, (uint64_t)base);
     w_store<R>(s, psi, base, hoff, P);
