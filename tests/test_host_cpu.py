@@ -583,3 +583,27 @@ def test_checked_variant_builds_and_reports_status():
     chk = ctypes.CDLL(str(path))
     for name in header_symbols():
         assert hasattr(chk, name), name
+
+
+def test_tuned_tile_widths_are_read_from_the_cache_file(tmp_path, monkeypatch):
+    """tile_bits_for reads the single-state tuner's cache file once per process
+    (TYXONQ_GB300_TUNE) and falls back to the shared-memory defaults."""
+    import json
+
+    import torch
+
+    from tyxonq_gb300 import autotune as A
+
+    f = tmp_path / "tune.json"
+    f.write_text(json.dumps({"fwd:24:c64": 11, "adj:24:c64": 10}))
+    monkeypatch.setenv("TYXONQ_GB300_TUNE", str(f))
+    monkeypatch.setattr(A, "_TUNED", {})
+    monkeypatch.setattr(A, "_LOADED", False)
+    assert A.tile_bits_for(24, torch.complex64) == 11
+    assert A.tile_bits_for(24, torch.complex64, adjoint=True) == 10
+    assert A.tile_bits_for(22, torch.complex64) == 13  # untuned: 2^13 complex64 amplitudes
+    assert A.tile_bits_for(22, torch.complex128, adjoint=True) == 11
+    A.set_tile_bits(9, torch.complex64, False, 7)
+    out = tmp_path / "out.json"
+    A.save(out)
+    assert json.loads(out.read_text())["fwd:9:c64"] == 7

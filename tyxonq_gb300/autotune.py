@@ -10,11 +10,13 @@
   ``tuned/<gpu>.json``), so the benchmark and the tests run the tuned
   schedule.  ``python -m tyxonq_gb300.autotune`` re-tunes on the benchmark's
   4096-instance workload and writes the file.
-* Single-state programs (``tune_forward``): tile width (local qubits per
-  shared-memory tile pass) per (n, dtype), kept per process and in
-  ``TYXONQ_GB300_TUNE`` (default ``~/.cache/tyxonq_gb300/tune.json``).
-  Untuned sizes use defaults from shared-memory capacity: a complex64 tile of
-  2^13 amplitudes is 64 KiB.
+* Single-state programs (``tune_forward``, ``tune_forward_sizes``;
+  ``python -m tyxonq_gb300.autotune --forward 20 24 28``): tile width (local
+  qubits per shared-memory tile pass) per (n, dtype), saved in
+  ``TYXONQ_GB300_TUNE`` (default ``~/.cache/tyxonq_gb300/tune.json``) and
+  read once per process by ``tile_bits_for``, which ``compile_forward`` and the
+  adjoint paths use when no width is given.  Untuned sizes use defaults from
+  shared-memory capacity: a complex64 tile of 2^13 amplitudes is 64 KiB.
 """
 from __future__ import annotations
 
@@ -40,7 +42,19 @@ def _default(n: int, dtype, adjoint: bool) -> int:
     return max(1, min(n, cap))
 
 
+_LOADED = False
+
+
 def tile_bits_for(n: int, dtype, adjoint: bool = False) -> int:
+    """Tile width for an n-qubit program: the tuned one (the cache file is read
+    once per process) or the shared-memory default."""
+    global _LOADED
+    if not _LOADED:
+        _LOADED = True
+        try:
+            load()
+        except (OSError, ValueError):  # an unreadable cache only costs the defaults
+            pass
     k = _key("adj" if adjoint else "fwd", n, dtype)
     if k in _TUNED:
         return min(_TUNED[k], n)
@@ -261,16 +275,44 @@ def tune_batched(instances, dtype=torch.complex64, steps: int = 3, order: Sequen
     return best, table
 
 
+def tune_forward_sizes(sizes: Sequence[int], depth: int = 40, dtype=torch.complex64,
+                       log: Callable[[str], None] | None = None) -> dict:
+    """Forward tile widths for random circuits (the 28-qubit benchmark circuit's
+    generator) of the given sizes; saved to the cache file that tile_bits_for
+    reads.  Returns {n: (best t, {t: ms})}."""
+    from .ir import lower_ops
+    from .workloads import random_circuit
+
+    class _C:
+        def __init__(self, n, ops):
+            self.num_qubits, self.ops = n, ops
+
+    out = {}
+    for n in sizes:
+        gates, _ = lower_ops(_C(n, random_circuit(n, depth, seed=1)), mode="run")
+        best, res = tune_forward(gates, n, dtype)
+        out[n] = (best, res)
+        if log:
+            log(f"forward n={n}: t={best} ({', '.join(f'{t}: {ms:.2f} ms' for t, ms in sorted(res.items()))})")
+    save()
+    return out
+
+
 def main() -> None:
     import argparse
 
     from .workloads import batched_vqe
 
-    ap = argparse.ArgumentParser(description="tune the batched VQE schedule on this GPU")
+    ap = argparse.ArgumentParser(description="tune the batched VQE schedule (and optionally the single-state "
+                                             "forward tile widths) on this GPU")
     ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--forward", type=int, nargs="*", default=None,
+                    help="also tune the forward tile width for random circuits of these qubit counts")
     args = ap.parse_args()
+    if args.forward:
+        tune_forward_sizes(args.forward, log=lambda m: print(m, flush=True))
     insts = batched_vqe(args.count, seed=3)
     sched, table = tune_batched(insts, steps=args.steps, log=lambda m: print(m, flush=True))
     from dataclasses import asdict
