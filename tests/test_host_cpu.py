@@ -607,3 +607,52 @@ def test_tuned_tile_widths_are_read_from_the_cache_file(tmp_path, monkeypatch):
     out = tmp_path / "out.json"
     A.save(out)
     assert json.loads(out.read_text())["fwd:9:c64"] == 7
+
+
+def test_op_record_jobs_one_per_pass_and_instance():
+    """rop_jobs: one job per distinct (kind, pass, instance angles) of the
+    forward and adjoint launches, consecutive record ranges, and every item
+    pointing at its job's records (group_begin) with its op count (group_count);
+    H psi items are left alone."""
+    from tyxonq_gb300.program import STAGE_DTYPE
+    from tyxonq_gb300.waves import rop_jobs
+
+    stages = np.zeros(6, dtype=STAGE_DTYPE)
+    stages["op_begin"] = [0, 3, 5, 9, 12, 20]
+    stages["op_end"] = [3, 5, 9, 12, 20, 21]
+    passes = [(12, 5, 0, 2, [0] * 16), (12, 5, 2, 4, [0] * 16), (12, 5, 4, 6, [0] * 16)]
+    # items: (psi_off, lam_off, pass, tile, theta_off, part_off, n, group_begin, group_count, basis_lo)
+    items = [(0, 0, 0, t, 0, 0, 14, 0, 0, -1) for t in range(4)]  # instance A, pass 0
+    items += [(0, 0, 0, t, 40, 0, 14, 0, 0, -1) for t in range(4)]  # instance B (other angles), pass 0
+    items += [(0, 0, 0, t, 0, t, 14, 7, 3, -1) for t in range(4)]  # H psi items
+    items += [(0, 0, 2, t, 0, 0, 14, 0, 0, -1) for t in range(4)]  # instance A, adjoint pass 2
+    launches = [("run", 0, 0, 8), ("run", 1, 8, 4), ("run", 2, 12, 4)]
+    out, jobs = rop_jobs(items, launches, passes, stages)
+    assert len(jobs) == 3
+    assert list(jobs["op_begin"]) == [0, 0, 12] and list(jobs["n_ops"]) == [5, 5, 9]
+    assert list(jobs["theta_off"]) == [0, 40, 0] and list(jobs["flags"]) == [0, 0, 1]
+    assert list(jobs["out_record"]) == [0, 5, 10]
+    assert all(r[7] == 0 and r[8] == 5 for r in out[0:4])
+    assert all(r[7] == 5 and r[8] == 5 for r in out[4:8])
+    assert out[8:12] == items[8:12]  # H psi items keep their group fields
+    assert all(r[7] == 10 and r[8] == 9 for r in out[12:16])
+
+
+def test_tile_group_order_keeps_partner_runs_and_groups_one_term_classes():
+    """order_groups_for_tiles only permutes groups: partner-tile runs (flip >> 12)
+    stay contiguous, and inside a run one-term groups come ordered by their
+    term's Z/Y bits 8..11, the multi-term groups after them."""
+    from tyxonq_gb300.hamiltonian import order_groups_for_tiles, random_pauli_sum, sort_terms_by_class
+
+    H = random_pauli_sum(16, 400, np.random.default_rng(3))
+    g, t = H.pack()
+    t = sort_terms_by_class(g, t, 12)
+    o = order_groups_for_tiles(g, t, 12)
+    assert sorted(map(tuple, o.tolist())) == sorted(map(tuple, g.tolist()))
+    hi = o["flip"] >> np.uint64(12)
+    assert (np.diff(hi.astype(np.int64)) >= 0).all()
+    for h in np.unique(hi):
+        run = o[hi == h]
+        one = run["n_terms"] == 1
+        cls = np.where(one, (t["zy"][run["first_term"]] >> np.uint64(8)) & np.uint64(15), 16).astype(np.int64)
+        assert (np.diff(cls) >= 0).all()
