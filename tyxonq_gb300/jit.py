@@ -221,8 +221,13 @@ def _geo_off(j: int, nlow: int, pos: list) -> int:
 
 
 # The last stage stores its registers straight to global memory when none of its
-# register bits is below this one (each warp store then covers whole 32-byte sectors).
-DIRECT_MIN_BIT = 2
+# register bits is below this one.  With register bits 0 or 1 a warp store fills
+# half of each 32-byte sector (the other half comes from another register's
+# store, merged in L2); measured on the 28-qubit circuit (5-bit stages), storing
+# every pass's last stage this way was the fastest: 13-qubit tiles 32.7 ->
+# 31.5 ms, 14-qubit tiles 31.9 -> 30.9 ms against a threshold of 2, and 35.9 /
+# 40.4 ms with no direct stores at all.
+DIRECT_MIN_BIT = 0
 
 
 def direct_last_ok(stages: np.ndarray, p, stage_bits: list | None = None) -> bool:
