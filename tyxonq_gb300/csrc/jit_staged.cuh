@@ -110,8 +110,9 @@ __device__ __forceinline__ int64_t geo_base(int64_t g) {
 // offset is the thread's part plus a constant and its shared-memory index the
 // thread's padded index plus a constant, so a chunk costs one copy instruction
 // and its address arithmetic folds into immediates.  Memory schedule and
-// shared-memory layout as jit_staged_forward (the offset table region is left
-// unused).  body(s, rops, gbase, on_free, gt): with G::DIRECT the body's last
+// shared-memory layout as the library's k_staged_forward: persistent CTAs,
+// cp.async double buffering when a CTA owns several tiles, the pass's op
+// records in shared memory (the offset table region is left unused).  body(s, rops, gbase, on_free, gt): with G::DIRECT the body's last
 // stage stores to gt = psi + gbase and calls on_free once its inputs are read.
 template <typename R, typename G, typename Body>
 __device__ __forceinline__ void jit_staged_forward_g(typename C2<R>::T* psi, int n, const PassArgs& P,
@@ -186,57 +187,6 @@ __device__ __forceinline__ void jit_staged_forward_g(typename C2<R>::T* psi, int
         load(buf0, geo_base<G>(gn));
         cp_async_commit();
       }
-    }
-    cur ^= dbuf;
-  }
-  cp_async_wait_group<0>();
-}
-
-// The tile loop of one forward pass (same memory schedule as k_staged_forward:
-// persistent CTAs, cp.async double buffering when a CTA owns several tiles,
-// the pass's op records in shared memory).  body(s, rops, gbase) applies every
-// stage of the pass to the padded tile s and ends with a barrier.
-template <typename R, typename Body>
-__device__ __forceinline__ void jit_staged_forward(typename C2<R>::T* psi, int n, const PassArgs& P,
-                                                   const tq_tile_stage* __restrict__ stages,
-                                                   const ROp<R>* __restrict__ rops_g, int dbuf, Body body) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int PT = padded_len(P.t);
-  cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem);
-  cplx<R>* buf1 = buf0 + (dbuf ? PT : 0);
-  int64_t* hoff = reinterpret_cast<int64_t*>(smem + (size_t)(dbuf ? 2 : 1) * PT * sizeof(cplx<R>));
-  ROp<R>* rops = reinterpret_cast<ROp<R>*>(reinterpret_cast<unsigned char*>(hoff) + staged_hoff_bytes(P.t, P.nlow));
-  build_hoff(hoff, P);
-  // the pass's compiled op records (k_rops_compile, once per program run)
-  const int op0 = stages[P.op_begin].op_begin;
-  const int nwords = (stages[P.op_end - 1].op_end - op0) * (int)(sizeof(ROp<R>) / 16);
-  const uint4* src = reinterpret_cast<const uint4*>(rops_g + op0);
-  uint4* dst = reinterpret_cast<uint4*>(rops);
-  for (int w = threadIdx.x; w < nwords; w += blockDim.x) dst[w] = __ldg(&src[w]);
-  __syncthreads();
-  const int64_t ntiles = int64_t(1) << (n - P.t);
-  int64_t g = blockIdx.x;
-  if (g < ntiles) staged_issue_load<R>(buf0, psi, tile_base(g, P), hoff, P);
-  cp_async_commit();
-  int cur = 0;
-  for (; g < ntiles; g += gridDim.x) {
-    const int64_t gn = g + gridDim.x;
-    cplx<R>* s = cur ? buf1 : buf0;
-    if (dbuf) {
-      if (gn < ntiles) staged_issue_load<R>(cur ? buf0 : buf1, psi, tile_base(gn, P), hoff, P);
-      cp_async_commit();
-      cp_async_wait_group<1>();
-    } else {
-      cp_async_wait_group<0>();
-    }
-    __syncthreads();
-    const uint64_t gbase = (uint64_t)tile_base(g, P);
-    body(s, rops, gbase);
-    staged_store<R>(s, psi, (int64_t)gbase, hoff, P);
-    __syncthreads();
-    if (!dbuf && gn < ntiles) {
-      staged_issue_load<R>(buf0, psi, tile_base(gn, P), hoff, P);
-      cp_async_commit();
     }
     cur ^= dbuf;
   }
