@@ -426,11 +426,6 @@ def pack_ops(fields: list) -> np.ndarray:
     return arr
 
 
-def encode_op(rec, g: Gate, loc: dict, **kw) -> None:
-    """Fill one tq_tile_op record (see op_fields)."""
-    rec[...] = pack_ops([op_fields(g, loc, **kw)])[0]
-
-
 @dataclass
 class EncodedTiles:
     passes: ctypes.Array
