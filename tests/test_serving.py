@@ -289,3 +289,26 @@ def test_coalesced_small_requests_match_the_oracle():
             np.testing.assert_allclose(r.gradient, g_ref, atol=1e-4)
         else:
             assert r.gradient is None
+
+
+def test_table_arena_appends_grows_and_keeps_retired_buffers():
+    """The micro-batch table arena (host and device copies, device "cpu" here):
+    appends return consecutive offsets, growth doubles the capacity, keeps the
+    contents and hands the replaced device buffer to the retired list."""
+    from tyxonq_gb300.coalesce import _Arena
+    from tyxonq_gb300.hamiltonian import TERM_DTYPE
+
+    ar = _Arena(TERM_DTYPE, torch.device("cpu"), capacity=4)
+    retired = []
+    a = np.zeros(3, dtype=TERM_DTYPE)
+    a["zy"] = [1, 2, 3]
+    b = np.zeros(4, dtype=TERM_DTYPE)
+    b["zy"] = [4, 5, 6, 7]
+    assert ar.append(a, retired) == 0 and retired == []
+    old = ar.dev
+    assert ar.append(b, retired) == 3
+    assert len(retired) == 1 and retired[0] is old and len(ar.host) == 8
+    dev = np.frombuffer(ar.dev.numpy().tobytes(), dtype=TERM_DTYPE)
+    assert list(dev["zy"][:7]) == [1, 2, 3, 4, 5, 6, 7]
+    assert list(ar.host["zy"][:7]) == [1, 2, 3, 4, 5, 6, 7]
+    assert ar.append(np.zeros(0, dtype=TERM_DTYPE), retired) == 7 and ar.size == 7
