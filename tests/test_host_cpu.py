@@ -656,3 +656,62 @@ def test_tile_group_order_keeps_partner_runs_and_groups_one_term_classes():
         one = run["n_terms"] == 1
         cls = np.where(one, (t["zy"][run["first_term"]] >> np.uint64(8)) & np.uint64(15), 16).astype(np.int64)
         assert (np.diff(cls) >= 0).all()
+
+
+def test_parametrised_program_with_commuted_diagonals_emulated_matches_oracle():
+    """compile_forward of a parametrised circuit (angles read from theta on the
+    device) reorders diagonal gates and remaps the parameter table; the staged
+    program, emulated with the device-side angle formulas, gives the oracle's
+    state up to a global phase."""
+    import torch
+
+    from tyxonq_gb300.batch import structure_gates
+
+    n, depth = 10, 3
+    rng = np.random.default_rng(7)
+    struct = []
+    for layer in range(depth):
+        for q in range(n):
+            struct.append(("h", (q,), None))
+        for q in range(0, n - 1, 2 if layer % 2 else 1):
+            struct.append(("cz" if q % 3 else "cx", (q, q + 1), None))
+        for q in range(n):  # diagonals behind CZ / CX controls: moved back to the H of their qubit
+            struct.append(("rz", (q,), len(struct)))
+    # parameter indices 0, 1, ... in gate order
+    struct2, n_par = [], 0
+    for nm, qs, p in struct:
+        struct2.append((nm, qs, None if p is None else n_par))
+        n_par += p is not None
+    theta = rng.uniform(-3, 3, n_par)
+    gates, params = structure_gates(struct2)
+    order = P.commute_diagonals([P._canon(g) for g in gates])
+    assert order != list(range(len(gates)))  # the diagonals do move here
+    prog = P.compile_forward(gates, n, torch.complex128, t=9, params=params)
+    psi = sv.init_state(n)
+    for kind, enc in prog.segments:
+        assert kind == "staged"
+        psi = psi.copy()
+        for pi in range(enc.n_passes):
+            pa = enc.passes[pi]
+            t = pa.t
+            pos = [pa.pos[j] for j in range(t)]
+            nonloc = [b for b in range(n) if b not in pos]
+            for g in range(1 << (n - t)):
+                base = sum(((g >> k) & 1) << b for k, b in enumerate(nonloc))
+                idx = np.array([base + sum(((j >> k) & 1) << pos[k] for k in range(t)) for j in range(1 << t)])
+                s = psi[idx]
+                for st in enc.stages_host[pa.op_begin:pa.op_end]:
+                    bits = [int(b) for b in st["bits"]]
+                    rest = [b for b in range(t) if b not in bits]
+                    for tid in range(1 << (t - 4)):
+                        b0 = sum(((tid >> k) & 1) << b for k, b in enumerate(rest))
+                        ridx = np.array([b0 + sum(((i >> k) & 1) << bits[k] for k in range(4)) for i in range(16)])
+                        v = s[ridx]
+                        for o in enc.ops_host[st["op_begin"]:st["op_end"]]:
+                            v = _op_matrix_local(o, theta, 4) @ v if o["pidx"] >= 0 else \
+                                _apply_local(v, o, 4, _zs(o, base, b0))
+                        s[ridx] = v
+                psi[idx] = s
+    ops = [(nm, *qs) if p is None else (nm, *qs, float(theta[p])) for nm, qs, p in struct2]
+    ref, _ = sv.run_ops(n, ops, mode="run")
+    assert abs(abs(np.vdot(ref, psi)) - 1.0) < 1e-10
