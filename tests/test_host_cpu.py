@@ -715,3 +715,26 @@ def test_parametrised_program_with_commuted_diagonals_emulated_matches_oracle():
     ops = [(nm, *qs) if p is None else (nm, *qs, float(theta[p])) for nm, qs, p in struct2]
     ref, _ = sv.run_ops(n, ops, mode="run")
     assert abs(abs(np.vdot(ref, psi)) - 1.0) < 1e-10
+
+
+@pytest.mark.parametrize("ops,routine", [
+    ([("h", 9), ("ry", 9, 0.3)], "j_ureal<"),  # real factors: a real 2x2
+    ([("rz", 9, 0.2), ("s", 9)], "r_d1<"),  # diagonal factors: a diagonal
+    ([("rx", 9, 0.4)], "r_ri<"),  # c I - i s X
+    ([("h", 9), ("rz", 9, 0.7)], "r_u1<"),  # a complex diagonal times a real matrix: general
+])
+def test_specialised_routine_follows_the_factors_shapes(ops, routine):
+    """The generated pass body applies a run of single-qubit ops on one register
+    bit with the cheapest routine its factors allow (register-routine choice of
+    the circuit-specialised kernels)."""
+    import torch
+
+    from tyxonq_gb300 import jit as J
+
+    n = 10
+    gates, _ = lower_ops(_C(n, ops), mode="run")
+    prog = P.compile_forward(gates, n, torch.complex64, t=9)
+    enc = [o for k, o in prog.segments if k == "staged"][0]
+    body = "\n".join(J._pass_body(enc.stages_host, enc.ops_host, enc.passes[0], False))
+    names = set(re.findall(r"([a-z_0-9]+<)R, NR", body))
+    assert names == {routine}, names

@@ -108,8 +108,6 @@ def _shape2(o, double: bool) -> str | None:
             return "diag"
         return "real" if all(v.imag == 0 for v in m) else "dense"
     if kind == TOP_D1:
-        if int(o["pidx"]) >= 0:
-            return "diag"
         return "diag"
     if kind == TOP_PROT:
         xm, zm = int(o["xm"]) & 15, int(o["zm"]) & 15
