@@ -187,6 +187,20 @@ def _ref_one(arg):
 
 
 # ------------------------------------------------------------------ our arm
+def _schedule_fields(sched) -> dict:
+    """The complex64 batched schedule's fields and where they came from (the
+    autotuned file for this GPU, or the builtin defaults)."""
+    from dataclasses import asdict
+
+    import torch
+
+    from tyxonq_gb300.autotune import SCHEDULE_FIELDS, load_schedule, schedule_path
+
+    out = {k: v for k, v in asdict(sched).items() if k in SCHEDULE_FIELDS}
+    out["source"] = str(schedule_path().name) if load_schedule(torch.complex64) else "builtin"
+    return out
+
+
 def _events():
     import torch
 
@@ -810,7 +824,7 @@ def main():
                                "50-500 random Pauli terms (weight 1-4, N(0,1)), energy + adjoint gradient",
                    "l2": "512 MiB buffer written between timed steps", "graph": "CUDA graph replay",
                    "classes": {c.name: len(c.work) for c in bv.launch_order}, "structures": bv.n_structures,
-                   "build_s": build_s},
+                   "build_s": build_s, "schedule": _schedule_fields(bv.sched)},
         "plain_gpu": {"value": plain_evals, "unit": "evals/s",
                       "sample": f"{len(sample)} of {len(insts)} (every 16th), each evaluation a replayed CUDA graph "
                                 "of one launch per gate",
