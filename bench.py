@@ -197,7 +197,10 @@ def _schedule_fields(sched) -> dict:
     from tyxonq_gb300.autotune import SCHEDULE_FIELDS, load_schedule, schedule_path
 
     out = {k: v for k, v in asdict(sched).items() if k in SCHEDULE_FIELDS}
-    out["source"] = str(schedule_path().name) if load_schedule(torch.complex64) else "builtin"
+    try:
+        out["source"] = str(schedule_path().name) if load_schedule(torch.complex64) else "builtin"
+    except (OSError, ValueError, RuntimeError) as e:  # the report line must not fail on this field
+        out["source"] = f"unknown ({type(e).__name__})"
     return out
 
 
