@@ -18,6 +18,7 @@ instances with the same structure; angles are read from theta on the device.
 from __future__ import annotations
 
 import ctypes
+import warnings
 from collections import defaultdict
 
 import numpy as np
@@ -234,7 +235,13 @@ class WavePlan:
         self.rops_buf = torch.empty(max(int(nat.load().tq_jit_rops_bytes(self.dt, n_rec)), 16), dtype=torch.uint8,
                                     device=device)
         if jit and items:
-            self._specialise(items, device)
+            try:
+                self._specialise(items, device)
+            except (nat.TqError, OSError) as e:
+                # a runtime compilation that fails leaves every item on the library's
+                # interpreting kernels: the same results, slower
+                warnings.warn(f"specialised wave kernels unavailable, interpreting kernels used: {e}")
+                self.jit_sub, self.jit_kernels, self.jit_bodies = {}, {}, 0
         pool_base = np.concatenate([[0], np.cumsum(lane_pool)]).astype(np.int64)
         part_base = np.concatenate([[0], np.cumsum(lane_part)]).astype(np.int64)
         pool_need, part_need = int(pool_base[-1]), int(part_base[-1])
