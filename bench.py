@@ -291,6 +291,15 @@ def bench_gate_kernels(args, dev):
         else:
             del pr
     spec_build_s = time.perf_counter() - t0
+    if best is None:  # no combination compiled: report the interpreting kernel's passes
+        prog = compile_forward(gates, n2, torch.complex64, t=13, staged=True)
+        a, b = _events()
+        a.record(st)
+        prog.run(psi)
+        b.record(st)
+        torch.cuda.synchronize()
+        best = ("t13_interpreter", prog)
+        tile_ms["t13_interpreter"] = {"ms": a.elapsed_time(b), "passes": prog.n_passes}
     best_t, prog = best
     spec_total = tile_ms[best_t]["ms"]
     spec_pass = spec_total / prog.n_passes

@@ -555,19 +555,26 @@ class ForwardProgram:
         register stages (32 amplitudes per thread: fewer shared-memory sweeps
         per pass) where every pass takes a specialised kernel; 4-bit stages
         otherwise."""
+        import warnings
+
         from . import jit
 
         count = 0
         for si, (kind, obj) in enumerate(self.segments):
             if kind != "staged":
                 continue
-            if obj.jit is None and stage_bits == 5 and obj.rb == STAGE_BITS:
-                wide = jit.specialise_wide(obj, dtype, device)
-                if wide is not None:
-                    self.segments[si] = (kind, wide)
-                    obj = wide
-            if obj.jit is None and obj.rb == STAGE_BITS:
-                obj.jit = jit.specialise(obj, dtype, device)
+            try:
+                if obj.jit is None and stage_bits == 5 and obj.rb == STAGE_BITS:
+                    wide = jit.specialise_wide(obj, dtype, device)
+                    if wide is not None:
+                        self.segments[si] = (kind, wide)
+                        obj = wide
+                if obj.jit is None and obj.rb == STAGE_BITS:
+                    obj.jit = jit.specialise(obj, dtype, device)
+            except (nat.TqError, OSError) as e:
+                # a runtime compilation that fails leaves the segment on the
+                # interpreting kernel: the same results, slower
+                warnings.warn(f"specialised pass kernels unavailable, interpreting kernel used: {e}")
             if obj.jit is not None:
                 count += obj.jit.n_kernels
         return count
