@@ -159,3 +159,24 @@ def test_tyxonq_chain_on_gpu_matches_reference_engine():
             assert abs(ez[k] - ez2[k]) < 1e-6, (nm, k)
         np.testing.assert_allclose(psi2, psi, atol=1e-6, err_msg=nm)
         np.testing.assert_allclose(ex2, ex, atol=1e-6)
+
+
+def test_engine_dtype_follows_tyxonq_set_dtype(monkeypatch):
+    """The engine's state dtype: its own argument, else TyxonQ's set_dtype choice
+    (an instance attribute of the numerics backend; the class default does not
+    count), else TYXONQ_GB300_DTYPE, else complex64."""
+    import torch
+
+    from tyxonq_gb300.engine import resolve_dtype
+
+    class _Backend:
+        dtypestr = "complex128"  # the class default of the reference backends
+
+    monkeypatch.delenv("TYXONQ_GB300_DTYPE", raising=False)
+    b = _Backend()
+    assert resolve_dtype(None, b) == torch.complex64  # nothing chosen
+    b.dtypestr = "complex128"  # what set_dtype("complex128") does
+    assert resolve_dtype(None, b) == torch.complex128
+    assert resolve_dtype("complex64", b) == torch.complex64  # the engine argument wins
+    monkeypatch.setenv("TYXONQ_GB300_DTYPE", "complex128")
+    assert resolve_dtype(None, _Backend()) == torch.complex128

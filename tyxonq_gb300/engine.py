@@ -46,6 +46,19 @@ def default_dtype() -> torch.dtype:
     return _DTYPES.get(os.environ.get("TYXONQ_GB300_DTYPE", "complex64"), torch.complex64)
 
 
+def resolve_dtype(dtype, backend) -> torch.dtype:
+    """State dtype of an engine: the engine's own argument, else a dtype the
+    program chose with TyxonQ's ``set_dtype`` (the backend instance then holds
+    its own ``dtypestr``, numerics/__init__.py:39-58; the class default does not
+    count), else ``TYXONQ_GB300_DTYPE``, else complex64."""
+    if dtype is not None:
+        return _DTYPES[dtype]
+    chosen = vars(backend).get("dtypestr") if hasattr(backend, "__dict__") else None
+    if chosen in _DTYPES:
+        return _DTYPES[chosen]
+    return default_dtype()
+
+
 class _TorchBackendStub:
     """Stand-in for the reference ArrayBackend when TyxonQ is not importable."""
 
@@ -95,7 +108,7 @@ class GpuStatevectorEngine:
     def __init__(self, backend_name: str | None = None, *, dtype=None, device=None, fusion: str | None = None,
                  seed: int | None = None, extended_gates: bool = False) -> None:
         self.backend = _resolve_backend(backend_name)
-        self.dtype = _DTYPES[dtype] if dtype is not None else default_dtype()
+        self.dtype = resolve_dtype(dtype, self.backend)
         self.device = torch.device(device if device is not None else "cuda")
         self.fusion = (fusion or os.environ.get("TYXONQ_GB300_FUSION", "fused")).lower()
         self.extended_gates = bool(extended_gates)
