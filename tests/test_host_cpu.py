@@ -738,3 +738,19 @@ def test_specialised_routine_follows_the_factors_shapes(ops, routine):
     body = "\n".join(J._pass_body(enc.stages_host, enc.ops_host, enc.passes[0], False))
     names = set(re.findall(r"([a-z_0-9]+<)R, NR", body))
     assert names == {routine}, names
+
+
+def test_fused_program_cache_keys_tell_circuits_apart():
+    """The engine's fused-program cache is keyed by every gate's kind, qubits,
+    matrix and angle: circuits that differ in one angle, one qubit or one gate
+    kind get different keys; the same circuit lowered twice gets the same key."""
+    def key(ops, n=4):
+        gates, _ = lower_ops(_C(n, ops), mode="run")
+        return tuple(P._gate_key(P._canon(g)) for g in gates)
+
+    base = [("h", 0), ("rx", 1, 0.3), ("cx", 0, 1), ("rz", 2, 0.7)]
+    assert key(base) == key(list(base))
+    assert key(base) != key([("h", 0), ("rx", 1, 0.30001), ("cx", 0, 1), ("rz", 2, 0.7)])
+    assert key(base) != key([("h", 0), ("rx", 2, 0.3), ("cx", 0, 1), ("rz", 2, 0.7)])
+    assert key(base) != key([("h", 0), ("ry", 1, 0.3), ("cx", 0, 1), ("rz", 2, 0.7)])
+    assert key(base) != key([("h", 0), ("rx", 1, 0.3), ("cz", 0, 1), ("rz", 2, 0.7)])
