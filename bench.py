@@ -187,6 +187,35 @@ def _ref_one(arg):
 
 
 # ------------------------------------------------------------------ our arm
+def _print_scaled_line(args, rank, world, value, ms, e2e, h2d, d2h, bv, insts, build_s, clk, waves_prof, l2_gbs):
+    """The report line of a multi-rank run (rank 0 prints): the headline over all
+    ranks (max step time over ranks), its e2e, the wave-phase roofline of rank 0;
+    the single-GPU sections (plain engine, gate kernels, small configurations,
+    serving, CPU baseline) belong to the one-GPU run."""
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": args.scaling,
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+        "config": {"workload": f"batched_vqe_{len(insts)} per rank" if args.scaling == "weak" else
+                   f"batched_vqe_{args.count} split over {world} ranks by estimated cost",
+                   "l2": "512 MiB buffer written between timed steps", "graph": "CUDA graph replay",
+                   "parallelism": f"{world} ranks, one GPU each, no data-path collective",
+                   "build_s": build_s, "schedule": _schedule_fields(bv.sched)},
+        "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"kernel": "tq_jit_wave_adjoint (rank 0)", "bound": "l2",
+                     "achieved": waves_prof["adjoint"]["gbs"] if "adjoint" in waves_prof else None,
+                     "peak": l2_gbs, "unit": "GB/s",
+                     "frac": waves_prof["adjoint"]["frac_of_l2_copy"] if "adjoint" in waves_prof else None,
+                     "traffic": WAVE_ADJ_DRAM_BYTES_PER_ITEM, "peak_kind": "measured in this run: L2-resident copy"},
+        "cpu_baseline": None,
+        "clocks": clk.summary(),
+        "gpu_launches": bv.kernel_launches() * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def _schedule_fields(sched) -> dict:
     """The complex64 batched schedule's fields and where they came from (the
     autotuned file for this GPU, or the builtin defaults)."""
@@ -739,6 +768,8 @@ def main():
 
     # ---------------- per-phase device time of the wave kernels (one evaluation, serialised on
     # one stream, CUDA events around every launch) against the measured L2 copy bandwidth
+    # (these per-GPU figures and the sections below them are taken on one GPU only: with
+    # several ranks the line reports the scaled headline and its e2e)
     waves_prof = bv.profile_waves()
     torch.cuda.synchronize()
     l2_gbs = measure_l2_copy_gbs()
@@ -771,6 +802,11 @@ def main():
     h2d = theta_host.numel() * 8
     d2h = (e_host.numel() + g_host.numel()) * 8
     energies = e_host.numpy().copy()
+
+    if world > 1:
+        _print_scaled_line(args, rank, world, value, ms, e2e, h2d, d2h, bv, insts, build_s, clk, waves_prof,
+                           l2_gbs)
+        return
 
     # ---------------- plain single-circuit engine on an every-16th-instance sample: one launch per
     # gate, each instance's evaluation captured once as a CUDA graph and replayed (GPU-bound)

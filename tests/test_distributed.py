@@ -103,3 +103,33 @@ def test_two_rank_gloo_strong_scaling_evaluation():
 def test_single_rank_passthrough(world):
     assert max_over_ranks(3.0) == 3.0
     np.testing.assert_array_equal(gather_results(np.array([1.0, 2.0])), [1.0, 2.0])
+
+
+def test_multi_rank_report_line(capsys):
+    """The report line of a multi-rank benchmark run: rank 0 prints one JSON
+    line with the scaled headline, e2e and the contract's keys; other ranks
+    print nothing."""
+    import json
+    import sys
+    from pathlib import Path
+    from types import SimpleNamespace
+
+    import torch
+
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench
+
+    from tyxonq_gb300.batch import Schedule
+
+    args = SimpleNamespace(steps=5, warmup=3, scaling="weak", count=4096)
+    bv = SimpleNamespace(sched=Schedule.builtin(torch.complex64), kernel_launches=lambda: 100)
+    clk = SimpleNamespace(summary=lambda: {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": [], "samples": 3})
+    prof = {"adjoint": {"gbs": 1200.0, "frac_of_l2_copy": 0.18}}
+    bench._print_scaled_line(args, 1, 2, 1.0, 2.0, 3.0, 8, 16, bv, [0] * 4096, 1.0, clk, prof, 6800.0)
+    assert capsys.readouterr().out == ""
+    bench._print_scaled_line(args, 0, 2, 35000.0, 234.0, 34900.0, 8, 16, bv, [0] * 4096, 1.0, clk, prof, 6800.0)
+    line = json.loads(capsys.readouterr().out.strip())
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "e2e", "roofline", "cpu_baseline", "clocks", "gpu_launches"):
+        assert k in line, k
+    assert line["n_gpus"] == 2 and line["value"] == 35000.0 and line["gpu_launches"] == 500
